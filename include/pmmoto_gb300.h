@@ -1,0 +1,215 @@
+/*
+ * pmmoto_gb300 -- C ABI of the GB300 voxel-morphology library.
+ *
+ * Conventions
+ *   - Arrays are C-ordered 3-D volumes (shape[0], shape[1], shape[2]);
+ *     2-D images use shape {1, n0, n1}.
+ *   - Array arguments are CUDA device pointers owned by the caller unless a
+ *     parameter is documented as a host pointer.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Work is
+ *     enqueued on it; functions that return host scalars synchronize it.
+ *   - Every function returns PMG_OK (0), a positive input error, or a
+ *     negative device error; pmg_last_error() describes the last failure on
+ *     the calling thread.  No exception crosses the ABI.
+ *
+ * Each entry point names the reference routine (PMMoTo v1.0.7, paths
+ * relative to its source tree) whose result it reproduces bit for bit.
+ */
+#ifndef PMMOTO_GB300_H
+#define PMMOTO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PMG_OK 0
+#define PMG_EINVAL 1   /* bad shape, pointer or parameter */
+#define PMG_ERANGE 2   /* size beyond a documented limit */
+#define PMG_ECUDA (-1) /* CUDA runtime error */
+#define PMG_EITER (-2) /* a bounded device loop hit its iteration cap */
+
+/* Boundary kinds of one face (core/boundary_types.py:11-17). */
+#define PMG_BC_END 0
+#define PMG_BC_WALL 1
+#define PMG_BC_PERIODIC 2
+
+/* Largest line length the envelope kernels accept. */
+#define PMG_MAX_LINE 8192
+
+/*
+ * Per-axis rules for importing periodic information into one EDT pass.
+ *   periodic      the axis wraps
+ *   Axis of the linear pass (correctors):
+ *     F = first zero voxel in [f_lo, n), L = last zero voxel in
+ *     [l_lo, n - l_hi); upper corrector = F + a_u, lower corrector =
+ *     n - L + a_l (infinite when no zero exists).
+ *   Axes of the envelope passes (boundary hulls):
+ *     the near-end hull segment search skips hf_lo voxels at the low end,
+ *     the far-end search skips hb_hi voxels at the high end.
+ * edt3d / edt2d use {p, 0, 0, 0, 1, 0, 0, 0}; the padded-subdomain EDT with
+ * pads (lo, hi) uses {p, 2lo, 2lo, 2hi, -lo, -hi-1, 2lo, 2hi}
+ * (filters/distance/euclidean_distance_transform.py:56-101, 306-528).
+ */
+typedef struct pmg_axis_cfg {
+    int32_t periodic, f_lo, l_lo, l_hi, a_u, a_l, hf_lo, hb_hi;
+} pmg_axis_cfg;
+
+/* Output forms of the EDT entry points. */
+#define PMG_EDT_SQUARED 0 /* float32 squared distance */
+#define PMG_EDT_DIST 1    /* float32 sqrt of it (np.sqrt on float32) */
+#define PMG_EDT_MORPH 2   /* internal: fused threshold of the morphology ops */
+
+/*
+ * Squared/plain Euclidean distance transform of a uint8 volume: zeros are
+ * the "solid" voxels, distinct nonzero values restart the linear pass.
+ * Pass order and arithmetic follow edt3d (euclidean_distance_transform.py:
+ * 208-303) with `cfg` as above; replaces the Python/Cython driver loops
+ * _distance.pyx:86-127, 308-353, 544-618 and the kernels
+ * squared_edt_1d / squared_edt_1d_parabolic / return_boundary_hull
+ * (_distance.hpp:135-356).  num_hull is the reference's hull count (4).
+ */
+int pmg_edt3d(const uint8_t *img, float *out, const int64_t shape[3],
+              const float res[3], const pmg_axis_cfg cfg[3], int32_t num_hull,
+              int32_t form, void *stream);
+
+/*
+ * edt2d (euclidean_distance_transform.py:104-205): linear pass along axis 1,
+ * envelope along axis 0.  img/out hold shape2[0]*shape2[1] values.
+ */
+int pmg_edt2d(const uint8_t *img, float *out, const int64_t shape2[2],
+              const float res[2], const int32_t periodic[2], int32_t num_hull,
+              int32_t form, void *stream);
+
+/*
+ * Morphological addition (dilate != 0) or subtraction of a padded
+ * single-rank subdomain image by the EDT path: addition / subtraction
+ * (filters/morphological_operators.py:103-228) with the halo extension of
+ * update_extended_buffer (core/communication.py:121-157).
+ *   bc[2d], bc[2d+1]   boundary kind of the low / high face of axis d
+ *   pad[2d], pad[2d+1] padding of the subdomain on those faces
+ *   ext[2d], ext[2d+1] extension of those faces (ceil(r/res) on periodic
+ *                      faces; ignored elsewhere)
+ *   res                voxel size, float32 as the reference passes it
+ *   radius, cmp64      compare sqrt(d2) <= radius in float64 when cmp64 is
+ *                      1 (a numpy float64 radius) or in float32 when 0 (a
+ *                      Python float radius, numpy's weak-scalar rule)
+ * img and out have the padded shape; out gets 0/1 with wall planes 0.
+ */
+int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3],
+              const int32_t bc[6], const int32_t pad[6], const int32_t ext[6],
+              const float res[3], double radius, int32_t cmp64, int32_t dilate,
+              void *stream);
+
+/*
+ * Connected components of a padded single-rank subdomain image (elements of
+ * elem_bytes = 1, 2, 4 or 8 bytes, compared by value): 26-connectivity, every
+ * nonzero value labelled separately, background 0 -- the call of
+ * connect_components (filters/connected_components.py:32-62) to the
+ * third-party cc3d, numbered 1..N in order of first voxel in C-order scan --
+ * followed, when an axis is periodic, by the reference's seam merge and
+ * renumbering (connect_subdomain_boundaries :65-101, core/voxels.py:167-397,
+ * core/_voxels.pyx:335-383, 548-579).  labels: uint64, padded shape.
+ * *count (host) receives the label count the reference returns.
+ */
+int pmg_cc_label(const void *img, int32_t elem_bytes, uint64_t *labels,
+                 const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],
+                 int64_t *count, void *stream);
+
+/* Selection modes of pmg_cc_select. */
+#define PMG_SEL_INLET 1    /* inlet_connected_img  (connected_components.py:254-296) */
+#define PMG_SEL_OUTLET 2   /* outlet_connected_img (:299-341) */
+#define PMG_SEL_BOTH 3     /* inlet_outlet_connected_img (:203-251) */
+#define PMG_SEL_ISOLATED 4 /* isolated_img (:344-392) */
+
+/*
+ * Keep the voxels of `img` (uint8, padded shape) whose component (periodic
+ * seams merged) touches the inlet and/or outlet face slab, as `mode` says;
+ * phase >= 0 keeps only voxels of that value.  out receives the kept value
+ * or 0, as uint8 (out_bytes 1) or uint64 (8).  inlet_box / outlet_box are
+ * {lo0, hi0, lo1, hi1, lo2, hi2} own-slab boxes of the face flagged inlet /
+ * outlet (the last such face in face order, core/voxels.py:400-454), or NULL
+ * / lo0 < 0 when the subdomain has none.
+ */
+int pmg_cc_select(const uint8_t *img, void *out, int32_t out_bytes,
+                  const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],
+                  const int64_t inlet_box[6], const int64_t outlet_box[6],
+                  int32_t mode, int32_t phase, void *stream);
+
+/*
+ * Sphere voxelisation of a padded grid (gen_sphere_img_brute_force,
+ * domain_generation/domain_generation.hpp:91-127, with Sphere::contains,
+ * particles/spheres.hpp:41-48): img = 1, then 0 where a voxel centre lies in
+ * any sphere, tested in float64 as (dx*dx + dy*dy + dz*dz) <= r*r.
+ * spheres: nsph rows of (x, y, z, r) float64 (device); cx/cy/cz: voxel-centre
+ * coordinates of the three axes (device, the subdomain's linspace coords);
+ * grid_c0 / grid_h (host): first centre and spacing per axis, used only to
+ * bound the voxels each sphere can reach.
+ */
+int pmg_spheres(const double *spheres, int64_t nsph, const double *cx,
+                const double *cy, const double *cz, const double grid_c0[3],
+                const double grid_h[3], uint8_t *img, const int64_t shape[3],
+                void *stream);
+
+/*
+ * update_buffer on one rank (core/communication.py:101-118): halo voxels of
+ * periodic axes take the value of the own voxel they copy; wall planes are
+ * set to 0.  elem_bytes 1 (uint8), 4 (float32) or 8 (uint64), in place.
+ */
+int pmg_update_buffer(void *img, int32_t elem_bytes, const int64_t shape[3],
+                      const int32_t bc[6], const int32_t pad[6], void *stream);
+
+/* Number of uint8 voxels equal to `value` in box {lo0,hi0,lo1,hi1,lo2,hi2}
+   (np.count_nonzero(img == value) of that region); *count is a host pointer. */
+int pmg_count_eq(const uint8_t *img, const int64_t shape[3], const int64_t box[6],
+                 int32_t value, int64_t *count, void *stream);
+
+/* Maximum of a float32 volume over a box (np.amax); *out is a host pointer. */
+int pmg_max_f32(const float *x, const int64_t shape[3], const int64_t box[6],
+                float *out, void *stream);
+
+/*
+ * porosimetry (filters/porosimetry.py:84-160) with mode="distance": erode
+ * pm_img by r_erode, keep the inlet-connected part when `inlet`, and if any
+ * voxel is left, constrain by the inlet-connected phase 1 of mp_img (when
+ * mp_img is not NULL and holds phase 1) and dilate by r_dilate.  ratio_* are
+ * ceil(radius/res) per axis (gen_struct_ratio); cmp_* as in pmg_morph.
+ */
+int pmg_porosimetry(const uint8_t *pm_img, const uint8_t *mp_img, uint8_t *out,
+                    const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],
+                    const int64_t inlet_box[6], const float res[3], double r_erode,
+                    int32_t cmp_erode, const int32_t ratio_erode[3], double r_dilate,
+                    int32_t cmp_dilate, const int32_t ratio_dilate[3], int32_t inlet,
+                    void *stream);
+
+/*
+ * drainage, standard method (filters/equilibrium_distribution.py:25-179)
+ * with mode="distance", on the device.  For each of n_radii probe radii
+ * (float64, host array, in capillary-pressure order): when active[k] the
+ * porosimetry step above with the inlet and multiphase constraints, else an
+ * empty morph; then the outlet-connected phase 2 of mp_img, the update
+ * mp = (morph == 1 && connected == 2) ? 1 : mp, the reservoir refill
+ * (rpad slabs set to 1) and counts[k] (host) = number of own voxels (own_box)
+ * equal to 2 -- the numerator of Multiphase.get_saturation.  mp_img (device)
+ * is updated in place; ratios holds ceil(r/res) per axis per radius.
+ */
+int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
+                 const int32_t bc[6], const int32_t pad[6], const int32_t rpad[6],
+                 const int64_t own_box[6], const int64_t inlet_box[6],
+                 const int64_t outlet_box[6], const float res[3], int32_t n_radii,
+                 const double *radii, const int32_t *active, const int32_t *ratios,
+                 int64_t *counts, void *stream);
+
+/* Message of the last failure on this host thread (empty if none). */
+int pmg_last_error(char *buf, size_t len);
+
+/* Library version and build information. */
+const char *pmg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PMMOTO_GB300_H */

@@ -1,0 +1,907 @@
+// Connected components on GB300 (sm_103a).
+//
+// Reference: pmmoto.filters.connected_components (src/pmmoto/filters/
+// connected_components.py:32-392) -- labelling by the third-party cc3d
+// (26-connectivity, each nonzero value separately, background 0), periodic
+// seam merge (connect_subdomain_boundaries :65-101 with core/voxels.py:
+// 167-397 and core/_voxels.pyx:335-383, 548-579), inlet/outlet selection
+// (:144-392, voxels.py:400-454).
+//
+// Device algorithm: lock-free union-find over voxel indices where a union
+// always links the larger root under the smaller, so a component's final root
+// is its smallest voxel index -- its first voxel in C-order raster scan.
+// Numbering components by the rank of their root therefore numbers them in
+// order of first appearance, the order cc3d issues labels.  Each voxel unites
+// with one representative of every 26-connected group of equal-valued
+// already-scanned neighbours (13 candidates), which removes most redundant
+// unions.  Periodic seams are united voxel-with-twin (the voxel its halo
+// copies), which is what the reference's pair matching does.
+//
+// Every data-dependent loop carries an iteration cap; hitting it sets a
+// device status word and the entry point returns PMG_EITER.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <array>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "pmg_common.cuh"
+
+namespace pmg {
+
+constexpr int kFindCap = 1 << 24;
+constexpr int kUniteCap = 1 << 20;
+
+struct Vol3 {
+    long long s0, s1, s2;
+};
+
+__device__ __forceinline__ int ld(const int *p) { return __ldcg(p); }
+
+__device__ __forceinline__ int find_root(const int *P, int x, int *err)
+{
+    int p = ld(P + x);
+    int it = 0;
+    while (p != x) {
+        x = p;
+        p = ld(P + x);
+        if (++it > kFindCap) {
+            atomicExch(err, 1);
+            break;
+        }
+    }
+    return x;
+}
+
+// Playne-Hawick union (atomicMin links the larger root under the smaller).
+__device__ __forceinline__ void unite(int *P, int a, int b, int *err)
+{
+    for (int it = 0; it < kUniteCap; it++) {
+        a = find_root(P, a, err);
+        b = find_root(P, b, err);
+        if (a == b)
+            return;
+        if (a < b) {
+            int old = atomicMin(P + b, a);
+            if (old == b)
+                return;
+            b = old;
+        } else {
+            int old = atomicMin(P + a, b);
+            if (old == a)
+                return;
+            a = old;
+        }
+    }
+    atomicExch(err, 2);
+}
+
+// The 13 already-scanned neighbours (C order) and their mutual 26-adjacency.
+__constant__ int c_nb[13][3];
+__constant__ unsigned short c_adj[13];
+
+static void host_tables(int nb[13][3], unsigned short adj[13])
+{
+    int n = 0;
+    for (int di = -1; di <= 0; di++)
+        for (int dj = -1; dj <= 1; dj++)
+            for (int dk = -1; dk <= 1; dk++) {
+                if (di == 0 && (dj > 0 || (dj == 0 && dk >= 0)))
+                    continue;
+                nb[n][0] = di;
+                nb[n][1] = dj;
+                nb[n][2] = dk;
+                n++;
+            }
+    for (int a = 0; a < 13; a++) {
+        adj[a] = 0;
+        for (int b = 0; b < 13; b++) {
+            if (a == b)
+                continue;
+            if (abs(nb[a][0] - nb[b][0]) <= 1 && abs(nb[a][1] - nb[b][1]) <= 1 &&
+                abs(nb[a][2] - nb[b][2]) <= 1)
+                adj[a] |= (unsigned short)(1u << b);
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_cc_init(const T *__restrict__ img, int *__restrict__ P, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        P[i] = img[i] != 0 ? (int)i : -1;
+}
+
+template <typename T>
+__global__ void k_cc_merge(const T *__restrict__ img, int *P, Vol3 V, int *err)
+{
+    const long long n = V.s0 * V.s1 * V.s2;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const T v = img[idx];
+        if (v == 0)
+            continue;
+        const long long k = idx % V.s2;
+        const long long r = idx / V.s2;
+        const long long j = r % V.s1;
+        const long long i = r / V.s1;
+        unsigned same = 0;
+#pragma unroll
+        for (int q = 0; q < 13; q++) {
+            const long long a = i + c_nb[q][0], b = j + c_nb[q][1], c = k + c_nb[q][2];
+            if (a < 0 || b < 0 || c < 0 || b >= V.s1 || c >= V.s2)
+                continue;
+            if (img[(a * V.s1 + b) * V.s2 + c] == v)
+                same |= 1u << q;
+        }
+        unsigned covered = 0;
+        while (same & ~covered) {
+            const int q = __ffs(same & ~covered) - 1;
+            const long long a = i + c_nb[q][0], b = j + c_nb[q][1], c = k + c_nb[q][2];
+            unite(P, (int)idx, (int)((a * V.s1 + b) * V.s2 + c), err);
+            // everything 26-connected to q inside `same` is united through q
+            unsigned grp = 1u << q, prev = 0;
+            while (grp != prev) {
+                prev = grp;
+                unsigned g = grp;
+                while (g) {
+                    const int w = __ffs(g) - 1;
+                    g &= g - 1;
+                    grp |= c_adj[w] & same;
+                }
+            }
+            covered |= grp;
+        }
+    }
+}
+
+// Seam twins: every halo voxel of a periodic feature is united with the own
+// voxel it copies, when both are nonzero (the reference pairs labels without
+// comparing values, skipping zeros).
+struct Twins {
+    long long s0, s1, s2;
+    int periodic[3];
+    int own_lo[3], own_len[3];
+};
+
+template <typename T>
+__global__ void k_cc_twins(const T *__restrict__ img, int *P, Twins W, int *err)
+{
+    const long long n = W.s0 * W.s1 * W.s2;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        long long c[3];
+        c[2] = idx % W.s2;
+        long long r = idx / W.s2;
+        c[1] = r % W.s1;
+        c[0] = r / W.s1;
+        bool halo = false;
+        long long t[3];
+        bool ok = true;
+        for (int d = 0; d < 3; d++) {
+            t[d] = c[d];
+            const long long S = d == 0 ? W.s0 : d == 1 ? W.s1 : W.s2;
+            const bool in_halo = c[d] < W.own_lo[d] || c[d] >= W.own_lo[d] + W.own_len[d];
+            if (in_halo) {
+                if (!W.periodic[d] || W.own_len[d] <= 0 || c[d] < 0 || c[d] >= S) {
+                    ok = false;
+                } else {
+                    long long q = (c[d] - W.own_lo[d]) % W.own_len[d];
+                    if (q < 0)
+                        q += W.own_len[d];
+                    t[d] = q + W.own_lo[d];
+                    halo = true;
+                }
+            }
+        }
+        if (!halo || !ok || img[idx] == 0)
+            continue;
+        const long long tw = (t[0] * W.s1 + t[1]) * W.s2 + t[2];
+        if (img[tw] != 0)
+            unite(P, (int)idx, (int)tw, err);
+    }
+}
+
+__global__ void k_cc_flatten(int *P, long long n, int *err)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int p = P[i];
+        if (p >= 0 && p != i)
+            P[i] = find_root(P, p, err);
+    }
+}
+
+// ---- numbering by root order -------------------------------------------
+constexpr int kNumBlock = 512;
+constexpr int kNumItems = 4; // voxels per thread in the numbering kernels
+constexpr long long kNumTile = (long long)kNumBlock * kNumItems;
+
+__global__ void k_root_count(const int *__restrict__ P, long long n, int *__restrict__ counts)
+{
+    typedef cub::BlockReduce<int, kNumBlock> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const long long base = blockIdx.x * kNumTile;
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < kNumItems; q++) {
+        const long long i = base + (long long)threadIdx.x * kNumItems + q;
+        if (i < n && P[i] == (int)i)
+            c++;
+    }
+    const int tot = BR(tmp).Sum(c);
+    if (threadIdx.x == 0)
+        counts[blockIdx.x] = tot;
+}
+
+// R[i] = rank of root i among all roots (0-based); P is left unchanged.
+__global__ void k_root_rank(const int *__restrict__ P, long long n, const int *__restrict__ offs,
+                            int *__restrict__ R)
+{
+    typedef cub::BlockScan<int, kNumBlock> BS;
+    __shared__ typename BS::TempStorage tmp;
+    const long long base = blockIdx.x * kNumTile;
+    int f[kNumItems];
+#pragma unroll
+    for (int q = 0; q < kNumItems; q++) {
+        const long long i = base + (long long)threadIdx.x * kNumItems + q;
+        f[q] = (i < n && P[i] == (int)i) ? 1 : 0;
+    }
+    int x[kNumItems];
+    BS(tmp).ExclusiveSum(f, x);
+#pragma unroll
+    for (int q = 0; q < kNumItems; q++) {
+        const long long i = base + (long long)threadIdx.x * kNumItems + q;
+        if (f[q])
+            R[i] = offs[blockIdx.x] + x[q];
+    }
+}
+
+__global__ void k_label_out(const int *__restrict__ P, const int *__restrict__ R, long long n,
+                            uint64_t *__restrict__ L)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int p = P[i];
+        L[i] = p < 0 ? 0ull : (uint64_t)R[p] + 1ull;
+    }
+}
+
+// ---- seam pairs for the reference's periodic numbering --------------------
+struct Box {
+    long long lo[3], hi[3];
+    __host__ __device__ long long size() const
+    {
+        return (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
+    }
+};
+
+// keys[r] = label(own/neighbour voxel r) << 32 | label(twin), rows in the
+// reference's order: own slab then neighbour slab of the feature, each
+// flattened in C order, paired with the opposite feature's neighbour then own.
+__global__ void k_seam_pairs(const uint64_t *__restrict__ L, Vol3 V, Box a0, Box a1, Box b0, Box b1,
+                             uint64_t *__restrict__ keys, uint32_t *__restrict__ idx)
+{
+    const long long n0 = a0.size(), n = n0 + a1.size();
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
+         r += (long long)gridDim.x * blockDim.x) {
+        const Box &A = r < n0 ? a0 : a1;
+        const Box &B = r < n0 ? b0 : b1;
+        const long long q = r < n0 ? r : r - n0;
+        const long long wa = A.hi[2] - A.lo[2], ha = A.hi[1] - A.lo[1];
+        const long long wb = B.hi[2] - B.lo[2], hb = B.hi[1] - B.lo[1];
+        const long long ak = q % wa, aj = (q / wa) % ha, ai = q / (wa * ha);
+        const long long bk = q % wb, bj = (q / wb) % hb, bi = q / (wb * hb);
+        const uint64_t la = L[((A.lo[0] + ai) * V.s1 + A.lo[1] + aj) * V.s2 + A.lo[2] + ak];
+        const uint64_t lb = L[((B.lo[0] + bi) * V.s1 + B.lo[1] + bj) * V.s2 + B.lo[2] + bk];
+        keys[r] = (la << 32) | lb;
+        idx[r] = (uint32_t)r;
+    }
+}
+
+__global__ void k_head_flags(const uint64_t *__restrict__ k, long long n, uint8_t *__restrict__ f)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        f[i] = (i == 0 || k[i] != k[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_apply_lut(uint64_t *L, long long n, const uint64_t *__restrict__ lut)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        L[i] = lut[L[i]];
+}
+
+__global__ void k_lut_flags(const uint64_t *__restrict__ bl, const uint64_t *__restrict__ bg, long long nbnd,
+                            uint8_t *__restrict__ flag, uint64_t *__restrict__ lut)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nbnd;
+         i += (long long)gridDim.x * blockDim.x) {
+        flag[bl[i]] = 1;
+        lut[bl[i]] = bg[i];
+    }
+}
+
+__global__ void k_lut_nonflag(const uint8_t *__restrict__ flag, long long m, int *__restrict__ nf)
+{
+    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < m;
+         l += (long long)gridDim.x * blockDim.x)
+        nf[l] = (l > 0 && !flag[l]) ? 1 : 0;
+}
+
+__global__ void k_lut_fill(const uint8_t *__restrict__ flag, const int *__restrict__ rank, long long m,
+                           uint64_t start, uint64_t *__restrict__ lut)
+{
+    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < m;
+         l += (long long)gridDim.x * blockDim.x) {
+        if (l == 0)
+            lut[0] = 0;
+        else if (!flag[l])
+            lut[l] = start + (uint64_t)rank[l];
+    }
+}
+
+// ---- inlet / outlet selection ---------------------------------------------
+__global__ void k_mark_face(const int *__restrict__ P, Vol3 V, Box b, uint8_t *__restrict__ mark,
+                            uint8_t bit)
+{
+    const long long n = b.size();
+    const long long w = b.hi[2] - b.lo[2], h = b.hi[1] - b.lo[1];
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long k = q % w, j = (q / w) % h, i = q / (w * h);
+        const long long idx = ((b.lo[0] + i) * V.s1 + b.lo[1] + j) * V.s2 + b.lo[2] + k;
+        const int p = P[idx];
+        if (p >= 0 && !(mark[p] & bit))
+            atomicOr((unsigned int *)(mark + (p & ~3ll)), (unsigned int)bit << (8 * (p & 3)));
+    }
+}
+
+template <typename TO>
+__global__ void k_select(const uint8_t *__restrict__ img, const int *__restrict__ P,
+                         const uint8_t *__restrict__ mark, long long n, int mode, int phase,
+                         TO *__restrict__ out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const uint8_t v = img[i];
+        const int p = P[i];
+        TO o = 0;
+        if (v != 0 && p >= 0 && (phase < 0 || v == phase)) {
+            const uint8_t m = mark[p];
+            const bool in = m & 1, ou = m & 2;
+            bool keep;
+            if (mode == PMG_SEL_INLET)
+                keep = in;
+            else if (mode == PMG_SEL_OUTLET)
+                keep = ou;
+            else if (mode == PMG_SEL_BOTH)
+                keep = in && ou;
+            else
+                keep = !(in || ou);
+            if (keep)
+                o = (TO)v;
+        }
+        out[i] = o;
+    }
+}
+
+// ---------------------------------------------------------------------------
+static bool g_tables_ready[64] = {false};
+
+static int ensure_tables()
+{
+    int dev = 0;
+    PMG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && g_tables_ready[dev])
+        return PMG_OK;
+    int nb[13][3];
+    unsigned short adj[13];
+    host_tables(nb, adj);
+    PMG_CUDA(cudaMemcpyToSymbol(c_nb, nb, sizeof(nb)));
+    PMG_CUDA(cudaMemcpyToSymbol(c_adj, adj, sizeof(adj)));
+    if (dev >= 0 && dev < 64)
+        g_tables_ready[dev] = true;
+    return PMG_OK;
+}
+
+static Twins make_twins(const int64_t *shape, const int32_t *bc, const int32_t *pad)
+{
+    Twins W;
+    W.s0 = shape[0];
+    W.s1 = shape[1];
+    W.s2 = shape[2];
+    for (int d = 0; d < 3; d++) {
+        W.periodic[d] = bc[2 * d] == PMG_BC_PERIODIC;
+        W.own_lo[d] = pad[2 * d];
+        W.own_len[d] = (int)(shape[d] - pad[2 * d] - pad[2 * d + 1]);
+    }
+    return W;
+}
+
+static bool any_periodic(const int32_t *bc)
+{
+    return bc[0] == PMG_BC_PERIODIC || bc[2] == PMG_BC_PERIODIC || bc[4] == PMG_BC_PERIODIC;
+}
+
+// Union-find of a volume into P (roots = smallest index); twins optional.
+template <typename T>
+static int uf_build(const T *img, int *P, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, bool twins, int *err, cudaStream_t st)
+{
+    PMG_TRY(ensure_tables());
+    const long long n = shape[0] * shape[1] * shape[2];
+    Vol3 V{shape[0], shape[1], shape[2]};
+    const int block = 256;
+    k_cc_init<T><<<grid_for(n, block, 1LL << 30), block, 0, st>>>(img, P, n);
+    PMG_CHECK_LAUNCH();
+    k_cc_merge<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P, V, err);
+    PMG_CHECK_LAUNCH();
+    if (twins && any_periodic(bc)) {
+        k_cc_twins<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P,
+                                                                         make_twins(shape, bc, pad), err);
+        PMG_CHECK_LAUNCH();
+    }
+    k_cc_flatten<<<grid_for(n, block, 152LL * 32), block, 0, st>>>(P, n, err);
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+static int read_err(int *err, cudaStream_t st)
+{
+    int h = 0;
+    PMG_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PMG_CUDA(cudaStreamSynchronize(st));
+    if (h != 0) {
+        set_error("connected components: union-find iteration cap reached (code %d)", h);
+        return PMG_EITER;
+    }
+    return PMG_OK;
+}
+
+// Feature slabs (src/pmmoto/core/features.py:76-139) of a single-rank
+// padded subdomain; `kind` is the feature's boundary kind (boundary_order).
+static void feature_slabs(const int f[3], int kind, const int64_t *shape, const int32_t *pad,
+                          Box &own, Box &nb)
+{
+    bool padded = false;
+    for (int d = 0; d < 6; d++)
+        padded |= pad[d] != 0;
+    for (int d = 0; d < 3; d++) {
+        const long long L = shape[d], pb = pad[2 * d], pa = pad[2 * d + 1];
+        if (f[d] == -1) {
+            if (pb && kind != PMG_BC_WALL) {
+                own.lo[d] = pb;
+                own.hi[d] = 2 * pb;
+            } else if (pb) {
+                own.lo[d] = 1;
+                own.hi[d] = 2;
+            } else {
+                own.lo[d] = 0;
+                own.hi[d] = 1;
+            }
+            nb.lo[d] = 0;
+            nb.hi[d] = padded ? (kind == PMG_BC_WALL ? 1 : pb) : 0;
+        } else if (f[d] == 1) {
+            if (pa && kind != PMG_BC_WALL) {
+                own.lo[d] = L - 2 * pa;
+                own.hi[d] = L - pa;
+            } else if (pa) {
+                own.lo[d] = L - 2;
+                own.hi[d] = L - 1;
+            } else {
+                own.lo[d] = L - 1;
+                own.hi[d] = L;
+            }
+            nb.lo[d] = padded ? (kind == PMG_BC_WALL ? L - 1 : L - pa) : 0;
+            nb.hi[d] = padded ? L : 0;
+        } else {
+            own.lo[d] = pb;
+            own.hi[d] = L - pa;
+            nb.lo[d] = padded ? pb : 0;
+            nb.hi[d] = padded ? L - pa : 0;
+        }
+    }
+}
+
+// Features in the reference's iteration order (faces, edges, corners;
+// core/orientation.py:40-183).
+static std::vector<std::array<int, 3>> feature_order()
+{
+    std::vector<std::array<int, 3>> faces, edges, corners;
+    for (int a = -1; a <= 1; a++)
+        for (int b = -1; b <= 1; b++)
+            for (int c = -1; c <= 1; c++) {
+                const int s = abs(a) + abs(b) + abs(c);
+                if (s == 1)
+                    faces.push_back({a, b, c});
+                else if (s == 2)
+                    edges.push_back({a, b, c});
+            }
+    for (int a : {-1, 1})
+        for (int b : {-1, 1})
+            for (int c : {-1, 1})
+                corners.push_back({a, b, c});
+    std::vector<std::array<int, 3>> all = faces;
+    all.insert(all.end(), edges.begin(), edges.end());
+    all.insert(all.end(), corners.begin(), corners.end());
+    return all;
+}
+
+// Periodic renumbering of the reference (connect_subdomain_boundaries on one
+// rank): boundary pairs of every periodic feature, deduplicated on the device
+// in first-occurrence order, replayed through the same hash-set container the
+// reference uses so its iteration order is reproduced, then the dict / stack
+// merge of merge_matched_voxels and local_to_global_labeling on the host
+// (boundary data only), and one relabel pass on the device.
+static int periodic_renumber(uint64_t *L, const int64_t *shape, const int32_t *bc,
+                             const int32_t *pad, int64_t count, int64_t *out_count,
+                             cudaStream_t st)
+{
+    const long long n = shape[0] * shape[1] * shape[2];
+    Vol3 V{shape[0], shape[1], shape[2]};
+    auto feats = feature_order();
+    // insertion-ordered map (key label -> neighbour list), as a Python dict
+    std::vector<uint64_t> keys_order;
+    std::vector<std::vector<uint64_t>> nbrs;
+    std::unordered_map<uint64_t, long long> key_pos;
+    for (auto &f : feats) {
+        int fid[3] = {f[0], f[1], f[2]};
+        bool has_nb = true;
+        int kind = PMG_BC_PERIODIC;
+        for (int d = 0; d < 3; d++) {
+            if (fid[d] == 0)
+                continue;
+            const int b = bc[2 * d + (fid[d] > 0 ? 1 : 0)];
+            if (b != PMG_BC_PERIODIC)
+                has_nb = false;
+            if (b == PMG_BC_END)
+                kind = PMG_BC_END;
+            else if (b == PMG_BC_WALL && kind != PMG_BC_END)
+                kind = PMG_BC_WALL;
+        }
+        if (!has_nb)
+            continue;
+        int opp[3] = {-fid[0], -fid[1], -fid[2]};
+        Box own, nb, oown, onb;
+        feature_slabs(fid, kind, shape, pad, own, nb);
+        feature_slabs(opp, kind, shape, pad, oown, onb);
+        const long long rows = own.size() + nb.size();
+        if (rows == 0)
+            continue;
+        if (own.size() != onb.size() || nb.size() != oown.size()) {
+            set_error("periodic merge: mismatched feature slabs");
+            return PMG_EINVAL;
+        }
+        // device: keys in row order, stable radix sort by key, first row of
+        // every distinct key
+        uint64_t *d_k = nullptr, *d_k2 = nullptr, *d_k3 = nullptr;
+        uint32_t *d_i = nullptr, *d_i2 = nullptr;
+        uint8_t *d_f = nullptr;
+        int *d_nsel = nullptr;
+        PMG_TRY(scratch_alloc((void **)&d_k, rows * 8, st));
+        PMG_TRY(scratch_alloc((void **)&d_k2, rows * 8, st));
+        PMG_TRY(scratch_alloc((void **)&d_k3, rows * 8, st));
+        PMG_TRY(scratch_alloc((void **)&d_i, rows * 4, st));
+        PMG_TRY(scratch_alloc((void **)&d_i2, rows * 4, st));
+        PMG_TRY(scratch_alloc((void **)&d_f, rows, st));
+        PMG_TRY(scratch_alloc((void **)&d_nsel, 2 * sizeof(int), st));
+        k_seam_pairs<<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(L, V, own, nb, onb, oown, d_k,
+                                                                      d_i);
+        PMG_CHECK_LAUNCH();
+        size_t tb = 0, tb2 = 0, tb3 = 0;
+        PMG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, d_k, d_k2, d_i, d_i2, (int)rows, 0, 64, st));
+        PMG_CUDA(cub::DeviceSelect::Flagged(nullptr, tb2, d_i2, d_f, d_i, d_nsel, (int)rows, st));
+        PMG_CUDA(cub::DeviceSelect::Flagged(nullptr, tb3, d_k2, d_f, d_k3, d_nsel + 1, (int)rows, st));
+        size_t tbs = std::max(tb, std::max(tb2, tb3));
+        void *d_t = nullptr;
+        PMG_TRY(scratch_alloc(&d_t, tbs, st));
+        PMG_CUDA(cub::DeviceRadixSort::SortPairs(d_t, tbs, d_k, d_k2, d_i, d_i2, (int)rows, 0, 64, st));
+        k_head_flags<<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(d_k2, rows, d_f);
+        PMG_CHECK_LAUNCH();
+        PMG_CUDA(cub::DeviceSelect::Flagged(d_t, tbs, d_i2, d_f, d_i, d_nsel, (int)rows, st));
+        PMG_CUDA(cub::DeviceSelect::Flagged(d_t, tbs, d_k2, d_f, d_k3, d_nsel + 1, (int)rows, st));
+        int nsel = 0;
+        PMG_CUDA(cudaMemcpyAsync(&nsel, d_nsel, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PMG_CUDA(cudaStreamSynchronize(st));
+        std::vector<uint32_t> first((size_t)nsel);
+        std::vector<uint64_t> dkeys((size_t)nsel);
+        if (nsel > 0) {
+            PMG_CUDA(cudaMemcpyAsync(first.data(), d_i, (size_t)nsel * 4, cudaMemcpyDeviceToHost, st));
+            PMG_CUDA(cudaMemcpyAsync(dkeys.data(), d_k3, (size_t)nsel * 8, cudaMemcpyDeviceToHost, st));
+        }
+        PMG_CUDA(cudaStreamSynchronize(st));
+        PMG_TRY(scratch_free(d_t, st));
+        PMG_TRY(scratch_free(d_k, st));
+        PMG_TRY(scratch_free(d_k2, st));
+        PMG_TRY(scratch_free(d_k3, st));
+        PMG_TRY(scratch_free(d_i, st));
+        PMG_TRY(scratch_free(d_i2, st));
+        PMG_TRY(scratch_free(d_f, st));
+        PMG_TRY(scratch_free(d_nsel, st));
+        std::vector<size_t> order((size_t)nsel);
+        for (size_t q = 0; q < order.size(); q++)
+            order[q] = q;
+        std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return first[x] < first[y]; });
+        // unique_pairs (_voxels.hpp:106-125): the same container fed the same
+        // sequence of first insertions iterates in the same order (repeated
+        // keys are no-ops)
+        std::unordered_set<unsigned long> uset;
+        for (size_t q : order)
+            uset.insert((unsigned long)dkeys[q]);
+        for (unsigned long e : uset) {
+            const uint64_t a = e >> 32, b = e & 0xFFFFFFFFul;
+            if (a == 0 || b == 0)
+                continue;
+            // process_matches_by_feature (_voxels.pyx:548-579)
+            auto it = key_pos.find(a);
+            if (it == key_pos.end()) {
+                key_pos.emplace(a, (long long)keys_order.size());
+                keys_order.push_back(a);
+                nbrs.push_back({b});
+            } else {
+                auto &lst = nbrs[(size_t)it->second];
+                if (std::find(lst.begin(), lst.end(), b) == lst.end())
+                    lst.push_back(b);
+            }
+        }
+    }
+    // merge_matched_voxels (_voxels.pyx:335-383): stack walk in key order
+    std::vector<uint64_t> bl, bg;
+    std::vector<char> visited(keys_order.size(), 0);
+    uint64_t global_id = 1;
+    for (size_t s = 0; s < keys_order.size(); s++) {
+        if (visited[s])
+            continue;
+        std::vector<uint64_t> stack{keys_order[s]};
+        std::vector<uint64_t> conns;
+        while (!stack.empty()) {
+            const uint64_t cur = stack.back();
+            stack.pop_back();
+            auto it = key_pos.find(cur);
+            if (it == key_pos.end()) {
+                set_error("periodic merge: neighbour label without a key");
+                return PMG_EINVAL;
+            }
+            if (visited[(size_t)it->second])
+                continue;
+            visited[(size_t)it->second] = 1;
+            conns.push_back(cur);
+            for (uint64_t nbl : nbrs[(size_t)it->second]) {
+                auto jt = key_pos.find(nbl);
+                if (jt == key_pos.end()) {
+                    set_error("periodic merge: neighbour label without a key");
+                    return PMG_EINVAL;
+                }
+                if (!visited[(size_t)jt->second])
+                    stack.push_back(nbl);
+            }
+        }
+        for (uint64_t c : conns) {
+            if (c > (uint64_t)count) {
+                set_error("periodic merge: label out of range");
+                return PMG_EINVAL;
+            }
+            bl.push_back(c);
+            bg.push_back(global_id);
+        }
+        global_id += conns.empty() ? 0 : 1;
+    }
+    // local_to_global_labeling (core/voxels.py:344-397) on the device:
+    // boundary labels take their merged id, the others global_id, +1, ...
+    // in increasing label order
+    const long long m = count + 1;
+    const long long nbnd = (long long)bl.size();
+    uint64_t *d_lut = nullptr, *d_bl = nullptr, *d_bg = nullptr;
+    uint8_t *d_flag = nullptr;
+    int *d_nf = nullptr, *d_rank = nullptr;
+    PMG_TRY(scratch_alloc((void **)&d_lut, (size_t)m * 8, st));
+    PMG_TRY(scratch_alloc((void **)&d_flag, (size_t)m, st));
+    PMG_TRY(scratch_alloc((void **)&d_nf, (size_t)m * 4, st));
+    PMG_TRY(scratch_alloc((void **)&d_rank, (size_t)m * 4, st));
+    PMG_TRY(scratch_alloc((void **)&d_bl, (size_t)(nbnd + 1) * 8, st));
+    PMG_TRY(scratch_alloc((void **)&d_bg, (size_t)(nbnd + 1) * 8, st));
+    PMG_CUDA(cudaMemsetAsync(d_flag, 0, (size_t)m, st));
+    if (nbnd > 0) {
+        PMG_CUDA(cudaMemcpyAsync(d_bl, bl.data(), (size_t)nbnd * 8, cudaMemcpyHostToDevice, st));
+        PMG_CUDA(cudaMemcpyAsync(d_bg, bg.data(), (size_t)nbnd * 8, cudaMemcpyHostToDevice, st));
+        k_lut_flags<<<grid_for(nbnd, 256, 1LL << 30), 256, 0, st>>>(d_bl, d_bg, nbnd, d_flag, d_lut);
+        PMG_CHECK_LAUNCH();
+    }
+    k_lut_nonflag<<<grid_for(m, 256, 1LL << 30), 256, 0, st>>>(d_flag, m, d_nf);
+    PMG_CHECK_LAUNCH();
+    size_t tb = 0;
+    PMG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, d_nf, d_rank, (int)m, st));
+    void *d_t = nullptr;
+    PMG_TRY(scratch_alloc(&d_t, tb, st));
+    PMG_CUDA(cub::DeviceScan::ExclusiveSum(d_t, tb, d_nf, d_rank, (int)m, st));
+    k_lut_fill<<<grid_for(m, 256, 1LL << 30), 256, 0, st>>>(d_flag, d_rank, m, global_id, d_lut);
+    PMG_CHECK_LAUNCH();
+    k_apply_lut<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(L, n, d_lut);
+    PMG_CHECK_LAUNCH();
+    const long long nloc = (long long)count - nbnd;
+    int64_t max_label = (int64_t)(nloc + (long long)global_id);
+    if (max_label < 1)
+        max_label = (int64_t)global_id;
+    PMG_TRY(scratch_free(d_t, st));
+    PMG_TRY(scratch_free(d_lut, st));
+    PMG_TRY(scratch_free(d_flag, st));
+    PMG_TRY(scratch_free(d_nf, st));
+    PMG_TRY(scratch_free(d_rank, st));
+    PMG_TRY(scratch_free(d_bl, st));
+    PMG_TRY(scratch_free(d_bg, st));
+    *out_count = max_label;
+    return PMG_OK;
+}
+
+template <typename T>
+static int cc_label_t(const T *img, uint64_t *labels, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, int64_t *count, cudaStream_t st)
+{
+    const long long n = shape[0] * shape[1] * shape[2];
+    int *P = nullptr, *R = nullptr, *err = nullptr, *cnt = nullptr, *offs = nullptr;
+    const long long nb = (n + kNumTile - 1) / kNumTile;
+    PMG_TRY(scratch_alloc((void **)&P, (size_t)n * 4, st));
+    PMG_TRY(scratch_alloc((void **)&R, (size_t)n * 4, st));
+    PMG_TRY(scratch_alloc((void **)&err, sizeof(int), st));
+    PMG_TRY(scratch_alloc((void **)&cnt, (size_t)nb * 4 + 4, st));
+    PMG_TRY(scratch_alloc((void **)&offs, (size_t)nb * 4 + 4, st));
+    PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    PMG_TRY(uf_build<T>(img, P, shape, bc, pad, false, err, st));
+    k_root_count<<<(unsigned)nb, kNumBlock, 0, st>>>(P, n, cnt);
+    PMG_CHECK_LAUNCH();
+    size_t tb = 0;
+    PMG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, offs, (int)nb + 1, st));
+    void *tmp = nullptr;
+    PMG_TRY(scratch_alloc(&tmp, tb, st));
+    PMG_CUDA(cudaMemsetAsync(cnt + nb, 0, 4, st));
+    PMG_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, offs, (int)nb + 1, st));
+    k_root_rank<<<(unsigned)nb, kNumBlock, 0, st>>>(P, n, offs, R);
+    PMG_CHECK_LAUNCH();
+    k_label_out<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(P, R, n, labels);
+    PMG_CHECK_LAUNCH();
+    int total = 0;
+    PMG_CUDA(cudaMemcpyAsync(&total, offs + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int s = read_err(err, st);
+    PMG_TRY(scratch_free(tmp, st));
+    PMG_TRY(scratch_free(P, st));
+    PMG_TRY(scratch_free(R, st));
+    PMG_TRY(scratch_free(err, st));
+    PMG_TRY(scratch_free(cnt, st));
+    PMG_TRY(scratch_free(offs, st));
+    if (s != PMG_OK)
+        return s;
+    *count = total;
+    if (any_periodic(bc))
+        return periodic_renumber(labels, shape, bc, pad, total, count, st);
+    return PMG_OK;
+}
+
+static int check_vol(const int64_t *shape)
+{
+    for (int d = 0; d < 3; d++)
+        if (shape[d] <= 0) {
+            set_error("shape[%d] must be positive", d);
+            return PMG_EINVAL;
+        }
+    const long long n = shape[0] * shape[1] * shape[2];
+    if (n >= (1LL << 31) - 1) {
+        set_error("volume of %lld voxels exceeds the 2^31-1 voxel limit of the int32 union-find", n);
+        return PMG_ERANGE;
+    }
+    return PMG_OK;
+}
+
+} // namespace pmg
+
+using namespace pmg;
+
+extern "C" int pmg_cc_label(const void *img, int32_t elem_bytes, uint64_t *labels,
+                            const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],
+                            int64_t *count, void *stream)
+{
+    if (!img || !labels || !shape || !bc || !pad || !count) {
+        set_error("pmg_cc_label: null argument");
+        return PMG_EINVAL;
+    }
+    PMG_TRY(check_vol(shape));
+    cudaStream_t st = as_stream(stream);
+    switch (elem_bytes) {
+    case 1:
+        return cc_label_t((const uint8_t *)img, labels, shape, bc, pad, count, st);
+    case 2:
+        return cc_label_t((const uint16_t *)img, labels, shape, bc, pad, count, st);
+    case 4:
+        return cc_label_t((const uint32_t *)img, labels, shape, bc, pad, count, st);
+    case 8:
+        return cc_label_t((const uint64_t *)img, labels, shape, bc, pad, count, st);
+    default:
+        set_error("pmg_cc_label: element size %d not supported", elem_bytes);
+        return PMG_EINVAL;
+    }
+}
+
+namespace pmg {
+
+// Selection with caller-provided scratch: P (n int32), mark (n bytes rounded
+// up to 4), err (one int, zeroed by the caller).  Does not synchronize.
+int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shape,
+               const int32_t *bc, const int32_t *pad, const int64_t *inlet_box,
+               const int64_t *outlet_box, int mode, int phase, int *P, uint8_t *mark, int *err,
+               cudaStream_t st)
+{
+    const long long n = shape[0] * shape[1] * shape[2];
+    PMG_CUDA(cudaMemsetAsync(mark, 0, ((size_t)n + 3) & ~(size_t)3, st));
+    PMG_TRY(uf_build<uint8_t>(img, P, shape, bc, pad, true, err, st));
+    Vol3 V{shape[0], shape[1], shape[2]};
+    const int64_t *boxes[2] = {inlet_box, outlet_box};
+    for (int w = 0; w < 2; w++) {
+        const int64_t *bx = boxes[w];
+        if (!bx || bx[0] < 0)
+            continue;
+        Box b;
+        for (int d = 0; d < 3; d++) {
+            b.lo[d] = bx[2 * d];
+            b.hi[d] = bx[2 * d + 1];
+            if (b.lo[d] < 0 || b.hi[d] > shape[d] || b.lo[d] > b.hi[d]) {
+                set_error("connected-image selection: face box outside the volume");
+                return PMG_EINVAL;
+            }
+        }
+        if (b.size() > 0) {
+            k_mark_face<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(P, V, b, mark,
+                                                                              (uint8_t)(1 << w));
+            PMG_CHECK_LAUNCH();
+        }
+    }
+    if (out_bytes == 1)
+        k_select<uint8_t><<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(img, P, mark, n, mode, phase,
+                                                                        (uint8_t *)out);
+    else
+        k_select<uint64_t><<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(img, P, mark, n, mode, phase,
+                                                                         (uint64_t *)out);
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+int check_err(int *err, cudaStream_t st) { return read_err(err, st); }
+
+int check_volume(const int64_t *shape) { return check_vol(shape); }
+
+} // namespace pmg
+
+extern "C" int pmg_cc_select(const uint8_t *img, void *out, int32_t out_bytes,
+                             const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],
+                             const int64_t inlet_box[6], const int64_t outlet_box[6], int32_t mode,
+                             int32_t phase, void *stream)
+{
+    if (!img || !out || !shape || !bc || !pad) {
+        set_error("pmg_cc_select: null argument");
+        return PMG_EINVAL;
+    }
+    if (out_bytes != 1 && out_bytes != 8) {
+        set_error("pmg_cc_select: output element size must be 1 or 8");
+        return PMG_EINVAL;
+    }
+    PMG_TRY(check_vol(shape));
+    cudaStream_t st = as_stream(stream);
+    const long long n = shape[0] * shape[1] * shape[2];
+    int *P = nullptr, *err = nullptr;
+    uint8_t *mark = nullptr;
+    PMG_TRY(scratch_alloc((void **)&P, (size_t)n * 4, st));
+    PMG_TRY(scratch_alloc((void **)&mark, ((size_t)n + 3) & ~(size_t)3, st));
+    PMG_TRY(scratch_alloc((void **)&err, sizeof(int), st));
+    PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    int s = select_run(img, out, out_bytes, shape, bc, pad, inlet_box, outlet_box, mode, phase, P,
+                       mark, err, st);
+    if (s == PMG_OK)
+        s = read_err(err, st);
+    PMG_TRY(scratch_free(P, st));
+    PMG_TRY(scratch_free(mark, st));
+    PMG_TRY(scratch_free(err, st));
+    return s;
+}

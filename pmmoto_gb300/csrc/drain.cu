@@ -1,0 +1,289 @@
+// Porosimetry and morphological drainage driven from native code.
+//
+// porosimetry (src/pmmoto/filters/porosimetry.py:84-160, mode="distance"):
+//   erode -> [inlet-connected] -> if phase 1 exists: [multiphase constraint:
+//   inlet-connected phase 1 of the multiphase image] -> dilate.
+// drainage, standard method (src/pmmoto/filters/equilibrium_distribution.py:
+//   25-179): per capillary pressure, porosimetry with the inlet and multiphase
+//   constraints, outlet-connected wetting phase, update, reservoir refill,
+//   wetting-phase count in the own region (the saturation numerator).
+// All images stay on the device between steps; the host reads back only the
+// two phase-existence counts porosimetry branches on and, at the end, the
+// per-pressure counts.
+#include <vector>
+
+#include "pmg_internal.cuh"
+
+namespace pmg {
+
+struct Boxes {
+    int64_t own[6];
+    int64_t inlet[6], outlet[6];
+    int32_t rpad[6];
+};
+
+__global__ void k_constrain(uint8_t *res, const uint8_t *__restrict__ nconn, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        if (res[i] != 1 || nconn[i] != 1)
+            res[i] = 0;
+}
+
+// mp = (morph == 1 && w == 2) ? 1 : mp; reservoir slabs -> 1
+__global__ void k_drain_update(uint8_t *mp, const uint8_t *__restrict__ morph, const uint8_t *__restrict__ w,
+                               long long s0, long long s1, long long s2, Boxes B)
+{
+    const long long n = s0 * s1 * s2;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long k = idx % s2, r = idx / s2, j = r % s1, i = r / s1;
+        uint8_t v = (morph[idx] == 1 && w[idx] == 2) ? (uint8_t)1 : mp[idx];
+        const bool res = (i < B.rpad[0]) || (i >= s0 - B.rpad[1]) || (j < B.rpad[2]) || (j >= s1 - B.rpad[3]) ||
+                         (k < B.rpad[4]) || (k >= s2 - B.rpad[5]);
+        if (res)
+            v = 1;
+        mp[idx] = v;
+    }
+}
+
+struct Work {
+    uint8_t *t1, *t2, *t3; // uint8 volumes
+    uint8_t *E;            // morphology scratch
+    float *A, *B;
+    int *P;
+    uint8_t *mark;
+    int *err;
+    unsigned long long *cnt; // scalar counter
+    void *base;
+};
+
+static int work_alloc(Work &w, const int64_t *shape, size_t morph_bytes, cudaStream_t st)
+{
+    const size_t n = (size_t)shape[0] * shape[1] * shape[2];
+    const size_t a = (n + 255) & ~(size_t)255;
+    const size_t total = 3 * a + ((morph_bytes + 255) & ~(size_t)255) + a * 4 + a + 512;
+    PMG_TRY(scratch_alloc(&w.base, total, st));
+    char *p = (char *)w.base;
+    w.t1 = (uint8_t *)p;
+    p += a;
+    w.t2 = (uint8_t *)p;
+    p += a;
+    w.t3 = (uint8_t *)p;
+    p += a;
+    w.E = (uint8_t *)p;
+    p += (morph_bytes + 255) & ~(size_t)255;
+    w.P = (int *)p;
+    p += a * 4;
+    w.mark = (uint8_t *)p;
+    p += a;
+    w.err = (int *)p;
+    w.cnt = (unsigned long long *)(p + 256);
+    return PMG_OK;
+}
+
+static void morph_split(Work &w, const int64_t *shape, const int32_t *bc, const int32_t *ext,
+                        uint8_t *&E, float *&A, float *&B)
+{
+    long long nv = 1;
+    for (int d = 0; d < 3; d++)
+        nv *= shape[d] + (bc[2 * d] == PMG_BC_PERIODIC ? ext[2 * d] + ext[2 * d + 1] : 0);
+    E = w.E;
+    A = (float *)(w.E + (((size_t)nv + 255) & ~(size_t)255));
+    B = A + nv;
+}
+
+static int count_sync(const uint8_t *img, const int64_t *shape, const int64_t *box, uint8_t value, Work &w,
+                      cudaStream_t st, long long &out)
+{
+    PMG_CUDA(cudaMemsetAsync(w.cnt, 0, sizeof(unsigned long long), st));
+    PMG_TRY(count_eq_async(img, shape, box, value, w.cnt, st));
+    unsigned long long h = 0;
+    PMG_CUDA(cudaMemcpyAsync(&h, w.cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PMG_CUDA(cudaStreamSynchronize(st));
+    out = (long long)h;
+    return PMG_OK;
+}
+
+// porosimetry.py:84-160 (mode="distance") into `out`.
+static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape, const int32_t *bc,
+                           const int32_t *pad, const int32_t *ext_e, const int32_t *ext_d, const float *res,
+                           double r_e, int cmp_e, double r_d, int cmp_d, int inlet, const uint8_t *mp,
+                           const Boxes &Bx, Work &w, cudaStream_t st)
+{
+    const long long n = shape[0] * shape[1] * shape[2];
+    const int64_t all[6] = {0, shape[0], 0, shape[1], 0, shape[2]};
+    uint8_t *E;
+    float *A, *B;
+    morph_split(w, shape, bc, ext_e, E, A, B);
+    PMG_TRY(morph_run(pm, w.t1, shape, bc, pad, ext_e, res, r_e, cmp_e, 0, E, A, B, st));
+    uint8_t *cur = w.t1;
+    if (inlet) {
+        PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+        PMG_TRY(select_run(w.t1, w.t2, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, -1, w.P, w.mark,
+                           w.err, st));
+        PMG_TRY(check_err(w.err, st));
+        cur = w.t2;
+    }
+    long long c1 = 0;
+    PMG_TRY(count_sync(cur, shape, all, 1, w, st, c1));
+    if (c1 > 0) {
+        if (mp) {
+            long long m1 = 0;
+            PMG_TRY(count_sync(mp, shape, all, 1, w, st, m1));
+            if (m1 > 0) {
+                PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+                PMG_TRY(select_run(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1, w.P,
+                                   w.mark, w.err, st));
+                PMG_TRY(check_err(w.err, st));
+                k_constrain<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(cur, w.t3, n);
+                PMG_CHECK_LAUNCH();
+            }
+        }
+        morph_split(w, shape, bc, ext_d, E, A, B);
+        PMG_TRY(morph_run(cur, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st));
+    } else if (cur != out) {
+        PMG_CUDA(cudaMemcpyAsync(out, cur, (size_t)n, cudaMemcpyDeviceToDevice, st));
+    }
+    return PMG_OK;
+}
+
+static int ext_of(const int32_t *bc, const int32_t *pad, const int32_t *ratio, int32_t *ext)
+{
+    for (int d = 0; d < 3; d++)
+        for (int s = 0; s < 2; s++) {
+            const int b = bc[2 * d + s];
+            ext[2 * d + s] = (b == PMG_BC_END || (b == PMG_BC_WALL && pad[2 * d + s] == 1)) ? 0 : ratio[d];
+        }
+    return PMG_OK;
+}
+
+static size_t max_morph_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext_a, const int32_t *ext_b)
+{
+    const size_t a = morph_scratch_bytes(shape, bc, ext_a), b = morph_scratch_bytes(shape, bc, ext_b);
+    return a > b ? a : b;
+}
+
+static int check_common(const int64_t *shape, const int32_t *bc, const int32_t *pad)
+{
+    if (!shape || !bc || !pad) {
+        set_error("null geometry argument");
+        return PMG_EINVAL;
+    }
+    return check_volume(shape);
+}
+
+} // namespace pmg
+
+using namespace pmg;
+
+extern "C" int pmg_porosimetry(const uint8_t *pm_img, const uint8_t *mp_img, uint8_t *out,
+                               const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],
+                               const int64_t inlet_box[6], const float res[3], double r_erode,
+                               int32_t cmp_erode, const int32_t ratio_erode[3], double r_dilate,
+                               int32_t cmp_dilate, const int32_t ratio_dilate[3], int32_t inlet,
+                               void *stream)
+{
+    PMG_TRY(check_common(shape, bc, pad));
+    if (!pm_img || !out || !res || !ratio_erode || !ratio_dilate) {
+        set_error("pmg_porosimetry: null argument");
+        return PMG_EINVAL;
+    }
+    cudaStream_t st = as_stream(stream);
+    int32_t ext_e[6], ext_d[6];
+    ext_of(bc, pad, ratio_erode, ext_e);
+    ext_of(bc, pad, ratio_dilate, ext_d);
+    Boxes Bx{};
+    for (int q = 0; q < 6; q++) {
+        Bx.inlet[q] = inlet_box ? inlet_box[q] : -1;
+        Bx.outlet[q] = -1;
+    }
+    Work w{};
+    PMG_TRY(work_alloc(w, shape, max_morph_bytes(shape, bc, ext_e, ext_d), st));
+    int s = porosimetry_run(pm_img, out, shape, bc, pad, ext_e, ext_d, res, r_erode, cmp_erode, r_dilate,
+                            cmp_dilate, inlet, mp_img, Bx, w, st);
+    int s2 = scratch_free(w.base, st);
+    return s != PMG_OK ? s : s2;
+}
+
+extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
+                            const int32_t bc[6], const int32_t pad[6], const int32_t rpad[6],
+                            const int64_t own_box[6], const int64_t inlet_box[6],
+                            const int64_t outlet_box[6], const float res[3], int32_t n_radii,
+                            const double *radii, const int32_t *active, const int32_t *ratios,
+                            int64_t *counts, void *stream)
+{
+    PMG_TRY(check_common(shape, bc, pad));
+    if (!pm_img || !mp_img || !rpad || !own_box || !res || !counts || n_radii < 0 ||
+        (n_radii > 0 && (!radii || !active || !ratios))) {
+        set_error("pmg_drainage: null argument");
+        return PMG_EINVAL;
+    }
+    cudaStream_t st = as_stream(stream);
+    const long long n = shape[0] * shape[1] * shape[2];
+    Boxes Bx{};
+    for (int q = 0; q < 6; q++) {
+        Bx.own[q] = own_box[q];
+        Bx.inlet[q] = inlet_box ? inlet_box[q] : -1;
+        Bx.outlet[q] = outlet_box ? outlet_box[q] : -1;
+        Bx.rpad[q] = rpad[q];
+    }
+    size_t mb = 0;
+    for (int k = 0; k < n_radii; k++) {
+        int32_t ext[6];
+        ext_of(bc, pad, ratios + 3 * k, ext);
+        const size_t b = morph_scratch_bytes(shape, bc, ext);
+        if (b > mb)
+            mb = b;
+    }
+    Work w{};
+    PMG_TRY(work_alloc(w, shape, mb, st));
+    uint8_t *morph = nullptr, *wet = nullptr;
+    unsigned long long *d_counts = nullptr;
+    int s = scratch_alloc((void **)&morph, (size_t)n, st);
+    if (s == PMG_OK)
+        s = scratch_alloc((void **)&wet, (size_t)n, st);
+    if (s == PMG_OK)
+        s = scratch_alloc((void **)&d_counts, sizeof(unsigned long long) * (size_t)(n_radii + 1), st);
+    if (s == PMG_OK)
+        s = cudaMemsetAsync(d_counts, 0, sizeof(unsigned long long) * (size_t)(n_radii + 1), st) == cudaSuccess
+                ? PMG_OK
+                : PMG_ECUDA;
+    for (int k = 0; k < n_radii && s == PMG_OK; k++) {
+        if (active[k]) {
+            int32_t ext[6];
+            ext_of(bc, pad, ratios + 3 * k, ext);
+            // the probe radius is a numpy float64: compare in float64
+            s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext, res, radii[k], 1, radii[k], 1, 1, mp_img,
+                                Bx, w, st);
+        } else {
+            s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        }
+        if (s != PMG_OK)
+            break;
+        PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+        s = select_run(mp_img, wet, 1, shape, bc, pad, nullptr, Bx.outlet, PMG_SEL_OUTLET, 2, w.P, w.mark, w.err,
+                       st);
+        if (s == PMG_OK)
+            s = check_err(w.err, st);
+        if (s != PMG_OK)
+            break;
+        k_drain_update<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(mp_img, morph, wet, shape[0], shape[1],
+                                                                    shape[2], Bx);
+        PMG_CHECK_LAUNCH();
+        s = count_eq_async(mp_img, shape, Bx.own, 2, d_counts + k, st);
+    }
+    if (s == PMG_OK && n_radii > 0) {
+        std::vector<unsigned long long> h((size_t)n_radii);
+        PMG_CUDA(cudaMemcpyAsync(h.data(), d_counts, sizeof(unsigned long long) * (size_t)n_radii,
+                                 cudaMemcpyDeviceToHost, st));
+        PMG_CUDA(cudaStreamSynchronize(st));
+        for (int k = 0; k < n_radii; k++)
+            counts[k] = (int64_t)h[(size_t)k];
+    }
+    scratch_free(morph, st);
+    scratch_free(wet, st);
+    scratch_free(d_counts, st);
+    int s2 = scratch_free(w.base, st);
+    return s != PMG_OK ? s : s2;
+}

@@ -1,0 +1,677 @@
+// Exact Euclidean distance transform on GB300 (sm_103a).
+//
+// Three kernels, one thread per 1-D line, lanes of a warp on neighbouring
+// lines so that the strided axes are read and written coalesced:
+//
+//  * k_pass0     -- the linear two-sweep pass of squared_edt_1d
+//                   (src/pmmoto/filters/distance/_distance.hpp:135-182) with
+//                   the periodic correctors of _distance.pyx:240-279 /
+//                   euclidean_distance_transform.py:395-447 found in-kernel.
+//  * k_envelope  -- the lower envelope of parabolas of
+//                   squared_edt_1d_parabolic (_distance.hpp:184-272) with the
+//                   periodic boundary hulls of return_boundary_hull
+//                   (_distance.hpp:296-356) computed in-kernel from the same
+//                   line, so the MPI feature exchange of the reference becomes
+//                   index arithmetic.
+//
+// The envelope stack is kept as a bitmask of surviving vertices in shared
+// memory (one bit per voxel of the line, words interleaved across the block so
+// every access is bank-conflict free).  A vertex's height is re-read from the
+// input line and a segment's range is recomputed from the two neighbouring
+// vertices with the same float expression the reference used when it pushed
+// the segment, so the result is bit-identical while the per-line state is
+// n/8 bytes instead of 16 n bytes.
+//
+// All floating-point steps use round-to-nearest intrinsics with no
+// multiply-add contraction, in the reference's operation order.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#include "edt_internal.cuh"
+
+namespace pmg {
+
+constexpr int kMaxHull = 8; // imported hulls per side (reference keeps <= 5)
+
+struct LineGeo {
+    long long base, stride;
+    int n;
+    int a, b; // coordinates of the line along the two other axes (d1 < d2)
+};
+
+__device__ __forceinline__ LineGeo line_addr(const Lines &L, long long li)
+{
+    LineGeo g;
+    const int a = L.b1lo + (int)(li / L.nb2);
+    const int b = L.b2lo + (int)(li - (li / L.nb2) * L.nb2);
+    g.a = a;
+    g.b = b;
+    if (L.ax == 0) { // lines over (j, k)
+        g.base = (long long)a * L.s2 + b;
+        g.stride = L.s1 * L.s2;
+        g.n = (int)L.s0;
+    } else if (L.ax == 1) { // lines over (i, k)
+        g.base = (long long)a * L.s1 * L.s2 + b;
+        g.stride = L.s2;
+        g.n = (int)L.s1;
+    } else { // lines over (i, j)
+        g.base = ((long long)a * L.s1 + b) * L.s2;
+        g.stride = 1;
+        g.n = (int)L.s2;
+    }
+    return g;
+}
+
+// ---------------------------------------------------------------------------
+// pass 0: squared_edt_1d along axis `ax`
+// ---------------------------------------------------------------------------
+__global__ void k_pass0(const uint8_t *__restrict__ img, float *__restrict__ out, Lines Ls,
+                        float res, pmg_axis_cfg cfg)
+{
+    const long long nlines = Ls.count();
+    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
+         li += (long long)gridDim.x * blockDim.x) {
+        const LineGeo g = line_addr(Ls, li);
+        const uint8_t *in = img + g.base;
+        float *d = out + g.base;
+        const long long st = g.stride;
+        const int n = g.n;
+        float lc = INFINITY, uc = INFINITY;
+        if (cfg.periodic) {
+            int F = -1, L = -1;
+            for (int i = cfg.f_lo; i < n; i++)
+                if (in[i * st] == 0) {
+                    F = i;
+                    break;
+                }
+            for (int i = n - cfg.l_hi - 1; i >= cfg.l_lo; i--)
+                if (in[i * st] == 0) {
+                    L = i;
+                    break;
+                }
+            if (F != -1)
+                uc = (float)(F + cfg.a_u);
+            if (L != -1)
+                lc = (float)(n - L + cfg.a_l);
+        }
+        // forward sweep (reset at zeros, restart at a change of nonzero value)
+        uint8_t seg = in[0];
+        float prev = seg == 0 ? 0.0f : fmul(lc, res);
+        d[0] = prev;
+        uint8_t prev_v = seg;
+        for (int i = 1; i < n; i++) {
+            const uint8_t v = in[i * st];
+            float cur;
+            if (v == 0) {
+                cur = 0.0f;
+            } else if (v == seg) {
+                cur = fadd(prev, res);
+            } else {
+                cur = res;
+                d[(i - 1) * st] = prev_v != 0 ? res : 0.0f;
+                seg = v;
+            }
+            d[i * st] = cur;
+            prev = cur;
+            prev_v = v;
+        }
+        // clamp the last voxel, backward sweep, square, inf -> FLT_MAX
+        float b = d[(n - 1) * st];
+        const float ucr = fmul(uc, res);
+        if (b > ucr)
+            b = ucr;
+        {
+            float q = fmul(b, b);
+            d[(n - 1) * st] = q == INFINITY ? FLT_MAX : q;
+        }
+        for (int i = n - 2; i >= 0; i--) {
+            const float a = d[i * st];
+            b = fminf(a, fadd(b, res));
+            const float q = fmul(b, b);
+            d[i * st] = q == INFINITY ? FLT_MAX : q;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// envelope stack kept as a bitmask in shared memory
+// ---------------------------------------------------------------------------
+struct Entry {
+    int v;
+    float h;
+};
+
+struct Stack {
+    uint32_t *bm; // word w of this thread at bm[w * nthr]
+    int nthr;
+    // imported lower hulls, bottom -> top (given ranges)
+    int lv[kMaxHull];
+    float lh[kMaxHull], lr[kMaxHull];
+    int nl;
+    // imported upper hulls pushed after the native vertices
+    int uv[kMaxHull];
+    float uh[kMaxHull], ur[kMaxHull];
+    int nu;
+    // native vertices (bits); ntv = topmost native vertex or -1
+    int nn, ntv;
+    // cached top of the whole stack
+    int tv;
+    float th, tr;
+
+    __device__ __forceinline__ uint32_t &word(int w) { return bm[(long long)w * nthr]; }
+    __device__ __forceinline__ void setbit(int v) { word(v >> 5) |= (1u << (v & 31)); }
+    __device__ __forceinline__ void clrbit(int v) { word(v >> 5) &= ~(1u << (v & 31)); }
+    // highest set bit strictly below v (callers guarantee one exists; the
+    // search still stops at word 0 so a broken invariant cannot leave the
+    // thread's shared-memory words)
+    __device__ __forceinline__ int prev_bit(int v)
+    {
+        int w = v >> 5;
+        uint32_t m = word(w) & ((1u << (v & 31)) - 1u);
+        while (m == 0) {
+            if (w == 0)
+                return 0;
+            --w;
+            m = word(w);
+        }
+        return (w << 5) + 31 - __clz(m);
+    }
+    // lowest set bit strictly above v, or -1 if none below `lim` bits
+    __device__ __forceinline__ int next_bit(int v, int nwords)
+    {
+        int w = (v + 1) >> 5;
+        if (w >= nwords)
+            return -1;
+        uint32_t m = (v + 1) & 31 ? word(w) & ~((1u << ((v + 1) & 31)) - 1u) : word(w);
+        while (m == 0) {
+            if (++w >= nwords)
+                return -1;
+            m = word(w);
+        }
+        return (w << 5) + __ffs(m) - 1;
+    }
+    __device__ __forceinline__ void clear(int nwords)
+    {
+        for (int w = 0; w < nwords; w++)
+            word(w) = 0u;
+    }
+};
+
+// Height of a native vertex (re-read from the input line).
+__device__ __forceinline__ float vh(const float *line, long long st, int v) { return line[v * st]; }
+
+// Range of the native vertex `v` = intersection with the entry below it.
+__device__ __forceinline__ float native_range(Stack &S, const float *line, long long st, int v,
+                                              float h, float aniso, int below_native_count)
+{
+    if (below_native_count > 0) {
+        int pv = S.prev_bit(v);
+        return isect(h, (float)v, vh(line, st, pv), (float)pv, aniso);
+    }
+    if (S.nl > 0)
+        return isect(h, (float)v, S.lh[S.nl - 1], (float)S.lv[S.nl - 1], aniso);
+    return -INFINITY;
+}
+
+// Pop the top entry and reload the cache with the new top.
+__device__ __forceinline__ void pop_top(Stack &S, const float *line, long long st, float aniso)
+{
+    if (S.nu > 0) {
+        --S.nu;
+        if (S.nu > 0) {
+            S.tv = S.uv[S.nu - 1];
+            S.th = S.uh[S.nu - 1];
+            S.tr = S.ur[S.nu - 1];
+            return;
+        }
+    } else if (S.nn > 0) {
+        S.clrbit(S.ntv);
+        --S.nn;
+        S.ntv = S.nn > 0 ? S.prev_bit(S.ntv) : -1;
+    } else {
+        --S.nl;
+    }
+    if (S.nn > 0) {
+        S.tv = S.ntv;
+        S.th = vh(line, st, S.ntv);
+        S.tr = native_range(S, line, st, S.ntv, S.th, aniso, S.nn - 1);
+    } else {
+        S.tv = S.lv[S.nl - 1];
+        S.th = S.lh[S.nl - 1];
+        S.tr = S.lr[S.nl - 1];
+    }
+}
+
+// update_hull (_distance.hpp:89-112) for vertex i with height f; `kind`
+// 0 = native vertex (a bit), 1 = imported upper hull.
+__device__ __forceinline__ void insert(Stack &S, const float *line, long long st, int i, float f,
+                                       float aniso, int kind)
+{
+    float s = isect(f, (float)i, S.th, (float)S.tv, aniso);
+    while (S.nl + S.nn + S.nu > 1 && s <= S.tr) {
+        pop_top(S, line, st, aniso);
+        s = isect(f, (float)i, S.th, (float)S.tv, aniso);
+    }
+    if (kind == 0) {
+        S.setbit(i);
+        ++S.nn;
+        S.ntv = i;
+    } else {
+        S.uv[S.nu] = i;
+        S.uh[S.nu] = f;
+        S.ur[S.nu] = s;
+        ++S.nu;
+    }
+    S.tv = i;
+    S.th = f;
+    S.tr = s;
+}
+
+// Build the envelope of a line segment [0, n) of `line` with no imports:
+// entry (0, f(0)) at the bottom, then vertices 1..n-1.
+__device__ __forceinline__ void build_plain(Stack &S, const float *line, long long st, int n,
+                                            float aniso)
+{
+    S.nl = 0;
+    S.nu = 0;
+    S.setbit(0);
+    S.nn = 1;
+    S.ntv = 0;
+    S.tv = 0;
+    S.th = vh(line, st, 0);
+    S.tr = -INFINITY;
+    for (int i = 1; i < n; i++)
+        insert(S, line, st, i, vh(line, st, i), aniso, 0);
+}
+
+// Iterator over the final stack, bottom to top.
+struct Iter {
+    int phase; // 0 lower, 1 native, 2 upper, 3 done
+    int idx;   // lower/upper index or native vertex
+};
+
+__device__ __forceinline__ bool iter_next(Stack &S, Iter &it, const float *line, long long st,
+                                          int nwords, Entry &e, int &is_lower, float &given_r)
+{
+    for (;;) {
+        if (it.phase == 0) {
+            if (it.idx < S.nl) {
+                e.v = S.lv[it.idx];
+                e.h = S.lh[it.idx];
+                given_r = S.lr[it.idx];
+                is_lower = 1;
+                ++it.idx;
+                return true;
+            }
+            it.phase = 1;
+            it.idx = -1;
+        }
+        if (it.phase == 1) {
+            int nb = S.nn > 0 ? S.next_bit(it.idx, nwords) : -1;
+            if (nb >= 0) {
+                it.idx = nb;
+                e.v = nb;
+                e.h = vh(line, st, nb);
+                is_lower = 0;
+                return true;
+            }
+            it.phase = 2;
+            it.idx = 0;
+        }
+        if (it.phase == 2) {
+            if (it.idx < S.nu) {
+                e.v = S.uv[it.idx];
+                e.h = S.uh[it.idx];
+                is_lower = 0;
+                ++it.idx;
+                return true;
+            }
+            it.phase = 3;
+        }
+        return false;
+    }
+}
+
+// return_boundary_hull (_distance.hpp:296-356) on segment [start, start+nv)
+// of the line: keep up to num_hull+1 finite parabolas from the chosen end,
+// vertices and ranges shifted by `corr`.  Returns the count; the bitmask is
+// left cleared.
+__device__ int boundary_hull(Stack &S, const float *line, long long st, int start, int nv,
+                             float aniso, int num_hull, int corr, bool forward, int *ov,
+                             float *oh, float *orr)
+{
+    const float *seg = line + (long long)start * st;
+    if (nv <= 0)
+        return 0;
+    if (nv == 1) {
+        const float f0 = seg[0];
+        if (f0 < FLT_MAX) {
+            ov[0] = corr;
+            oh[0] = f0;
+            orr[0] = INFINITY;
+            return 1;
+        }
+        // the reference reads its "phantom" second slot here: vertex 0, height 0
+        ov[0] = corr;
+        oh[0] = 0.0f;
+        orr[0] = INFINITY;
+        return 1;
+    }
+    const int nwords = (nv + 31) >> 5;
+    build_plain(S, seg, st, nv, aniso);
+    const int top = S.nn - 1; // stack index of the top entry
+    const int keep = num_hull < top ? num_hull : top;
+    int cnt = 0;
+    if (forward) {
+        int v = -1;
+        float prev_h = 0.0f;
+        int prev_v = 0;
+        for (int k = 0; k <= top && cnt <= keep; k++) {
+            v = S.next_bit(v, nwords);
+            const float h = vh(seg, st, v);
+            const float r = k == 0 ? -INFINITY : isect(h, (float)v, prev_h, (float)prev_v, aniso);
+            if (h < FLT_MAX) {
+                ov[cnt] = v + corr;
+                oh[cnt] = h;
+                orr[cnt] = fadd(r, (float)corr);
+                ++cnt;
+                if (h == 0.9f)
+                    break;
+            }
+            prev_h = h;
+            prev_v = v;
+        }
+    } else {
+        int v = S.ntv;
+        float h = vh(seg, st, v);
+        for (int k = top; k >= 0 && cnt <= keep; k--) {
+            int pv = 0;
+            float ph = 0.0f, r;
+            if (k > 0) {
+                pv = S.prev_bit(v);
+                ph = vh(seg, st, pv);
+                r = isect(h, (float)v, ph, (float)pv, aniso);
+            } else {
+                r = -INFINITY;
+            }
+            if (h < FLT_MAX) {
+                ov[cnt] = v + corr;
+                oh[cnt] = h;
+                orr[cnt] = fadd(r, (float)corr);
+                ++cnt;
+                if (h == 0.9f)
+                    break;
+            }
+            v = pv;
+            h = ph;
+        }
+    }
+    S.clear(nwords);
+    return cnt;
+}
+
+// ---------------------------------------------------------------------------
+// envelope pass along axis `ax`: fin -> fout (out of place)
+// ---------------------------------------------------------------------------
+__global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
+                           float res, pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me)
+{
+    const long long nlines = Ls.count();
+    extern __shared__ uint32_t smem_bm[];
+    const float aniso = fmul(res, res);
+    Stack S;
+    S.bm = smem_bm + threadIdx.x;
+    S.nthr = blockDim.x;
+    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
+         li += (long long)gridDim.x * blockDim.x) {
+        const LineGeo g = line_addr(Ls, li);
+        const float *line = fin + g.base;
+        const long long st = g.stride;
+        const int n = g.n;
+        const int nwords = (n + 31) >> 5;
+        S.clear(nwords);
+        S.nl = 0;
+        S.nu = 0;
+        int up_v[kMaxHull];
+        float up_h[kMaxHull], up_r[kMaxHull];
+        int n_up = 0;
+        if (cfg.periodic) {
+            // first / last zero (a zero height is exactly a zero voxel of the
+            // original image: pass 0 gives 0 only there and every later pass
+            // keeps it, all other values being >= res^2 > 0)
+            int bf = -1, bb = -1;
+            for (int i = cfg.hf_lo; i < n; i++)
+                if (line[i * st] == 0.0f) {
+                    bf = i;
+                    break;
+                }
+            for (int i = n - cfg.hb_hi - 1; i >= 0; i--)
+                if (line[i * st] == 0.0f) {
+                    bb = i;
+                    break;
+                }
+            // near end (forward) -> upper imports
+            int start, nv, corr;
+            if (bf == -1) {
+                start = cfg.hf_lo;
+                nv = n - cfg.hf_lo;
+            } else {
+                start = cfg.hf_lo;
+                nv = bf - cfg.hf_lo + 1;
+            }
+            corr = 0;
+            n_up = boundary_hull(S, line, st, start, nv, aniso, num_hull, corr, true, up_v, up_h,
+                                 up_r);
+            // far end (backward) -> lower imports, given in top-down order
+            int lo_v[kMaxHull];
+            float lo_h[kMaxHull], lo_r[kMaxHull];
+            if (bb == -1) {
+                start = 0;
+                nv = n - cfg.hb_hi;
+            } else {
+                start = bb;
+                nv = n - bb - cfg.hb_hi;
+            }
+            corr = -nv;
+            const int n_lo = boundary_hull(S, line, st, start, nv, aniso, num_hull, corr, false,
+                                           lo_v, lo_h, lo_r);
+            // the reference pushes the lower list in reverse (rbegin..rend)
+            for (int j = 0; j < n_lo; j++) {
+                S.lv[j] = lo_v[n_lo - 1 - j];
+                S.lh[j] = lo_h[n_lo - 1 - j];
+                S.lr[j] = lo_r[n_lo - 1 - j];
+            }
+            S.nl = n_lo;
+        }
+        // main build
+        int loop_start;
+        if (S.nl > 0) {
+            loop_start = 0;
+            S.nn = 0;
+            S.ntv = -1;
+            S.tv = S.lv[S.nl - 1];
+            S.th = S.lh[S.nl - 1];
+            S.tr = S.lr[S.nl - 1];
+        } else {
+            loop_start = 1;
+            S.setbit(0);
+            S.nn = 1;
+            S.ntv = 0;
+            S.tv = 0;
+            S.th = vh(line, st, 0);
+            S.tr = -INFINITY;
+        }
+        for (int i = loop_start; i < n; i++)
+            insert(S, line, st, i, vh(line, st, i), aniso, 0);
+        for (int j = 0; j < n_up; j++)
+            insert(S, line, st, up_v[j] + n, up_h[j], aniso, 1);
+
+        // evaluation sweep
+        Iter it{0, 0};
+        Entry cur, nxt;
+        int is_lower;
+        float given_r;
+        iter_next(S, it, line, st, nwords, cur, is_lower, given_r);
+        bool has_next = iter_next(S, it, line, st, nwords, nxt, is_lower, given_r);
+        float nr = has_next ? (is_lower ? given_r : isect(nxt.h, (float)nxt.v, cur.h, (float)cur.v, aniso))
+                            : INFINITY;
+        float *o = fout + g.base;
+        // morphology epilogue: output row of the unextended volume
+        long long mrow = 0;
+        bool mwall_row = false;
+        if (form == PMG_EDT_MORPH) {
+            const long long io = g.a - me.e0, jo = g.b - me.e1;
+            mrow = (io * me.o1 + jo) * me.o2;
+            mwall_row = (me.wall[0] && io == 0) || (me.wall[1] && io == me.o0 - 1) ||
+                        (me.wall[2] && jo == 0) || (me.wall[3] && jo == me.o1 - 1);
+        }
+        for (int i = 0; i < n; i++) {
+            const float fi = (float)i;
+            while (nr < fi) {
+                cur = nxt;
+                has_next = iter_next(S, it, line, st, nwords, nxt, is_lower, given_r);
+                nr = has_next ? (is_lower ? given_r : isect(nxt.h, (float)nxt.v, cur.h, (float)cur.v, aniso))
+                              : INFINITY;
+            }
+            const float dx = (float)(i - cur.v);
+            float val = fadd(fmul(aniso, fmul(dx, dx)), cur.h);
+            if (form == PMG_EDT_MORPH) {
+                const int ko = i - me.e2;
+                if (ko < 0 || ko >= me.o2)
+                    continue;
+                const float dist = __fsqrt_rn(val);
+                const bool within = me.cmp64 ? ((double)dist <= me.r64) : (dist <= me.r32);
+                uint8_t v = me.dilate ? (uint8_t)within : (uint8_t)!within;
+                if (mwall_row || (me.wall[4] && ko == 0) || (me.wall[5] && ko == me.o2 - 1))
+                    v = 0;
+                me.out[mrow + ko] = v;
+                continue;
+            }
+            if (form == PMG_EDT_DIST)
+                val = __fsqrt_rn(val);
+            o[i * st] = val;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host drivers
+// ---------------------------------------------------------------------------
+int launch_pass0(const uint8_t *img, float *out, const Lines &Ls, float res,
+                 const pmg_axis_cfg &cfg, cudaStream_t st)
+{
+    const int block = 256;
+    k_pass0<<<grid_for(Ls.count(), block, 1LL << 30), block, 0, st>>>(img, out, Ls, res, cfg);
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+static int envelope_block(int n)
+{
+    // shared bitmask: ceil(n/32) words per thread; keep <= 48 KB per block
+    int words = (n + 31) / 32;
+    int block = 256;
+    while (block > 32 && (size_t)words * block * 4 > 48 * 1024)
+        block >>= 1;
+    return block;
+}
+
+int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
+                    const pmg_axis_cfg &cfg, int num_hull, int form, const MorphEpi &me,
+                    cudaStream_t st)
+{
+    const int n = (int)(Ls.ax == 0 ? Ls.s0 : Ls.ax == 1 ? Ls.s1 : Ls.s2);
+    int block = envelope_block(n);
+    size_t smem = (size_t)((n + 31) / 32) * block * 4;
+    if (smem > 48 * 1024)
+        PMG_CUDA(cudaFuncSetAttribute(k_envelope, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    k_envelope<<<grid_for(Ls.count(), block, 1LL << 30), block, smem, st>>>(
+        fin, fout, Ls, res, cfg, num_hull, form, me);
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+static int check_shape(const int64_t *shape, int nd)
+{
+    for (int d = 0; d < nd; d++) {
+        if (shape[d] <= 0) {
+            set_error("shape[%d] = %lld must be positive", d, (long long)shape[d]);
+            return PMG_EINVAL;
+        }
+        if (shape[d] > PMG_MAX_LINE) {
+            set_error("shape[%d] = %lld exceeds the line limit %d", d, (long long)shape[d],
+                      PMG_MAX_LINE);
+            return PMG_ERANGE;
+        }
+    }
+    return PMG_OK;
+}
+
+// EDT with one ping-pong buffer: pass 0 -> out, envelope 1: out -> tmp,
+// envelope 2: tmp -> out.
+int edt3d_run(const uint8_t *img, float *out, float *tmp, const int64_t *shape, const float *res,
+              const pmg_axis_cfg *cfg, int num_hull, int form, cudaStream_t st)
+{
+    MorphEpi none{};
+    PMG_TRY(launch_pass0(img, out, all_lines(shape, 0), res[0], cfg[0], st));
+    PMG_TRY(launch_envelope(out, tmp, all_lines(shape, 1), res[1], cfg[1], num_hull,
+                            PMG_EDT_SQUARED, none, st));
+    PMG_TRY(launch_envelope(tmp, out, all_lines(shape, 2), res[2], cfg[2], num_hull, form, none,
+                            st));
+    return PMG_OK;
+}
+
+} // namespace pmg
+
+using namespace pmg;
+
+extern "C" int pmg_edt3d(const uint8_t *img, float *out, const int64_t shape[3], const float res[3],
+                         const pmg_axis_cfg cfg[3], int32_t num_hull, int32_t form, void *stream)
+{
+    if (!img || !out || !shape || !res || !cfg) {
+        set_error("pmg_edt3d: null argument");
+        return PMG_EINVAL;
+    }
+    PMG_TRY(check_shape(shape, 3));
+    if (num_hull < 0 || num_hull + 1 > kMaxHull) {
+        set_error("pmg_edt3d: num_hull %d outside [0, %d]", num_hull, kMaxHull - 1);
+        return PMG_ERANGE;
+    }
+    cudaStream_t st = as_stream(stream);
+    size_t bytes = (size_t)shape[0] * shape[1] * shape[2] * sizeof(float);
+    void *tmp = nullptr;
+    PMG_TRY(scratch_alloc(&tmp, bytes, st));
+    int s = edt3d_run(img, out, (float *)tmp, shape, res, cfg, num_hull, form, st);
+    int s2 = scratch_free(tmp, st);
+    return s != PMG_OK ? s : s2;
+}
+
+extern "C" int pmg_edt2d(const uint8_t *img, float *out, const int64_t shape2[2], const float res[2],
+                         const int32_t periodic[2], int32_t num_hull, int32_t form, void *stream)
+{
+    if (!img || !out || !shape2 || !res || !periodic) {
+        set_error("pmg_edt2d: null argument");
+        return PMG_EINVAL;
+    }
+    PMG_TRY(check_shape(shape2, 2));
+    if (num_hull < 0 || num_hull + 1 > kMaxHull) {
+        set_error("pmg_edt2d: num_hull %d outside [0, %d]", num_hull, kMaxHull - 1);
+        return PMG_ERANGE;
+    }
+    cudaStream_t st = as_stream(stream);
+    const int64_t shape[3] = {1, shape2[0], shape2[1]};
+    pmg_axis_cfg c_lin = {periodic[1], 0, 0, 0, 1, 0, 0, 0};
+    pmg_axis_cfg c_env = {periodic[0], 0, 0, 0, 1, 0, 0, 0};
+    size_t bytes = (size_t)shape2[0] * shape2[1] * sizeof(float);
+    void *tmp = nullptr;
+    PMG_TRY(scratch_alloc(&tmp, bytes, st));
+    MorphEpi none{};
+    int s = launch_pass0(img, (float *)tmp, all_lines(shape, 2), res[1], c_lin, st);
+    if (s == PMG_OK)
+        s = launch_envelope((float *)tmp, out, all_lines(shape, 1), res[0], c_env, num_hull, form,
+                            none, st);
+    int s2 = scratch_free(tmp, st);
+    return s != PMG_OK ? s : s2;
+}

@@ -1,0 +1,175 @@
+// Morphological addition / subtraction on the GPU (EDT path).
+//
+// The reference (src/pmmoto/filters/morphological_operators.py:103-228)
+// wrap-pads the padded subdomain by ceil(r/res) voxels on periodic faces
+// (communication.update_extended_buffer, core/communication.py:121-157),
+// zeroes wall planes, runs a non-periodic EDT of the extended image (or of its
+// logical_not for addition), thresholds d <= r, removes the extension and
+// zeroes wall planes again.  Here the extended image is produced by one
+// gather kernel whose periodic axes read the own region modulo its length --
+// the halo exchange becomes index arithmetic -- and the threshold, unpadding
+// and wall rule are fused into the last envelope pass, which writes the
+// uint8 result directly.
+#include "edt_internal.cuh"
+
+namespace pmg {
+
+struct ExtAxis {
+    int periodic;
+    int own_lo, own_len; // own region of the padded axis
+    int ext_lo;          // low-side extension
+    int wall_lo, wall_hi;
+    long long S, X;      // padded and extended lengths
+};
+
+struct ExtGeo {
+    ExtAxis ax[3];
+};
+
+__device__ __forceinline__ long long src_index(const ExtAxis &a, long long x, bool &zero)
+{
+    const long long p = x - a.ext_lo; // coordinate in the padded image
+    if (a.periodic) {
+        long long q = (x - (a.own_lo + a.ext_lo)) % a.own_len;
+        if (q < 0)
+            q += a.own_len;
+        return q + a.own_lo;
+    }
+    if ((a.wall_lo && p == 0) || (a.wall_hi && p == a.S - 1))
+        zero = true;
+    return p;
+}
+
+// E[x] = img[wrap(x)] (0 on wall planes); logical_not for addition.
+__global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ ext, ExtGeo G,
+                         int logical_not)
+{
+    const long long X1 = G.ax[1].X, X2 = G.ax[2].X;
+    const long long total = G.ax[0].X * X1 * X2;
+    const long long S1 = G.ax[1].S, S2 = G.ax[2].S;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long x2 = e % X2;
+        const long long r = e / X2;
+        const long long x1 = r % X1;
+        const long long x0 = r / X1;
+        bool zero = false;
+        const long long s0 = src_index(G.ax[0], x0, zero);
+        const long long s1 = src_index(G.ax[1], x1, zero);
+        const long long s2 = src_index(G.ax[2], x2, zero);
+        uint8_t v = zero ? (uint8_t)0 : img[(s0 * S1 + s1) * S2 + s2];
+        if (logical_not)
+            v = v == 0 ? 1 : 0;
+        ext[e] = v;
+    }
+}
+
+int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
+              const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
+              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st)
+{
+    ExtGeo G;
+    int64_t X[3];
+    for (int d = 0; d < 3; d++) {
+        ExtAxis &a = G.ax[d];
+        a.periodic = bc[2 * d] == PMG_BC_PERIODIC;
+        a.own_lo = pad[2 * d];
+        a.own_len = (int)(shape[d] - pad[2 * d] - pad[2 * d + 1]);
+        a.ext_lo = a.periodic ? ext[2 * d] : 0;
+        a.wall_lo = bc[2 * d] == PMG_BC_WALL;
+        a.wall_hi = bc[2 * d + 1] == PMG_BC_WALL;
+        a.S = shape[d];
+        a.X = shape[d] + (a.periodic ? ext[2 * d] + ext[2 * d + 1] : 0);
+        X[d] = a.X;
+        if (a.periodic && a.own_len <= 0) {
+            set_error("morph: empty own region on periodic axis %d", d);
+            return PMG_EINVAL;
+        }
+    }
+    const long long total = (long long)X[0] * X[1] * X[2];
+    k_extend<<<grid_for(total, 256, 1LL << 30), 256, 0, st>>>(img, E, G, dilate);
+    PMG_CHECK_LAUNCH();
+
+    pmg_axis_cfg plain = {0, 0, 0, 0, 1, 0, 0, 0};
+    MorphEpi me{};
+    me.out = out;
+    me.o0 = shape[0];
+    me.o1 = shape[1];
+    me.o2 = shape[2];
+    me.e0 = G.ax[0].ext_lo;
+    me.e1 = G.ax[1].ext_lo;
+    me.e2 = G.ax[2].ext_lo;
+    for (int d = 0; d < 3; d++) {
+        me.wall[2 * d] = G.ax[d].wall_lo;
+        me.wall[2 * d + 1] = G.ax[d].wall_hi;
+    }
+    me.r32 = (float)radius;
+    me.r64 = radius;
+    me.cmp64 = cmp64;
+    me.dilate = dilate;
+
+    PMG_TRY(launch_pass0(E, A, all_lines(X, 0), res[0], plain, st));
+    Lines L1 = all_lines(X, 1); // lines over (i, k): keep i inside the unextended range
+    L1.b1lo = me.e0;
+    L1.nb1 = (int)shape[0];
+    PMG_TRY(launch_envelope(A, B, L1, res[1], plain, 4, PMG_EDT_SQUARED, me, st));
+    Lines L2 = all_lines(X, 2); // lines over (i, j): both inside the unextended range
+    L2.b1lo = me.e0;
+    L2.nb1 = (int)shape[0];
+    L2.b2lo = me.e1;
+    L2.nb2 = (int)shape[1];
+    PMG_TRY(launch_envelope(B, nullptr, L2, res[2], plain, 4, PMG_EDT_MORPH, me, st));
+    return PMG_OK;
+}
+
+size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext)
+{
+    long long n = 1;
+    for (int d = 0; d < 3; d++)
+        n *= shape[d] + (bc[2 * d] == PMG_BC_PERIODIC ? ext[2 * d] + ext[2 * d + 1] : 0);
+    // uint8 extended image (256-byte aligned) + two float32 buffers
+    return (((size_t)n + 255) & ~(size_t)255) + 2 * (size_t)n * sizeof(float);
+}
+
+} // namespace pmg
+
+using namespace pmg;
+
+extern "C" int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3],
+                         const int32_t bc[6], const int32_t pad[6], const int32_t ext[6],
+                         const float res[3], double radius, int32_t cmp64, int32_t dilate,
+                         void *stream)
+{
+    if (!img || !out || !shape || !bc || !pad || !ext || !res) {
+        set_error("pmg_morph: null argument");
+        return PMG_EINVAL;
+    }
+    for (int d = 0; d < 3; d++) {
+        if (shape[d] <= 0) {
+            set_error("pmg_morph: shape[%d] must be positive", d);
+            return PMG_EINVAL;
+        }
+        const long long X = shape[d] + (bc[2 * d] == PMG_BC_PERIODIC ? ext[2 * d] + ext[2 * d + 1] : 0);
+        if (X > PMG_MAX_LINE) {
+            set_error("pmg_morph: extended axis %d length %lld exceeds %d", d, X, PMG_MAX_LINE);
+            return PMG_ERANGE;
+        }
+        if (ext[2 * d] < 0 || ext[2 * d + 1] < 0) {
+            set_error("pmg_morph: negative extension");
+            return PMG_EINVAL;
+        }
+    }
+    cudaStream_t st = as_stream(stream);
+    const size_t bytes = morph_scratch_bytes(shape, bc, ext);
+    void *buf = nullptr;
+    PMG_TRY(scratch_alloc(&buf, bytes, st));
+    long long nvox = 1;
+    for (int d = 0; d < 3; d++)
+        nvox *= shape[d] + (bc[2 * d] == PMG_BC_PERIODIC ? ext[2 * d] + ext[2 * d + 1] : 0);
+    uint8_t *E = (uint8_t *)buf;
+    float *A = (float *)((char *)buf + (((size_t)nvox + 255) & ~(size_t)255));
+    float *B = A + nvox;
+    int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st);
+    int s2 = scratch_free(buf, st);
+    return s != PMG_OK ? s : s2;
+}

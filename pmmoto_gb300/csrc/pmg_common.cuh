@@ -1,0 +1,79 @@
+// Shared definitions for the pmmoto_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "../../include/pmmoto_gb300.h"
+
+namespace pmg {
+
+// ---------------------------------------------------------------------------
+// error reporting: every C entry point returns a status; the message of the
+// last failure on the calling host thread is kept for pmg_last_error().
+// ---------------------------------------------------------------------------
+void set_error(const char *fmt, ...);
+
+#define PMG_CUDA(call)                                                        \
+    do {                                                                      \
+        cudaError_t e__ = (call);                                             \
+        if (e__ != cudaSuccess) {                                             \
+            ::pmg::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call,       \
+                             cudaGetErrorString(e__));                        \
+            return PMG_ECUDA;                                                 \
+        }                                                                     \
+    } while (0)
+
+#define PMG_CHECK_LAUNCH() PMG_CUDA(cudaGetLastError())
+
+#define PMG_TRY(expr)                                                         \
+    do {                                                                      \
+        int s__ = (expr);                                                     \
+        if (s__ != PMG_OK)                                                    \
+            return s__;                                                       \
+    } while (0)
+
+// Stream-ordered scratch from the device's default memory pool (kept
+// resident between calls by raising the pool's release threshold once).
+int scratch_alloc(void **p, size_t bytes, cudaStream_t st);
+int scratch_free(void *p, cudaStream_t st);
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned grid_for(long long n, int block, long long cap = 152LL * 64)
+{
+    long long g = (n + block - 1) / block;
+    if (g < 1)
+        g = 1;
+    if (g > cap)
+        g = cap;
+    return (unsigned)g;
+}
+
+// ---------------------------------------------------------------------------
+// exact float32 arithmetic (round-to-nearest, no contraction), matching the
+// reference's x86-64 build where no multiply-add is fused.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+// Intersection abscissa of the parabolas a(x-r)^2+f_r and a(x-q)^2+f_q as
+// the reference computes it (_distance.hpp:60-72): float numerator, then
+// (float)((double)num / (2.0 * factor1)).  Both operands of that division
+// are float32 values, and double has 53 >= 2*24+2 significand bits, so
+// rounding the double quotient to float equals the correctly rounded float32
+// quotient (double rounding is innocuous for division at these precisions;
+// S. A. Figueroa, "When is double rounding innocuous?", SIGNUM 1995).  The
+// float32 IEEE division __fdiv_rn therefore gives the same bits without the
+// slow FP64 path.  2*factor1 is exact in float32 (a power-of-two scaling).
+__device__ __forceinline__ float isect(float f_r, float r, float f_q, float q, float aniso)
+{
+    float factor1 = fmul(fsub(r, q), aniso);
+    float factor2 = fadd(r, q);
+    float num = fadd(fsub(f_r, f_q), fmul(factor1, factor2));
+    return __fdiv_rn(num, fmul(2.0f, factor1));
+}
+
+} // namespace pmg

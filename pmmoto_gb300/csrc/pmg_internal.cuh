@@ -1,0 +1,25 @@
+// Internal entry points shared between translation units (not part of the C ABI).
+#pragma once
+
+#include "pmg_common.cuh"
+
+namespace pmg {
+
+int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
+              const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
+              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st);
+size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext);
+
+int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shape,
+               const int32_t *bc, const int32_t *pad, const int64_t *inlet_box,
+               const int64_t *outlet_box, int mode, int phase, int *P, uint8_t *mark, int *err,
+               cudaStream_t st);
+int check_err(int *err, cudaStream_t st);
+int check_volume(const int64_t *shape);
+
+int update_buffer_run(void *img, int elem_bytes, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, cudaStream_t st);
+int count_eq_async(const uint8_t *img, const int64_t *shape, const int64_t *box, uint8_t value,
+                   unsigned long long *d_cnt, cudaStream_t st);
+
+} // namespace pmg

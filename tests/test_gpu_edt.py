@@ -1,0 +1,93 @@
+"""EDT parity: CUDA path vs the oracle and the reference's golden fixtures."""
+
+import hashlib
+import json
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def D():
+    from pmmoto_gb300.filters import distance
+    return distance
+
+
+def test_kat_lines(D):
+    # the 1-D known answers are single lines of a (1, 1, n) volume along axis 2
+    img = np.array([1, 1, 0, 0, 1, 1, 0, 1, 1, 1, 1, 1, 1, 0, 1], dtype=np.uint8)
+    out = D.edt3d(img.reshape(len(img), 1, 1), squared=True).ravel()
+    np.testing.assert_array_equal(out, O.initial_envelope_1d(img))
+
+
+@pytest.mark.parametrize("ci", range(6))
+def test_edt3d_golden(D, golden, golden_meta, ci):
+    c = golden_meta["edt3d_cases"][ci]
+    out = D.edt3d(golden[f"edt3d_{ci}_in"], periodic=c["periodic"], resolution=c["resolution"], squared=True)
+    np.testing.assert_array_equal(out, golden[f"edt3d_{ci}_out"])
+
+
+def test_edt3d_labels(D, golden):
+    np.testing.assert_array_equal(D.edt3d(golden["edt3d_labels_in"], squared=True), golden["edt3d_labels_out"])
+
+
+def test_edt2d(D, golden):
+    np.testing.assert_array_equal(D.edt2d(golden["edt2d_in"], periodic=(True, True)), golden["edt2d_out_p"])
+    np.testing.assert_array_equal(D.edt2d(golden["edt2d_in"]), golden["edt2d_out_n"])
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_edt3d_random_vs_oracle(D, seed):
+    rng = np.random.default_rng(100 + seed)
+    shape = tuple(int(x) for x in rng.integers(1, 45, 3))
+    p0 = float(rng.choice([0.0, 0.01, 0.1, 0.4, 0.9, 1.0]))
+    img = (rng.random(shape) >= p0).astype(np.uint8)
+    if seed % 4 == 3:
+        img = rng.integers(0, 4, shape).astype(np.uint8)
+    per = tuple(bool(x) for x in rng.integers(0, 2, 3))
+    res = [(1.0, 1.0, 1.0), (0.01, 0.01, 0.01), (1.0, 0.32325245, 233.0), (1 / 3, 1 / 3, 1 / 7)][seed % 4]
+    got = D.edt3d(img, periodic=per, resolution=res, squared=True)
+    want = O.edt3d(img, periodic=per, resolution=res, squared=True)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(D.edt3d(img, periodic=per, resolution=res), np.sqrt(want))
+
+
+def test_edt_subdomain_golden(D, golden, golden_meta):
+    from tests._helpers import geom_from_meta
+    for ci, case in enumerate(golden_meta["sub_cases"]):
+        g = geom_from_meta(O, case["geom"])
+        sd = _FakeSD(g)
+        np.testing.assert_array_equal(D.edt(golden[f"sub_{ci}_img"], sd), golden[f"sub_{ci}_edt"])
+
+
+class _FakeDomain:
+    def __init__(self, g):
+        self.resolution = g.resolution
+        self.periodic = g.periodic
+        self.boundary_types = g.boundary_types
+        self.num_subdomains = 1
+
+
+class _FakeSD:
+    def __init__(self, g):
+        self.domain = _FakeDomain(g)
+        self.pad = g.pad
+
+
+def test_c1_full_size_hashes(D, golden_meta):
+    """128^3 periodic pack (400 spheres): EDT digests equal the reference's."""
+    for seed, want in golden_meta["c1_full"].items():
+        r2 = np.random.default_rng(int(seed))
+        sph = np.c_[r2.random((400, 3)), r2.uniform(0.03, 0.08, 400)]
+        g = O.Geom((128, 128, 128), boundary_types=(("periodic",) * 2,) * 3)
+        img = O.gen_pm_spheres_domain(g, sph)
+        assert hashlib.sha256(img.tobytes()).hexdigest() == want["img_sha"]
+        own = np.ascontiguousarray(img[1:-1, 1:-1, 1:-1])
+        e3 = D.edt3d(own, periodic=(True, True, True))
+        assert hashlib.sha256(e3.tobytes()).hexdigest() == want["edt3d_sha"]
+        es = D.edt(img, _FakeSD(g))
+        assert hashlib.sha256(es.tobytes()).hexdigest() == want["edt_sd_sha"]

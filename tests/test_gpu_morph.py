@@ -1,0 +1,58 @@
+"""Erode / dilate parity: CUDA path vs the reference fixtures and the oracle."""
+
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests._helpers import geom_from_meta, sd_from_meta
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def M():
+    from pmmoto_gb300.filters import morphological_operators
+    return morphological_operators
+
+
+@pytest.mark.parametrize("ci", range(5))
+def test_morph_golden(M, golden, golden_meta, ci):
+    case = golden_meta["sub_cases"][ci]
+    sd = sd_from_meta(case["geom"])
+    img = golden[f"sub_{ci}_img"]
+    for ri, r in enumerate(case["radii"]):
+        np.testing.assert_array_equal(M.erode(sd, img, r), golden[f"sub_{ci}_erode_{ri}"])
+        np.testing.assert_array_equal(M.dilate(sd, img, r), golden[f"sub_{ci}_dilate_{ri}"])
+        np.testing.assert_array_equal(M.erode(sd, img, np.float64(r)), golden[f"sub_{ci}_erode64_{ri}"])
+
+
+@pytest.mark.parametrize("kinds", list(itertools.product(["end", "wall", "periodic"], repeat=3))[::2])
+def test_morph_random_vs_oracle(M, kinds):
+    rng = np.random.default_rng(sum(map(ord, "".join(kinds))))
+    vox = (20, 17, 23)
+    box = tuple((0.0, v / 20) for v in vox)
+    bts = tuple((k, k) for k in kinds)
+    from pmmoto_gb300.core import initialize
+    sd = initialize(vox, box=box, boundary_types=bts)
+    g = O.Geom(vox, boundary_types=bts, box=box)
+    img = (rng.random(sd.voxels) > 0.3).astype(np.uint8)
+    img = O.update_buffer(g, img)
+    for r in (0.05, 0.1, np.float64(0.15), 0.24):
+        np.testing.assert_array_equal(M.erode(sd, img, r), O.erode(g, img, r))
+        np.testing.assert_array_equal(M.dilate(sd, img, r), O.dilate(g, img, r))
+    np.testing.assert_array_equal(M.opening(sd, img, 0.1), O.opening(g, img, 0.1))
+    np.testing.assert_array_equal(M.closing(sd, img, 0.1), O.closing(g, img, 0.1))
+
+
+def test_morph_errors(M):
+    from pmmoto_gb300.core import initialize
+    sd = initialize((10, 10, 10), boundary_types=(("periodic",) * 2,) * 3)
+    img = np.ones(sd.voxels, np.uint8)
+    with pytest.raises(ValueError):
+        M.erode(sd, img, 0.01)  # radius below the resolution
+    with pytest.raises(SystemExit):
+        M.erode(sd, img, 1.5)  # extension beyond the subdomain
+    with pytest.raises(NotImplementedError):
+        M.erode(sd, img, 0.2, fft=True)
