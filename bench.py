@@ -1,0 +1,421 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 voxel-morphology path.
+
+Workload (one "step" = one dense exact drainage curve): a 512^3 sphere pack
+(3,000 spheres, centres uniform in the unit box, radii uniform in
+[0.02, 0.05]) padded to 512 x 514 x 514, walls on the y and z faces, inlet at
+x = 0 and outlet at x = max; 40 probe radii uniform from 1 to 20 voxels
+(capillary pressures 2 / (r * res)), each radius running erosion by the EDT,
+inlet-connected components, the multiphase constraint, dilation, the
+outlet-connected wetting phase and the saturation count -- PMMoTo's
+drainage(..., mode="distance") with the standard method.  Inputs are
+synthetic (seeded), the image stays resident in HBM for `value`; `e2e` feeds
+host buffers through the package's C ABI each step.
+
+Prints one JSON line.  `--impl reference` times the CPU restatement of the
+same path (the oracle, all host threads) on a bounded sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_VOX = 512
+N_SPHERES = 3000
+R_LO, R_HI = 0.02, 0.05
+N_RADII = 40
+METRIC = "drainage curves/s (dense exact, 40 radii, 512^3 pack)"
+UNIT = "curves/s"
+
+
+def workload_config():
+    return {"workload": "sphere-pack drainage 512^3 (512x514x514 padded), 3000 spheres r~U[0.02,0.05], "
+                        "walls y/z, inlet x-, outlet x+, 40 radii linspace(1,20) voxels, mode=distance",
+            "voxels": [N_VOX, N_VOX + 2, N_VOX + 2], "spheres": N_SPHERES, "radii": N_RADII,
+            "l2": "inputs larger than L2 (135 MB uint8 image, 1.1 GB float32 EDT scratch per pass)"}
+
+
+def make_pack(seed):
+    rng = np.random.default_rng(seed)
+    return np.c_[rng.random((N_SPHERES, 3)), rng.uniform(R_LO, R_HI, N_SPHERES)]
+
+
+def radii_for(res):
+    r_vox = np.linspace(1, 20, N_RADII)
+    pcs = sorted(list(2.0 / (r_vox * res)))
+    return pcs, [2.0 * 1 / pc * np.cos(np.deg2rad(0)) for pc in pcs]
+
+
+def geom_kwargs():
+    return dict(box=((0.0, 1.0),) * 3, boundary_types=(("end", "end"), ("wall", "wall"), ("wall", "wall")),
+                inlet=((True, False), (False, False), (False, False)),
+                outlet=((False, True), (False, False), (False, False)))
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def prof_read(L):
+    names = ctypes.create_string_buffer(8192)
+    cap = 64
+    ms = (ctypes.c_double * cap)()
+    by = (ctypes.c_double * cap)()
+    n = (ctypes.c_longlong * cap)()
+    cnt = ctypes.c_int32(0)
+    L.pmg_prof_read(names, 8192, ms, by, n, cap, ctypes.byref(cnt))
+    keys = names.value.decode().split("\n")
+    return {keys[i]: {"ms": ms[i], "bytes": by[i], "launches": n[i]} for i in range(cnt.value)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_gpu(args):
+    import torch
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import pmmoto_gb300 as P
+    from pmmoto_gb300 import _lib
+    from pmmoto_gb300.filters import equilibrium_distribution as ED
+
+    L = _lib.lib()
+    L.pmg_launch_count.restype = ctypes.c_longlong
+    sd = P.initialize((N_VOX,) * 3, **geom_kwargs())
+    sph = make_pack(1234 + rank)
+    t_setup = time.time()
+    pm_t = P.domain_generation.gen_pm_spheres_domain(sd, torch.as_tensor(sph, device="cuda"))
+    pm = P.domain_generation.PorousMedia(sd, pm_t.img)
+    mp0 = P.domain_generation.gen_mp_constant(pm, 2)
+    pcs, radii = radii_for(sd.domain.resolution[0])
+    _ = pm.max_distance  # cached once per medium, as PorousMedia caches it
+    phi = pm.porosity
+    setup_s = time.time() - t_setup
+
+    def step():
+        mp = P.domain_generation.Multiphase(pm, mp0.img, 2)
+        counts, _ = ED.drainage_counts(mp, radii, mode="distance")
+        return counts
+
+    for _ in range(args.warmup):
+        counts = step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    L.pmg_prof_reset()
+    L.pmg_prof_enable(1)
+    n0 = L.pmg_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            counts = step()
+        e1.record()
+        torch.cuda.synchronize()
+    L.pmg_prof_enable(0)
+    launches = L.pmg_launch_count() - n0
+    ms = e0.elapsed_time(e1)
+    prof = prof_read(L)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    sat = [float(c / np.prod(sd.domain.voxels)) / phi for c in counts]
+
+    # end to end: host image in pinned memory -> device, drainage, saturations back
+    host_pm = torch.empty(pm_t.img.shape, dtype=torch.uint8, pin_memory=True)
+    host_pm.copy_(pm_t.img.cpu())
+    host_mp = torch.empty_like(host_pm, pin_memory=True)
+    host_mp.copy_(mp0.img.cpu())
+    dev_pm = torch.empty_like(pm_t.img)
+    dev_mp = torch.empty_like(pm_t.img)
+
+    def e2e_step():
+        dev_pm.copy_(host_pm, non_blocking=True)
+        dev_mp.copy_(host_mp, non_blocking=True)
+        pm_e = P.domain_generation.PorousMedia(sd, dev_pm)
+        pm_e._porosity, pm_e._max_distance = phi, pm.max_distance
+        mp_e = P.domain_generation.Multiphase(pm_e, dev_mp, 2)
+        c, _ = ED.drainage_counts(mp_e, radii, mode="distance")
+        return [float(x / np.prod(sd.domain.voxels)) / phi for x in c]  # counts came back to the host
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sat_e = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    assert sat_e == sat, "end-to-end path disagrees with the resident path"
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = load_peaks()
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else ("none", {"ms": 1, "bytes": 0, "launches": 1})
+    ach = top[1]["bytes"] / (top[1]["ms"] / 1e3) / 1e9 if top[1]["ms"] > 0 else 0.0
+    traffic = load_traffic(top[0])
+    total_prof_ms = sum(v["ms"] for v in prof.values())
+    out = {
+        "metric": METRIC, "value": world * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(workload_config(), parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+        "clocks": clk.summary(),
+        "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(host_pm.numel() * 2), "d2h_bytes_per_step": int(8 * N_RADII)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": top[0], "achieved": round(ach, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(ach / peak, 4), "peak_kind": peak_kind,
+                     "traffic": traffic, "launches": int(top[1]["launches"]),
+                     "avg_launch_ms": top[1]["ms"] / max(1, top[1]["launches"]),
+                     "share": round(top[1]["ms"] / total_prof_ms, 3) if total_prof_ms else None},
+        "kernels": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                        "GBps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+                    for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])},
+        "saturation_first_last": [sat[0], sat[-1]],
+        "porosity": phi,
+        "setup_s": round(setup_s, 3),
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(sd_voxels=sd.voxels, pm_img=pm_t.img.cpu().numpy(), pcs=pcs)
+    print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def load_traffic(kernel):
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    v = d.get(kernel)
+    return v.get("bytes_per_launch") if isinstance(v, dict) else None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle: CPU restatement of the reference, all host threads)
+# ---------------------------------------------------------------------------
+
+SAMPLE_IDX = (20,)
+
+
+def cpu_baseline(sd_voxels=None, pm_img=None, pcs=None):
+    from oracle import oracle as O
+
+    L = O.lib()
+    L.or_num_threads.restype = ctypes.c_int
+    cores = int(L.or_num_threads())
+    g = O.Geom((N_VOX,) * 3, **{k: v for k, v in geom_kwargs().items()})
+    if pm_img is None:
+        pm_img = O.gen_pm_spheres_domain(g, make_pack(1234))
+    if pcs is None:
+        pcs, _ = radii_for(g.resolution[0])
+    sample = [pcs[i] for i in SAMPLE_IDX]
+    dmax = O.max_distance(g, pm_img)  # once per medium in the reference (PorousMedia caches it)
+    t0 = time.perf_counter()
+    O.drainage(g, pm_img, sample, dmax=dmax)
+    dt = time.perf_counter() - t0
+    per_curve = dt * N_RADII / len(sample)
+    return {"value": 1.0 / per_curve, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(sample)} of {N_RADII} radii (capillary pressures #{SAMPLE_IDX}) of the same 512^3 "
+                      f"drainage, {dt:.1f} s, scaled x{N_RADII / len(sample):g} to one curve"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    g = O.Geom((N_VOX,) * 3, **geom_kwargs())
+    pm_img = O.gen_pm_spheres_domain(g, make_pack(1234))
+    pcs, _ = radii_for(g.resolution[0])
+    for _ in range(min(args.warmup, 1)):
+        pass  # the CPU path has nothing to warm up beyond its first call
+    vals = []
+    cb = None
+    for _ in range(args.steps):
+        cb = cpu_baseline(pm_img=pm_img, pcs=pcs)
+        vals.append(1.0 / cb["value"])
+    v = len(vals) / sum(vals)
+    cb["value"] = v
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
+           "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_case(args):
+    """Single-operator cases on a seeded random medium (for ncu captures and
+    per-operator rates): 'edt' = periodic edt3d, 'cc' = connected components
+    with periodic merge, 'morph' = erosion (EDT path); N^3 voxels."""
+    import torch
+
+    import pmmoto_gb300 as P
+    from pmmoto_gb300 import _lib
+    from pmmoto_gb300.filters import connected_components as CC
+    from pmmoto_gb300.filters import distance as D
+    from pmmoto_gb300.filters import morphological_operators as M
+    from pmmoto_gb300.core.geometry import geo_of
+
+    n = args.n
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    img = (torch.rand((n, n, n), device="cuda", generator=g) >= 0.35).to(torch.uint8)
+    sd = P.initialize((n - 2,) * 3, boundary_types=(("periodic", "periodic"),) * 3)
+    geo = geo_of(sd)
+    out = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
+    cfg = D.edt3d_cfg((True, True, True))
+    res = np.ones(3, np.float32)
+
+    def op():
+        if args.case == "edt":
+            D.edt3d_device(img, res, cfg, True, out)
+        elif args.case == "cc":
+            CC.connect_components_device(img, geo)
+        else:
+            M.morph_device(geo, img, 4.0 * sd.domain.resolution[0], False)
+
+    for _ in range(args.warmup):
+        op()
+    torch.cuda.synchronize()
+    L = _lib.lib()
+    L.pmg_prof_reset()
+    L.pmg_prof_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        op()
+    e1.record()
+    torch.cuda.synchronize()
+    L.pmg_prof_enable(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    prof = prof_read(L)
+    peak, _ = load_peaks()
+    print(json.dumps({"case": args.case, "n": n, "ms": ms, "gvox_s": n**3 / ms / 1e6,
+                      "kernels": {k: {"ms_per_step": v["ms"] / args.steps, "launches": v["launches"],
+                                      "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] else None,
+                                      "frac": v["bytes"] / (v["ms"] / 1e3) / 1e9 / peak if v["ms"] else None}
+                                  for k, v in prof.items()}}), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph"])
+    ap.add_argument("--n", type=int, default=512, help="volume side of the single-operator cases")
+    args = ap.parse_args()
+    if args.case != "drainage":
+        run_case(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

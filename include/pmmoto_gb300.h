@@ -96,12 +96,19 @@ int pmg_edt2d(const uint8_t *img, float *out, const int64_t shape2[2],
  *   radius, cmp64      compare sqrt(d2) <= radius in float64 when cmp64 is
  *                      1 (a numpy float64 radius) or in float32 when 0 (a
  *                      Python float radius, numpy's weak-scalar rule)
+ *   ball_sq            < 0 for the EDT path above.  >= 0 selects the FFT
+ *                      path of the reference (fft=True): scipy fftconvolve
+ *                      with the structuring element {i^2+j^2+k^2 <= R2},
+ *                      R2 = (radius/res)^2 in float64 (gen_struct_element,
+ *                      :66-100), thresholded; that equals comparing the
+ *                      integer squared voxel-unit distance with
+ *                      ball_sq = floor(R2), which is what is done.
  * img and out have the padded shape; out gets 0/1 with wall planes 0.
  */
 int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3],
               const int32_t bc[6], const int32_t pad[6], const int32_t ext[6],
               const float res[3], double radius, int32_t cmp64, int32_t dilate,
-              void *stream);
+              double ball_sq, void *stream);
 
 /*
  * Connected components of a padded single-rank subdomain image (elements of
@@ -175,14 +182,16 @@ int pmg_max_f32(const float *x, const int64_t shape[3], const int64_t box[6],
  * pm_img by r_erode, keep the inlet-connected part when `inlet`, and if any
  * voxel is left, constrain by the inlet-connected phase 1 of mp_img (when
  * mp_img is not NULL and holds phase 1) and dilate by r_dilate.  ratio_* are
- * ceil(radius/res) per axis (gen_struct_ratio); cmp_* as in pmg_morph.
+ * ceil(radius/res) per axis (gen_struct_ratio); cmp_* and ball_* as in
+ * pmg_morph (ball_* >= 0 selects the reference's FFT erosion / dilation:
+ * mode "morph" uses both, mode "hybrid" only ball_dilate).
  */
 int pmg_porosimetry(const uint8_t *pm_img, const uint8_t *mp_img, uint8_t *out,
                     const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],
                     const int64_t inlet_box[6], const float res[3], double r_erode,
                     int32_t cmp_erode, const int32_t ratio_erode[3], double r_dilate,
                     int32_t cmp_dilate, const int32_t ratio_dilate[3], int32_t inlet,
-                    void *stream);
+                    double ball_erode, double ball_dilate, void *stream);
 
 /*
  * drainage, standard method (filters/equilibrium_distribution.py:25-179)
@@ -193,14 +202,32 @@ int pmg_porosimetry(const uint8_t *pm_img, const uint8_t *mp_img, uint8_t *out,
  * mp = (morph == 1 && connected == 2) ? 1 : mp, the reservoir refill
  * (rpad slabs set to 1) and counts[k] (host) = number of own voxels (own_box)
  * equal to 2 -- the numerator of Multiphase.get_saturation.  mp_img (device)
- * is updated in place; ratios holds ceil(r/res) per axis per radius.
+ * is updated in place; ratios holds ceil(r/res) per axis per radius;
+ * ball_erode / ball_dilate (host arrays or NULL) select the FFT-mode ball per
+ * radius as in pmg_porosimetry.
  */
 int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
                  const int32_t bc[6], const int32_t pad[6], const int32_t rpad[6],
                  const int64_t own_box[6], const int64_t inlet_box[6],
                  const int64_t outlet_box[6], const float res[3], int32_t n_radii,
                  const double *radii, const int32_t *active, const int32_t *ratios,
-                 int64_t *counts, void *stream);
+                 const double *ball_erode, const double *ball_dilate, int64_t *counts,
+                 void *stream);
+
+/* Number of kernels this library has launched in the process. */
+long long pmg_launch_count(void);
+
+/*
+ * Per-kernel timing: when enabled, every launch records a CUDA event pair on
+ * its stream with the launch's algorithmic bytes.  pmg_prof_read resolves
+ * them (synchronizing on the events) into per-kernel totals: `names` gets
+ * newline-separated kernel names, ms / bytes / launches the totals, *count
+ * the number of kernels (at most cap).  pmg_prof_reset clears the totals.
+ */
+int pmg_prof_enable(int32_t on);
+int pmg_prof_reset(void);
+int pmg_prof_read(char *names, size_t names_len, double *ms, double *bytes,
+                  long long *launches, int32_t cap, int32_t *count);
 
 /* Message of the last failure on this host thread (empty if none). */
 int pmg_last_error(char *buf, size_t len);

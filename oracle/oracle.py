@@ -393,22 +393,47 @@ def struct_ratio(resolution, radius):
     return tuple(int(math.ceil(radius / res)) for res in resolution)
 
 
-def addition(geom: Geom, img, radius):
-    """addition, morphological_operators.py:103-149 (fft=False)."""
-    ratio = struct_ratio(geom.resolution, radius)
+def struct_element(resolution, radius):
+    """gen_struct_element, morphological_operators.py:66-100."""
+    ratio = struct_ratio(resolution, radius)
+    grids = [np.linspace(-r, r, r * 2 + 1) for r in ratio]
+    xg, yg, zg = np.meshgrid(*grids, indexing="ij")
+    s = xg**2 + yg**2 + zg**2
+    r = radius / resolution[0]
+    return ratio, np.array(s <= r * r, dtype=np.uint8)
+
+
+def addition(geom: Geom, img, radius, fft=False):
+    """addition, morphological_operators.py:103-149."""
+    ratio, se = struct_element(geom.resolution, radius)
     halo_img, halo = update_extended_buffer(geom, img, ratio)
-    d = edt3d(np.logical_not(halo_img), resolution=geom.resolution)
-    out = np.where((d <= radius), 1, 0).astype(np.uint8)
+    if fft:
+        from scipy.signal import fftconvolve
+
+        out = (fftconvolve(halo_img, se, mode="same") > 0.1).astype(np.uint8)
+    else:
+        d = edt3d(np.logical_not(halo_img), resolution=geom.resolution)
+        out = np.where((d <= radius), 1, 0).astype(np.uint8)
     out = _unpad(out, halo)
     return geom.set_wall_bcs(out)
 
 
-def subtraction(geom: Geom, img, radius):
-    """subtraction, morphological_operators.py:175-228 (fft=False)."""
-    ratio = struct_ratio(geom.resolution, radius)
+def subtraction(geom: Geom, img, radius, fft=False):
+    """subtraction, morphological_operators.py:175-228."""
+    ratio, se = struct_element(geom.resolution, radius)
     halo_img, halo = update_extended_buffer(geom, img, ratio)
-    d = edt3d(halo_img, resolution=geom.resolution)
-    out = np.where((d <= radius), 0, 1).astype(np.uint8)
+    if fft:
+        from scipy.signal import fftconvolve
+
+        _pad = 1
+        if any(b == END for bt in geom.boundary_types for b in bt):
+            _pad = int(np.max(ratio))
+        _img = np.pad(halo_img, _pad, mode="constant", constant_values=1)
+        _img = fftconvolve(_img, se, mode="same") > (se.sum() - 0.1)
+        out = _unpad(_img, tuple((_pad, _pad) for _ in range(3))).astype(np.uint8)
+    else:
+        d = edt3d(halo_img, resolution=geom.resolution)
+        out = np.where((d <= radius), 0, 1).astype(np.uint8)
     out = _unpad(out, halo)
     return geom.set_wall_bcs(out)
 
@@ -568,8 +593,8 @@ def isolated_img(geom, img, phase=None):
 # Porosimetry and drainage
 # --------------------------------------------------------------------------
 
-def porosimetry(geom: Geom, pm_img, radius, inlet=False, mp_img=None):
-    """porosimetry, porosimetry.py:84-160 with mode="distance"."""
+def porosimetry(geom: Geom, pm_img, radius, inlet=False, mp_img=None, mode="distance"):
+    """porosimetry, porosimetry.py:84-160."""
     if isinstance(radius, (int, float)):
         r_e = r_d = radius
     elif isinstance(radius, list) and len(radius) == 2:
@@ -580,14 +605,14 @@ def porosimetry(geom: Geom, pm_img, radius, inlet=False, mp_img=None):
         ratio = struct_ratio(geom.resolution, r)
         if any(geom.voxels[d] < ratio[d] for d in range(3)):
             raise SystemExit(1)
-    res = subtraction(geom, pm_img, r_e)
+    res = subtraction(geom, pm_img, r_e, fft=(mode == "morph"))
     if inlet:
         res = inlet_connected_img(geom, res)
     if np.count_nonzero(res == 1) > 0:
         if mp_img is not None and np.count_nonzero(mp_img == 1) > 0:
             n_conn = inlet_connected_img(geom, mp_img, 1)
             res = np.where((res != 1) | (n_conn != 1), 0, res)
-        res = addition(geom, res, r_d)
+        res = addition(geom, res, r_d, fft=(mode in ("morph", "hybrid")))
     return res.astype(np.uint8)
 
 
@@ -604,8 +629,8 @@ def max_distance(geom: Geom, pm_img):
     return float(np.amax(d))
 
 
-def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1):
-    """drainage + _standard_method (equilibrium_distribution.py:25-179), mode="distance".
+def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1, mode="distance", dmax=None):
+    """drainage + _standard_method (equilibrium_distribution.py:25-179).
 
     Returns (saturations, final multiphase image)."""
     if isinstance(capillary_pressures, (int, float)):
@@ -614,7 +639,6 @@ def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1):
         capillary_pressures = sorted(capillary_pressures)
     mp_img = np.where(pm_img == 1, 2, 0).astype(np.uint8)
     phi = porosity(geom, pm_img)
-    dmax = None
     sat = np.zeros(len(capillary_pressures))
     for n, pc in enumerate(capillary_pressures):
         radius = 0 if pc == 0 else 2.0 * gamma / pc * np.cos(np.deg2rad(0))
@@ -626,7 +650,7 @@ def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1):
             if radius > dmax:
                 morph = np.zeros_like(pm_img, dtype=np.uint8)
             else:
-                morph = porosimetry(geom, pm_img, radius, inlet=True, mp_img=mp_img)
+                morph = porosimetry(geom, pm_img, radius, inlet=True, mp_img=mp_img, mode=mode)
         w = outlet_connected_img(geom, mp_img, 2)
         mp_img = np.where((morph == 1) & (w == 2), 1, mp_img)
         mp_img = geom.update_reservoir(mp_img, mp_img.dtype.type(1))
@@ -635,8 +659,8 @@ def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1):
     return sat, mp_img
 
 
-def pore_size_distribution(geom: Geom, pm_img, radii, inlet=False):
-    """pore_size_distribution with explicit radii (porosimetry.py:163-227), mode="distance"."""
+def pore_size_distribution(geom: Geom, pm_img, radii, inlet=False, mode="distance"):
+    """pore_size_distribution with explicit radii (porosimetry.py:163-227)."""
     if isinstance(radii, (int, float)):
         radii = [radii]
     elif isinstance(radii, list):
@@ -645,7 +669,7 @@ def pore_size_distribution(geom: Geom, pm_img, radii, inlet=False):
         radii = np.sort(np.asarray(radii))[::-1]
     out = np.zeros_like(pm_img, dtype=np.double)
     for radius in radii:
-        tmp = porosimetry(geom, pm_img, radius, inlet=inlet)
+        tmp = porosimetry(geom, pm_img, radius, inlet=inlet, mode=mode)
         if np.any(tmp):
             out = np.where((pm_img == 1) & (out == 0) & (tmp == 1), radius, out)
     return out

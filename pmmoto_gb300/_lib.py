@@ -40,9 +40,19 @@ class PmgError(RuntimeError):
 def _declare(L):
     P = ctypes.c_void_p
     i32, i64 = ctypes.c_int32, ctypes.c_int64
+    f64 = ctypes.c_double
     sig = {
         "pmg_edt3d": [P, P, P, P, P, i32, i32, P],
         "pmg_edt2d": [P, P, P, P, P, i32, i32, P],
+        "pmg_morph": [P, P, P, P, P, P, P, f64, i32, i32, f64, P],
+        "pmg_cc_label": [P, i32, P, P, P, P, P, P],
+        "pmg_cc_select": [P, P, i32, P, P, P, P, P, i32, i32, P],
+        "pmg_spheres": [P, i64, P, P, P, P, P, P, P, P],
+        "pmg_update_buffer": [P, i32, P, P, P, P],
+        "pmg_count_eq": [P, P, P, i32, P, P],
+        "pmg_max_f32": [P, P, P, P, P],
+        "pmg_porosimetry": [P, P, P, P, P, P, P, P, f64, i32, P, f64, i32, P, i32, f64, f64, P],
+        "pmg_drainage": [P, P, P, P, P, P, P, P, P, P, i32, P, P, P, P, P, P, P],
         "pmg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
     }
     for name, args in sig.items():

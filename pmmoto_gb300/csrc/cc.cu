@@ -437,16 +437,32 @@ static int uf_build(const T *img, int *P, const int64_t *shape, const int32_t *b
     const long long n = shape[0] * shape[1] * shape[2];
     Vol3 V{shape[0], shape[1], shape[2]};
     const int block = 256;
-    k_cc_init<T><<<grid_for(n, block, 1LL << 30), block, 0, st>>>(img, P, n);
+    {
+        const int ps__ = prof_begin("k_cc_init", st);
+        k_cc_init<T><<<grid_for(n, block, 1LL << 30), block, 0, st>>>(img, P, n);
+        prof_end(ps__, (double)n * (sizeof(T) + 4), st);
+    }
     PMG_CHECK_LAUNCH();
-    k_cc_merge<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P, V, err);
+    {
+        const int ps__ = prof_begin("k_cc_merge", st);
+        k_cc_merge<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P, V, err);
+        prof_end(ps__, (double)n * (sizeof(T) + 4), st);
+    }
     PMG_CHECK_LAUNCH();
     if (twins && any_periodic(bc)) {
-        k_cc_twins<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P,
+        {
+            const int ps__ = prof_begin("k_cc_twins", st);
+            k_cc_twins<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P,
                                                                          make_twins(shape, bc, pad), err);
+            prof_end(ps__, 0.0, st);
+        }
         PMG_CHECK_LAUNCH();
     }
-    k_cc_flatten<<<grid_for(n, block, 152LL * 32), block, 0, st>>>(P, n, err);
+    {
+        const int ps__ = prof_begin("k_cc_flatten", st);
+        k_cc_flatten<<<grid_for(n, block, 152LL * 32), block, 0, st>>>(P, n, err);
+        prof_end(ps__, (double)n * 8, st);
+    }
     PMG_CHECK_LAUNCH();
     return PMG_OK;
 }
@@ -590,8 +606,12 @@ static int periodic_renumber(uint64_t *L, const int64_t *shape, const int32_t *b
         PMG_TRY(scratch_alloc((void **)&d_i2, rows * 4, st));
         PMG_TRY(scratch_alloc((void **)&d_f, rows, st));
         PMG_TRY(scratch_alloc((void **)&d_nsel, 2 * sizeof(int), st));
-        k_seam_pairs<<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(L, V, own, nb, onb, oown, d_k,
+        {
+            const int ps__ = prof_begin("k_seam_pairs", st);
+            k_seam_pairs<<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(L, V, own, nb, onb, oown, d_k,
                                                                       d_i);
+            prof_end(ps__, (double)rows * 28, st);
+        }
         PMG_CHECK_LAUNCH();
         size_t tb = 0, tb2 = 0, tb3 = 0;
         PMG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, d_k, d_k2, d_i, d_i2, (int)rows, 0, 64, st));
@@ -601,7 +621,11 @@ static int periodic_renumber(uint64_t *L, const int64_t *shape, const int32_t *b
         void *d_t = nullptr;
         PMG_TRY(scratch_alloc(&d_t, tbs, st));
         PMG_CUDA(cub::DeviceRadixSort::SortPairs(d_t, tbs, d_k, d_k2, d_i, d_i2, (int)rows, 0, 64, st));
-        k_head_flags<<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(d_k2, rows, d_f);
+        {
+            const int ps__ = prof_begin("k_head_flags", st);
+            k_head_flags<<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(d_k2, rows, d_f);
+            prof_end(ps__, (double)rows * 9, st);
+        }
         PMG_CHECK_LAUNCH();
         PMG_CUDA(cub::DeviceSelect::Flagged(d_t, tbs, d_i2, d_f, d_i, d_nsel, (int)rows, st));
         PMG_CUDA(cub::DeviceSelect::Flagged(d_t, tbs, d_k2, d_f, d_k3, d_nsel + 1, (int)rows, st));
@@ -709,19 +733,35 @@ static int periodic_renumber(uint64_t *L, const int64_t *shape, const int32_t *b
     if (nbnd > 0) {
         PMG_CUDA(cudaMemcpyAsync(d_bl, bl.data(), (size_t)nbnd * 8, cudaMemcpyHostToDevice, st));
         PMG_CUDA(cudaMemcpyAsync(d_bg, bg.data(), (size_t)nbnd * 8, cudaMemcpyHostToDevice, st));
-        k_lut_flags<<<grid_for(nbnd, 256, 1LL << 30), 256, 0, st>>>(d_bl, d_bg, nbnd, d_flag, d_lut);
+        {
+            const int ps__ = prof_begin("k_lut_flags", st);
+            k_lut_flags<<<grid_for(nbnd, 256, 1LL << 30), 256, 0, st>>>(d_bl, d_bg, nbnd, d_flag, d_lut);
+            prof_end(ps__, (double)nbnd * 25, st);
+        }
         PMG_CHECK_LAUNCH();
     }
-    k_lut_nonflag<<<grid_for(m, 256, 1LL << 30), 256, 0, st>>>(d_flag, m, d_nf);
+    {
+        const int ps__ = prof_begin("k_lut_nonflag", st);
+        k_lut_nonflag<<<grid_for(m, 256, 1LL << 30), 256, 0, st>>>(d_flag, m, d_nf);
+        prof_end(ps__, (double)m * 5, st);
+    }
     PMG_CHECK_LAUNCH();
     size_t tb = 0;
     PMG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, d_nf, d_rank, (int)m, st));
     void *d_t = nullptr;
     PMG_TRY(scratch_alloc(&d_t, tb, st));
     PMG_CUDA(cub::DeviceScan::ExclusiveSum(d_t, tb, d_nf, d_rank, (int)m, st));
-    k_lut_fill<<<grid_for(m, 256, 1LL << 30), 256, 0, st>>>(d_flag, d_rank, m, global_id, d_lut);
+    {
+        const int ps__ = prof_begin("k_lut_fill", st);
+        k_lut_fill<<<grid_for(m, 256, 1LL << 30), 256, 0, st>>>(d_flag, d_rank, m, global_id, d_lut);
+        prof_end(ps__, (double)m * 13, st);
+    }
     PMG_CHECK_LAUNCH();
-    k_apply_lut<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(L, n, d_lut);
+    {
+        const int ps__ = prof_begin("k_apply_lut", st);
+        k_apply_lut<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(L, n, d_lut);
+        prof_end(ps__, (double)n * 16, st);
+    }
     PMG_CHECK_LAUNCH();
     const long long nloc = (long long)count - nbnd;
     int64_t max_label = (int64_t)(nloc + (long long)global_id);
@@ -752,7 +792,11 @@ static int cc_label_t(const T *img, uint64_t *labels, const int64_t *shape, cons
     PMG_TRY(scratch_alloc((void **)&offs, (size_t)nb * 4 + 4, st));
     PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     PMG_TRY(uf_build<T>(img, P, shape, bc, pad, false, err, st));
-    k_root_count<<<(unsigned)nb, kNumBlock, 0, st>>>(P, n, cnt);
+    {
+        const int ps__ = prof_begin("k_root_count", st);
+        k_root_count<<<(unsigned)nb, kNumBlock, 0, st>>>(P, n, cnt);
+        prof_end(ps__, (double)n * 4, st);
+    }
     PMG_CHECK_LAUNCH();
     size_t tb = 0;
     PMG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, offs, (int)nb + 1, st));
@@ -760,9 +804,17 @@ static int cc_label_t(const T *img, uint64_t *labels, const int64_t *shape, cons
     PMG_TRY(scratch_alloc(&tmp, tb, st));
     PMG_CUDA(cudaMemsetAsync(cnt + nb, 0, 4, st));
     PMG_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, offs, (int)nb + 1, st));
-    k_root_rank<<<(unsigned)nb, kNumBlock, 0, st>>>(P, n, offs, R);
+    {
+        const int ps__ = prof_begin("k_root_rank", st);
+        k_root_rank<<<(unsigned)nb, kNumBlock, 0, st>>>(P, n, offs, R);
+        prof_end(ps__, (double)n * 4, st);
+    }
     PMG_CHECK_LAUNCH();
-    k_label_out<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(P, R, n, labels);
+    {
+        const int ps__ = prof_begin("k_label_out", st);
+        k_label_out<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(P, R, n, labels);
+        prof_end(ps__, (double)n * 12, st);
+    }
     PMG_CHECK_LAUNCH();
     int total = 0;
     PMG_CUDA(cudaMemcpyAsync(&total, offs + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -853,17 +905,29 @@ int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shap
             }
         }
         if (b.size() > 0) {
-            k_mark_face<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(P, V, b, mark,
+            {
+                const int ps__ = prof_begin("k_mark_face", st);
+                k_mark_face<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(P, V, b, mark,
                                                                               (uint8_t)(1 << w));
+                prof_end(ps__, (double)b.size() * 4, st);
+            }
             PMG_CHECK_LAUNCH();
         }
     }
     if (out_bytes == 1)
-        k_select<uint8_t><<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(img, P, mark, n, mode, phase,
+        {
+            const int ps__ = prof_begin("k_select", st);
+            k_select<uint8_t><<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(img, P, mark, n, mode, phase,
                                                                         (uint8_t *)out);
+            prof_end(ps__, (double)n * (5 + out_bytes), st);
+        }
     else
-        k_select<uint64_t><<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(img, P, mark, n, mode, phase,
+        {
+            const int ps__ = prof_begin("k_select", st);
+            k_select<uint64_t><<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(img, P, mark, n, mode, phase,
                                                                          (uint64_t *)out);
+            prof_end(ps__, (double)n * (5 + out_bytes), st);
+        }
     PMG_CHECK_LAUNCH();
     return PMG_OK;
 }

@@ -109,14 +109,14 @@ static int count_sync(const uint8_t *img, const int64_t *shape, const int64_t *b
 static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape, const int32_t *bc,
                            const int32_t *pad, const int32_t *ext_e, const int32_t *ext_d, const float *res,
                            double r_e, int cmp_e, double r_d, int cmp_d, int inlet, const uint8_t *mp,
-                           const Boxes &Bx, Work &w, cudaStream_t st)
+                           const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d)
 {
     const long long n = shape[0] * shape[1] * shape[2];
     const int64_t all[6] = {0, shape[0], 0, shape[1], 0, shape[2]};
     uint8_t *E;
     float *A, *B;
     morph_split(w, shape, bc, ext_e, E, A, B);
-    PMG_TRY(morph_run(pm, w.t1, shape, bc, pad, ext_e, res, r_e, cmp_e, 0, E, A, B, st));
+    PMG_TRY(morph_run(pm, w.t1, shape, bc, pad, ext_e, res, r_e, cmp_e, 0, E, A, B, st, ball_e));
     uint8_t *cur = w.t1;
     if (inlet) {
         PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
@@ -136,12 +136,16 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
                 PMG_TRY(select_run(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1, w.P,
                                    w.mark, w.err, st));
                 PMG_TRY(check_err(w.err, st));
-                k_constrain<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(cur, w.t3, n);
+                {
+                    const int ps__ = prof_begin("k_constrain", st);
+                    k_constrain<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(cur, w.t3, n);
+                    prof_end(ps__, (double)n * 3, st);
+                }
                 PMG_CHECK_LAUNCH();
             }
         }
         morph_split(w, shape, bc, ext_d, E, A, B);
-        PMG_TRY(morph_run(cur, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st));
+        PMG_TRY(morph_run(cur, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st, ball_d));
     } else if (cur != out) {
         PMG_CUDA(cudaMemcpyAsync(out, cur, (size_t)n, cudaMemcpyDeviceToDevice, st));
     }
@@ -182,7 +186,7 @@ extern "C" int pmg_porosimetry(const uint8_t *pm_img, const uint8_t *mp_img, uin
                                const int64_t inlet_box[6], const float res[3], double r_erode,
                                int32_t cmp_erode, const int32_t ratio_erode[3], double r_dilate,
                                int32_t cmp_dilate, const int32_t ratio_dilate[3], int32_t inlet,
-                               void *stream)
+                               double ball_erode, double ball_dilate, void *stream)
 {
     PMG_TRY(check_common(shape, bc, pad));
     if (!pm_img || !out || !res || !ratio_erode || !ratio_dilate) {
@@ -201,7 +205,7 @@ extern "C" int pmg_porosimetry(const uint8_t *pm_img, const uint8_t *mp_img, uin
     Work w{};
     PMG_TRY(work_alloc(w, shape, max_morph_bytes(shape, bc, ext_e, ext_d), st));
     int s = porosimetry_run(pm_img, out, shape, bc, pad, ext_e, ext_d, res, r_erode, cmp_erode, r_dilate,
-                            cmp_dilate, inlet, mp_img, Bx, w, st);
+                            cmp_dilate, inlet, mp_img, Bx, w, st, ball_erode, ball_dilate);
     int s2 = scratch_free(w.base, st);
     return s != PMG_OK ? s : s2;
 }
@@ -211,7 +215,8 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
                             const int64_t own_box[6], const int64_t inlet_box[6],
                             const int64_t outlet_box[6], const float res[3], int32_t n_radii,
                             const double *radii, const int32_t *active, const int32_t *ratios,
-                            int64_t *counts, void *stream)
+                            const double *ball_erode, const double *ball_dilate, int64_t *counts,
+                            void *stream)
 {
     PMG_TRY(check_common(shape, bc, pad));
     if (!pm_img || !mp_img || !rpad || !own_box || !res || !counts || n_radii < 0 ||
@@ -255,7 +260,7 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
             ext_of(bc, pad, ratios + 3 * k, ext);
             // the probe radius is a numpy float64: compare in float64
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext, res, radii[k], 1, radii[k], 1, 1, mp_img,
-                                Bx, w, st);
+                                Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
@@ -268,8 +273,12 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
             s = check_err(w.err, st);
         if (s != PMG_OK)
             break;
-        k_drain_update<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(mp_img, morph, wet, shape[0], shape[1],
+        {
+            const int ps__ = prof_begin("k_drain_update", st);
+            k_drain_update<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(mp_img, morph, wet, shape[0], shape[1],
                                                                     shape[2], Bx);
+            prof_end(ps__, (double)n * 4, st);
+        }
         PMG_CHECK_LAUNCH();
         s = count_eq_async(mp_img, shape, Bx.own, 2, d_counts + k, st);
     }

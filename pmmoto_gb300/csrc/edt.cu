@@ -540,8 +540,13 @@ __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fo
                 const int ko = i - me.e2;
                 if (ko < 0 || ko >= me.o2)
                     continue;
-                const float dist = __fsqrt_rn(val);
-                const bool within = me.cmp64 ? ((double)dist <= me.r64) : (dist <= me.r32);
+                bool within;
+                if (me.thr_sq >= 0.0) {
+                    within = (double)val <= me.thr_sq;
+                } else {
+                    const float dist = __fsqrt_rn(val);
+                    within = me.cmp64 ? ((double)dist <= me.r64) : (dist <= me.r32);
+                }
                 uint8_t v = me.dilate ? (uint8_t)within : (uint8_t)!within;
                 if (mwall_row || (me.wall[4] && ko == 0) || (me.wall[5] && ko == me.o2 - 1))
                     v = 0;
@@ -562,7 +567,11 @@ int launch_pass0(const uint8_t *img, float *out, const Lines &Ls, float res,
                  const pmg_axis_cfg &cfg, cudaStream_t st)
 {
     const int block = 256;
-    k_pass0<<<grid_for(Ls.count(), block, 1LL << 30), block, 0, st>>>(img, out, Ls, res, cfg);
+    {
+        const int ps__ = prof_begin("k_pass0", st);
+        k_pass0<<<grid_for(Ls.count(), block, 1LL << 30), block, 0, st>>>(img, out, Ls, res, cfg);
+        prof_end(ps__, (double)Ls.count() * (Ls.ax == 0 ? Ls.s0 : Ls.ax == 1 ? Ls.s1 : Ls.s2) * 5, st);
+    }
     PMG_CHECK_LAUNCH();
     return PMG_OK;
 }
@@ -587,8 +596,12 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     if (smem > 48 * 1024)
         PMG_CUDA(cudaFuncSetAttribute(k_envelope, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    k_envelope<<<grid_for(Ls.count(), block, 1LL << 30), block, smem, st>>>(
+    {
+        const int ps__ = prof_begin("k_envelope", st);
+        k_envelope<<<grid_for(Ls.count(), block, 1LL << 30), block, smem, st>>>(
         fin, fout, Ls, res, cfg, num_hull, form, me);
+        prof_end(ps__, (double)Ls.count() * n * 4 + (form == PMG_EDT_MORPH ? (double)Ls.count() * me.o2 : (double)Ls.count() * n * 4), st);
+    }
     PMG_CHECK_LAUNCH();
     return PMG_OK;
 }

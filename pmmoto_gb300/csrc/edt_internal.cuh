@@ -43,6 +43,8 @@ struct MorphEpi {
     double r64;           // radius as float64
     int cmp64;            // 1: compare in float64 (numpy float64 radius)
     int dilate;           // 1: addition (1 where d <= r), 0: subtraction
+    double thr_sq;        // >= 0: compare the squared unit-resolution distance
+                          // with this integer bound instead (FFT-ball modes)
 };
 
 int launch_pass0(const uint8_t *img, float *out, const Lines &Ls, float res,

@@ -66,7 +66,7 @@ __global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ 
 
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
-              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st)
+              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq)
 {
     ExtGeo G;
     int64_t X[3];
@@ -87,7 +87,11 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
         }
     }
     const long long total = (long long)X[0] * X[1] * X[2];
-    k_extend<<<grid_for(total, 256, 1LL << 30), 256, 0, st>>>(img, E, G, dilate);
+    {
+        const int ps__ = prof_begin("k_extend", st);
+        k_extend<<<grid_for(total, 256, 1LL << 30), 256, 0, st>>>(img, E, G, dilate);
+        prof_end(ps__, (double)total * 2, st);
+    }
     PMG_CHECK_LAUNCH();
 
     pmg_axis_cfg plain = {0, 0, 0, 0, 1, 0, 0, 0};
@@ -107,6 +111,12 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
     me.r64 = radius;
     me.cmp64 = cmp64;
     me.dilate = dilate;
+    me.thr_sq = thr_sq;
+    // the ball of the FFT modes is measured in voxels: unit resolution keeps
+    // every squared distance an exact integer in float32
+    const float unit[3] = {1.0f, 1.0f, 1.0f};
+    if (thr_sq >= 0.0)
+        res = unit;
 
     PMG_TRY(launch_pass0(E, A, all_lines(X, 0), res[0], plain, st));
     Lines L1 = all_lines(X, 1); // lines over (i, k): keep i inside the unextended range
@@ -138,7 +148,7 @@ using namespace pmg;
 extern "C" int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3],
                          const int32_t bc[6], const int32_t pad[6], const int32_t ext[6],
                          const float res[3], double radius, int32_t cmp64, int32_t dilate,
-                         void *stream)
+                         double ball_sq, void *stream)
 {
     if (!img || !out || !shape || !bc || !pad || !ext || !res) {
         set_error("pmg_morph: null argument");
@@ -169,7 +179,7 @@ extern "C" int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3
     uint8_t *E = (uint8_t *)buf;
     float *A = (float *)((char *)buf + (((size_t)nvox + 255) & ~(size_t)255));
     float *B = A + nvox;
-    int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st);
+    int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st, ball_sq);
     int s2 = scratch_free(buf, st);
     return s != PMG_OK ? s : s2;
 }

@@ -41,6 +41,14 @@ int scratch_free(void *p, cudaStream_t st);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Launch accounting.  Every kernel launch is bracketed by prof_begin /
+// prof_end: the launch counter always advances; when profiling is switched
+// on (pmg_prof_enable) a CUDA event pair is recorded on the launching stream
+// together with the launch's algorithmic bytes, and pmg_prof_read later
+// resolves the events into per-kernel totals.
+int prof_begin(const char *name, cudaStream_t st);
+void prof_end(int slot, double bytes, cudaStream_t st);
+
 inline unsigned grid_for(long long n, int block, long long cap = 152LL * 64)
 {
     long long g = (n + block - 1) / block;

@@ -7,7 +7,7 @@ namespace pmg {
 
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
-              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st);
+              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq = -1.0);
 size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext);
 
 int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shape,

@@ -1,7 +1,11 @@
 // Runtime support: error strings, stream-ordered scratch memory, version.
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
+#include <vector>
 
 #include "pmg_common.cuh"
 
@@ -56,7 +60,108 @@ int scratch_free(void *p, cudaStream_t st)
     return PMG_OK;
 }
 
+static std::atomic<long long> g_launches{0};
+static std::atomic<int> g_prof_on{0};
+struct ProfRec {
+    const char *name;
+    cudaEvent_t a, b;
+    double bytes;
+};
+static std::mutex g_prof_mu;
+static std::vector<ProfRec> g_prof;
+struct ProfTot {
+    double ms = 0, bytes = 0;
+    long long n = 0;
+};
+static std::map<std::string, ProfTot> g_prof_tot;
+
+int prof_begin(const char *name, cudaStream_t st)
+{
+    g_launches.fetch_add(1);
+    if (!g_prof_on.load())
+        return -1;
+    ProfRec r{name, nullptr, nullptr, 0.0};
+    if (cudaEventCreate(&r.a) != cudaSuccess || cudaEventCreate(&r.b) != cudaSuccess)
+        return -1;
+    cudaEventRecord(r.a, st);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof.push_back(r);
+    return (int)g_prof.size() - 1;
+}
+
+void prof_end(int slot, double bytes, cudaStream_t st)
+{
+    if (slot < 0)
+        return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (slot >= (int)g_prof.size())
+        return;
+    g_prof[(size_t)slot].bytes = bytes;
+    cudaEventRecord(g_prof[(size_t)slot].b, st);
+}
+
+static void prof_resolve()
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (auto &r : g_prof) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            ProfTot &t = g_prof_tot[r.name];
+            t.ms += ms;
+            t.bytes += r.bytes;
+            t.n += 1;
+        }
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    g_prof.clear();
+}
+
 } // namespace pmg
+
+extern "C" long long pmg_launch_count(void) { return pmg::g_launches.load(); }
+
+extern "C" int pmg_prof_enable(int32_t on)
+{
+    pmg::prof_resolve();
+    pmg::g_prof_on.store(on ? 1 : 0);
+    return PMG_OK;
+}
+
+extern "C" int pmg_prof_reset(void)
+{
+    pmg::prof_resolve();
+    std::lock_guard<std::mutex> lk(pmg::g_prof_mu);
+    pmg::g_prof_tot.clear();
+    return PMG_OK;
+}
+
+extern "C" int pmg_prof_read(char *names, size_t names_len, double *ms, double *bytes,
+                             long long *launches, int32_t cap, int32_t *count)
+{
+    if (!names || !ms || !bytes || !launches || !count || cap < 0) {
+        pmg::set_error("pmg_prof_read: null argument");
+        return PMG_EINVAL;
+    }
+    pmg::prof_resolve();
+    std::lock_guard<std::mutex> lk(pmg::g_prof_mu);
+    std::string joined;
+    int k = 0;
+    for (auto &kv : pmg::g_prof_tot) {
+        if (k >= cap)
+            break;
+        joined += kv.first;
+        joined += "\n";
+        ms[k] = kv.second.ms;
+        bytes[k] = kv.second.bytes;
+        launches[k] = kv.second.n;
+        k++;
+    }
+    *count = k;
+    strncpy(names, joined.c_str(), names_len - 1);
+    names[names_len - 1] = '\0';
+    return PMG_OK;
+}
 
 extern "C" int pmg_last_error(char *buf, size_t len)
 {

@@ -175,11 +175,23 @@ int update_buffer_run(void *img, int elem_bytes, const int64_t *shape, const int
     const long long n = shape[0] * shape[1] * shape[2];
     const unsigned g = grid_for(n, 256, 152LL * 16);
     if (elem_bytes == 1)
-        k_update_buffer<uint8_t><<<g, 256, 0, st>>>((uint8_t *)img, H);
+        {
+            const int ps__ = prof_begin("k_update_buffer", st);
+            k_update_buffer<uint8_t><<<g, 256, 0, st>>>((uint8_t *)img, H);
+            prof_end(ps__, 0.0, st);
+        }
     else if (elem_bytes == 4)
-        k_update_buffer<float><<<g, 256, 0, st>>>((float *)img, H);
+        {
+            const int ps__ = prof_begin("k_update_buffer", st);
+            k_update_buffer<float><<<g, 256, 0, st>>>((float *)img, H);
+            prof_end(ps__, 0.0, st);
+        }
     else if (elem_bytes == 8)
-        k_update_buffer<uint64_t><<<g, 256, 0, st>>>((uint64_t *)img, H);
+        {
+            const int ps__ = prof_begin("k_update_buffer", st);
+            k_update_buffer<uint64_t><<<g, 256, 0, st>>>((uint64_t *)img, H);
+            prof_end(ps__, 0.0, st);
+        }
     else {
         set_error("update_buffer: element size %d not supported", elem_bytes);
         return PMG_EINVAL;
@@ -195,8 +207,12 @@ int count_eq_async(const uint8_t *img, const int64_t *shape, const int64_t *box,
     const long long n0 = box[1] - box[0], n1 = box[3] - box[2], n2 = box[5] - box[4];
     if (n0 <= 0 || n1 <= 0 || n2 <= 0)
         return PMG_OK;
-    k_count_eq<<<grid_for(n0 * n1 * n2, 256, 152LL * 8), 256, 0, st>>>(img, shape[1], shape[2], box[0], n0, box[2],
+    {
+        const int ps__ = prof_begin("k_count_eq", st);
+        k_count_eq<<<grid_for(n0 * n1 * n2, 256, 152LL * 8), 256, 0, st>>>(img, shape[1], shape[2], box[0], n0, box[2],
                                                                       n1, box[4], n2, value, d_cnt);
+        prof_end(ps__, (double)(n0 * n1 * n2), st);
+    }
     PMG_CHECK_LAUNCH();
     return PMG_OK;
 }
@@ -235,7 +251,11 @@ extern "C" int pmg_spheres(const double *spheres, int64_t nsph, const double *cx
         Grid1 gx{cx, shape[0], grid_c0[0], grid_h[0]}, gy{cy, shape[1], grid_c0[1], grid_h[1]},
             gz{cz, shape[2], grid_c0[2], grid_h[2]};
         const long long blocks = nsph < (1LL << 20) ? nsph : (1LL << 20);
-        k_spheres<<<(unsigned)blocks, 256, 0, st>>>(spheres, nsph, gx, gy, gz, img);
+        {
+            const int ps__ = prof_begin("k_spheres", st);
+            k_spheres<<<(unsigned)blocks, 256, 0, st>>>(spheres, nsph, gx, gy, gz, img);
+            prof_end(ps__, 0.0, st);
+        }
         PMG_CHECK_LAUNCH();
     }
     return PMG_OK;
@@ -287,8 +307,12 @@ extern "C" int pmg_max_f32(const float *x, const int64_t shape[3], const int64_t
     PMG_CUDA(cudaMemsetAsync(d, 0, sizeof(unsigned int), st));
     const long long n0 = box[1] - box[0], n1 = box[3] - box[2], n2 = box[5] - box[4];
     if (n0 > 0 && n1 > 0 && n2 > 0) {
-        k_max_f32<<<grid_for(n0 * n1 * n2, 256, 152LL * 8), 256, 0, st>>>(x, shape[1], shape[2], box[0], n0,
+        {
+            const int ps__ = prof_begin("k_max_f32", st);
+            k_max_f32<<<grid_for(n0 * n1 * n2, 256, 152LL * 8), 256, 0, st>>>(x, shape[1], shape[2], box[0], n0,
                                                                          box[2], n1, box[4], n2, d);
+            prof_end(ps__, (double)(n0 * n1 * n2) * 4, st);
+        }
         PMG_CHECK_LAUNCH();
     }
     PMG_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st));

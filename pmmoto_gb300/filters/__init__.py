@@ -1,5 +1,5 @@
 """GPU drop-ins for ``pmmoto.filters``."""
 
-from . import distance  # noqa: F401
+from . import connected_components, distance, equilibrium_distribution, morphological_operators, porosimetry  # noqa: F401
 
-__all__ = ["distance"]
+__all__ = ["morphological_operators", "connected_components", "distance", "porosimetry", "equilibrium_distribution"]

@@ -1,0 +1,105 @@
+"""Drop-in for ``pmmoto.filters.equilibrium_distribution`` on the GPU
+(src/pmmoto/filters/equilibrium_distribution.py:25-289).
+
+The standard (Hilpert & Miller) drainage runs on the device in one native
+call: for every capillary pressure the probe radius is formed on the host
+exactly as the reference forms it (float64), and the porosimetry step, the
+outlet-connected wetting phase, the update and the saturation count run as
+CUDA kernels without host round trips beyond porosimetry's branch tests.
+"""
+
+from __future__ import annotations
+
+import logging
+
+import numpy as np
+import torch
+
+from .. import _dev
+from .._lib import check, host_ptr, i64_array, lib
+from ..core.geometry import geo_of
+from . import morphological_operators as morph
+from .porosimetry import MODES
+
+__all__ = ["drainage"]
+
+
+def _radius(pc, gamma, contact_angle):
+    """Multiphase.get_probe_radius (multiphase.py:98-116)."""
+    if pc == 0:
+        return 0
+    return 2.0 * gamma / pc * np.cos(np.deg2rad(contact_angle))
+
+
+def drainage_counts(multiphase, radii, mode="distance"):
+    """Run the drainage sweep for the given probe radii on the device; returns
+    (per-radius own-region phase-2 counts, final multiphase CUDA tensor)."""
+    sd = multiphase.subdomain
+    g = geo_of(sd)
+    pm, _ = morph.to_u8(multiphase.porous_media.img)
+    mp, _ = morph.to_u8(multiphase.img)
+    mp = mp.clone()
+    n = len(radii)
+    active = np.zeros(n, dtype=np.int32)
+    ratios = np.zeros((max(n, 1), 3), dtype=np.int32)
+    rad = np.zeros(max(n, 1), dtype=np.float64)
+    be = np.full(max(n, 1), -1.0)
+    bd = np.full(max(n, 1), -1.0)
+    min_res = min(sd.domain.resolution)
+    for k, r in enumerate(radii):
+        rad[k] = float(r)
+        if r < min_res or r > multiphase.porous_media.max_distance:
+            continue
+        morph.check_radii(sd, [r, r])
+        active[k] = 1
+        ratios[k] = morph.gen_struct_element(g.res, r)[0]
+        if mode == "morph":
+            be[k] = morph.ball_sq(g.res, r)
+        if mode in ("morph", "hybrid"):
+            bd[k] = morph.ball_sq(g.res, r)
+    from .connected_components import _box
+
+    counts = np.zeros(max(n, 1), dtype=np.int64)
+    rpad = np.ascontiguousarray([g.rpad[d][s] for d in range(3) for s in (0, 1)], dtype=np.int32)
+    res32 = np.ascontiguousarray([np.float32(r) for r in g.res], dtype=np.float32)
+    own = np.ascontiguousarray([v for lohi in g.own_box() for v in lohi], dtype=np.int64)
+    st = lib().pmg_drainage(_dev.ptr(pm), _dev.ptr(mp), host_ptr(i64_array(pm.shape)), host_ptr(g.bc_codes()),
+                            host_ptr(g.pad_flat()), host_ptr(rpad), host_ptr(own),
+                            host_ptr(_box(g.face_slab("inlet"))), host_ptr(_box(g.face_slab("outlet"))),
+                            host_ptr(res32), n, host_ptr(rad), host_ptr(active), host_ptr(ratios), host_ptr(be),
+                            host_ptr(bd), host_ptr(counts), _dev.stream_ptr(pm.device))
+    check(st, "drainage")
+    return counts[:n], mp
+
+
+def drainage(multiphase, capillary_pressures, gamma=1, contact_angle=0, method="standard", mode="hybrid",
+             save=False, out_folder="drainage_out"):
+    """Wetting-phase saturation at each capillary pressure (standard method,
+    equilibrium_distribution.py:25-179).  multiphase.img is updated."""
+    if isinstance(capillary_pressures, (int, float)):
+        capillary_pressures = [capillary_pressures]
+    elif isinstance(capillary_pressures, list):
+        sorted_cp = sorted(capillary_pressures)
+        if capillary_pressures != sorted_cp:
+            logging.warning("The capillary pressure must be monotonically increasing. Sorting.")
+            capillary_pressures = sorted_cp
+    if method == "standard":
+        if contact_angle != 0:
+            raise ValueError("The standard approach requires a zero contact angle!")
+    elif method in ("contact_angle", "extended_contact_angle"):
+        raise NotImplementedError(f"drainage method {method!r} is not part of the GPU build")
+    else:
+        raise ValueError(f"{method} is not implemented. ")
+    if mode not in MODES:
+        raise ValueError(f"mode {mode} must be one of {MODES}")
+    if save:
+        raise NotImplementedError("saving VTK images is not part of the GPU build")
+    radii = [_radius(pc, gamma, contact_angle) for pc in capillary_pressures]
+    counts, mp = drainage_counts(multiphase, radii, mode)
+    total = np.prod(multiphase.subdomain.domain.voxels)
+    phi = multiphase.porous_media.porosity
+    sat = np.zeros(len(capillary_pressures))
+    for k in range(len(capillary_pressures)):
+        sat[k] = float(counts[k] / total) / phi
+    multiphase.img = mp if isinstance(multiphase.img, torch.Tensor) else mp.cpu().numpy()
+    return sat

@@ -1,11 +1,17 @@
-"""Drop-in for ``pmmoto.filters.morphological_operators`` (EDT path on the GPU).
+"""Drop-in for ``pmmoto.filters.morphological_operators`` on the GPU.
 
 Same functions and arguments as src/pmmoto/filters/morphological_operators.py.
-``fft=False`` (the EDT path) runs as one CUDA pipeline: wrap extension of the
-periodic faces, exact EDT, threshold, unpad and wall rule fused.  The
-reference's FFT variant (``fft=True``) is a scipy convolution whose results
-are not always identical to the EDT path, so it raises NotImplementedError
-instead of silently computing something else.
+Both variants run as one CUDA pipeline (wrap extension of the periodic faces,
+exact EDT, threshold, unpad and wall rule fused):
+
+* ``fft=False`` -- the reference's EDT path: ``sqrt(d2) <= radius`` in the
+  precision numpy uses for the comparison.
+* ``fft=True`` -- the reference convolves with the structuring element
+  ``{(i, j, k) : i*i + j*j + k*k <= (radius/res)**2}`` (scipy fftconvolve,
+  thresholded at 0.1 / sum - 0.1).  A voxel is reached by a 1-voxel through
+  that element exactly when the squared voxel-unit distance to the nearest
+  1-voxel is at most ``floor((radius/res)**2)``, so the same EDT kernels with
+  unit resolution and that integer bound give the convolution's result.
 """
 
 from __future__ import annotations
@@ -89,7 +95,13 @@ def to_u8(img):
     return t.contiguous(), kind
 
 
-def morph_device(g, t: torch.Tensor, radius, dilate: bool, out: torch.Tensor | None = None):
+def ball_sq(resolution, radius) -> float:
+    """floor of (radius/res)^2 as gen_struct_element forms it (float64)."""
+    r = radius / resolution[0]
+    return float(np.floor(r * r))
+
+
+def morph_device(g, t: torch.Tensor, radius, dilate: bool, out: torch.Tensor | None = None, fft: bool = False):
     """Addition/subtraction of a contiguous uint8 CUDA tensor of the padded shape."""
     ratio = gen_struct_element(g.res, radius)[0]
     _check_buffer(g, ratio)
@@ -100,17 +112,16 @@ def morph_device(g, t: torch.Tensor, radius, dilate: bool, out: torch.Tensor | N
     res32 = np.ascontiguousarray([np.float32(r) for r in g.res], dtype=np.float32)
     st = lib().pmg_morph(_dev.ptr(t), _dev.ptr(out), host_ptr(i64_array(g.shape)), host_ptr(g.bc_codes()),
                          host_ptr(g.pad_flat()), host_ptr(_ext(g, ratio)), host_ptr(res32), float(radius),
-                         int(compare_in_float64(radius)), int(bool(dilate)), _dev.stream_ptr(t.device))
+                         int(compare_in_float64(radius)), int(bool(dilate)),
+                         ball_sq(g.res, radius) if fft else -1.0, _dev.stream_ptr(t.device))
     check(st, "addition" if dilate else "subtraction")
     return out
 
 
 def _run(subdomain, img, radius, fft, dilate):
-    if fft:
-        raise NotImplementedError("the FFT morphology path is not part of the GPU build; use fft=False")
     g = geo_of(subdomain)
     t, kind = to_u8(img)
-    return _dev.give_back(morph_device(g, t, radius, dilate), kind)
+    return _dev.give_back(morph_device(g, t, radius, dilate, fft=bool(fft)), kind)
 
 
 def addition(subdomain, img, radius, fft=False):

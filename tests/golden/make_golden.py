@@ -128,6 +128,10 @@ def main():
             put(f"sub_{ci}_erode_{ri}", morph.erode(sd, pmo.img, r))
             put(f"sub_{ci}_dilate_{ri}", morph.dilate(sd, pmo.img, r))
             put(f"sub_{ci}_erode64_{ri}", morph.erode(sd, pmo.img, np.float64(r)))
+            put(f"sub_{ci}_erodefft_{ri}", morph.erode(sd, pmo.img, r, fft=True))
+            put(f"sub_{ci}_dilatefft_{ri}", morph.dilate(sd, pmo.img, r, fft=True))
+            for mode in ("hybrid", "morph"):
+                put(f"sub_{ci}_por_{mode}_{ri}", pm.filters.porosimetry.porosimetry(sd, pmo, r, mode=mode))
         sub_cases.append({"geom": geom_meta(vox, bts, box), "radii": list(radii), "cc_count": int(n)})
     meta["sub_cases"] = sub_cases
 
@@ -175,6 +179,11 @@ def main():
     put("drain_por_r", pm.filters.porosimetry.porosimetry(sd, pmo, 0.1, inlet=True, mode="distance"))
     put("drain_psd", pm.filters.porosimetry.pore_size_distribution(
         sd, pmo, radii=[0.03, 0.06, 0.09, 0.12], inlet=False, mode="distance"))
+    put("drain_psd_auto", pm.filters.porosimetry.pore_size_distribution(sd, pmo, num_radii=6, mode="distance"))
+    mp_h = pm.domain_generation.gen_mp_constant(pmo, 2)
+    put("drain_sat_hybrid", pm.filters.equilibrium_distribution.drainage(mp_h, pcs, mode="hybrid"))
+    mp_m = pm.domain_generation.gen_mp_constant(pmo, 2)
+    put("drain_sat_morph", pm.filters.equilibrium_distribution.drainage(mp_m, pcs, mode="morph"))
     meta["drain_geom"] = geom_meta(vox, (E, W, W), box, inlet, outlet)
 
     # ---- ink bottle (tests/applications/test_drainage_inkbottle.py) -------------
@@ -188,6 +197,8 @@ def main():
     put("ink_sat_expected", np.array(tmod.w_saturation_expected, dtype=np.float64))
     put("ink_sat_distance", pm.filters.equilibrium_distribution.drainage(mp_ink, list(tmod.capillary_pressure),
                                                                         mode="distance"))
+    mp_ink2 = tmod.initialize_ink_bottle()
+    put("ink_sat_hybrid", pm.filters.equilibrium_distribution.drainage(mp_ink2, list(tmod.capillary_pressure)))
     meta["ink_geom"] = geom_meta((140, 30, 30), (E, E, E), ((0.0, 14.0), (-1.5, 1.5), (-1.5, 1.5)),
                                  ((0, 1), (0, 0), (0, 0)), ((1, 0), (0, 0), (0, 0)), 10)
 

@@ -26,6 +26,8 @@ def test_morph_golden(M, golden, golden_meta, ci):
         np.testing.assert_array_equal(M.erode(sd, img, r), golden[f"sub_{ci}_erode_{ri}"])
         np.testing.assert_array_equal(M.dilate(sd, img, r), golden[f"sub_{ci}_dilate_{ri}"])
         np.testing.assert_array_equal(M.erode(sd, img, np.float64(r)), golden[f"sub_{ci}_erode64_{ri}"])
+        np.testing.assert_array_equal(M.erode(sd, img, r, fft=True), golden[f"sub_{ci}_erodefft_{ri}"])
+        np.testing.assert_array_equal(M.dilate(sd, img, r, fft=True), golden[f"sub_{ci}_dilatefft_{ri}"])
 
 
 @pytest.mark.parametrize("kinds", list(itertools.product(["end", "wall", "periodic"], repeat=3))[::2])
@@ -54,5 +56,3 @@ def test_morph_errors(M):
         M.erode(sd, img, 0.01)  # radius below the resolution
     with pytest.raises(SystemExit):
         M.erode(sd, img, 1.5)  # extension beyond the subdomain
-    with pytest.raises(NotImplementedError):
-        M.erode(sd, img, 0.2, fft=True)

@@ -62,6 +62,10 @@ def test_subdomain_golden(golden, golden_meta, ci):
         np.testing.assert_array_equal(O.erode(g, img, r), golden[f"sub_{ci}_erode_{ri}"])
         np.testing.assert_array_equal(O.dilate(g, img, r), golden[f"sub_{ci}_dilate_{ri}"])
         np.testing.assert_array_equal(O.erode(g, img, np.float64(r)), golden[f"sub_{ci}_erode64_{ri}"])
+        np.testing.assert_array_equal(O.erode(g, img, r, fft=True), golden[f"sub_{ci}_erodefft_{ri}"])
+        np.testing.assert_array_equal(O.dilate(g, img, r, fft=True), golden[f"sub_{ci}_dilatefft_{ri}"])
+        for mode in ("hybrid", "morph"):
+            np.testing.assert_array_equal(O.porosimetry(g, img, r, mode=mode), golden[f"sub_{ci}_por_{mode}_{ri}"])
 
 
 @pytest.mark.parametrize("ci", range(8))
@@ -86,6 +90,9 @@ def test_inlet_outlet_and_drainage_golden(golden, golden_meta):
     np.testing.assert_array_equal(mp_img, golden["drain_mp_img"])
     np.testing.assert_array_equal(O.porosimetry(g, img, 0.1, inlet=True), golden["drain_por_r"])
     np.testing.assert_array_equal(O.pore_size_distribution(g, img, [0.03, 0.06, 0.09, 0.12]), golden["drain_psd"])
+    for mode in ("hybrid", "morph"):
+        sat, _ = O.drainage(g, img, list(golden["drain_pcs"]), mode=mode)
+        np.testing.assert_array_equal(sat, golden[f"drain_sat_{mode}"])
 
 
 def test_inkbottle_golden(golden, golden_meta):
@@ -94,6 +101,9 @@ def test_inkbottle_golden(golden, golden_meta):
     np.testing.assert_array_equal(sat, golden["ink_sat_distance"])
     # the reference test's own expected curve (6 decimals)
     np.testing.assert_array_almost_equal(sat, golden["ink_sat_expected"])
+    sat_h, _ = O.drainage(g, golden["ink_img"], list(golden["ink_pcs"]), mode="hybrid")
+    np.testing.assert_array_equal(sat_h, golden["ink_sat_hybrid"])
+    np.testing.assert_array_almost_equal(sat_h, golden["ink_sat_expected"])
 
 
 def test_sphere_kat(golden):
