@@ -74,8 +74,14 @@ def lib():
     return _lib
 
 
+class _Ptr(ctypes.c_void_p):
+    """c_void_p that keeps its array alive for the duration of the call."""
+
+
 def _ptr(a: np.ndarray) -> ctypes.c_void_p:
-    return ctypes.c_void_p(a.ctypes.data)
+    p = _Ptr(a.ctypes.data)
+    p._keep = a
+    return p
 
 
 # --------------------------------------------------------------------------

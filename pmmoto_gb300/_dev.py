@@ -33,8 +33,18 @@ def give_back(t: torch.Tensor, kind: str):
     return t if kind == "torch" else t.cpu().numpy()
 
 
+class _DevPtr(ctypes.c_void_p):
+    """A c_void_p holding a reference to the tensor it points into."""
+
+
 def ptr(t: torch.Tensor) -> ctypes.c_void_p:
-    return ctypes.c_void_p(t.data_ptr())
+    if not t.is_cuda:
+        raise ValueError("device pointers must come from CUDA tensors")
+    if not t.is_contiguous():
+        raise ValueError("CUDA tensors passed to the C ABI must be contiguous")
+    p = _DevPtr(t.data_ptr())
+    p._keep = t
+    return p
 
 
 def stream_ptr(device=None) -> ctypes.c_void_p:

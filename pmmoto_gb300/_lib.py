@@ -99,5 +99,14 @@ def i64_array(vals) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(vals, dtype=np.int64))
 
 
+class _HostPtr(ctypes.c_void_p):
+    """A c_void_p that owns a reference to the array it points into, so an
+    array built inline in an argument list lives until the call returns."""
+
+
 def host_ptr(a: np.ndarray) -> ctypes.c_void_p:
-    return ctypes.c_void_p(a.ctypes.data)
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("host arrays passed to the C ABI must be C-contiguous")
+    p = _HostPtr(a.ctypes.data)
+    p._keep = a
+    return p

@@ -860,6 +860,7 @@ extern "C" int pmg_cc_label(const void *img, int32_t elem_bytes, uint64_t *label
         set_error("pmg_cc_label: null argument");
         return PMG_EINVAL;
     }
+    PMG_TRY(check_geometry(shape, bc, pad));
     PMG_TRY(check_vol(shape));
     cudaStream_t st = as_stream(stream);
     switch (elem_bytes) {
@@ -951,6 +952,7 @@ extern "C" int pmg_cc_select(const uint8_t *img, void *out, int32_t out_bytes,
         set_error("pmg_cc_select: output element size must be 1 or 8");
         return PMG_EINVAL;
     }
+    PMG_TRY(check_geometry(shape, bc, pad));
     PMG_TRY(check_vol(shape));
     cudaStream_t st = as_stream(stream);
     const long long n = shape[0] * shape[1] * shape[2];

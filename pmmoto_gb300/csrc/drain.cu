@@ -170,10 +170,7 @@ static size_t max_morph_bytes(const int64_t *shape, const int32_t *bc, const int
 
 static int check_common(const int64_t *shape, const int32_t *bc, const int32_t *pad)
 {
-    if (!shape || !bc || !pad) {
-        set_error("null geometry argument");
-        return PMG_EINVAL;
-    }
+    PMG_TRY(check_geometry(shape, bc, pad));
     return check_volume(shape);
 }
 
@@ -224,6 +221,12 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         set_error("pmg_drainage: null argument");
         return PMG_EINVAL;
     }
+    PMG_TRY(check_box6(shape, own_box));
+    for (int q = 0; q < 6; q++)
+        if (rpad[q] < 0) {
+            set_error("pmg_drainage: negative reservoir pad");
+            return PMG_EINVAL;
+        }
     cudaStream_t st = as_stream(stream);
     const long long n = shape[0] * shape[1] * shape[2];
     Boxes Bx{};

@@ -154,6 +154,7 @@ extern "C" int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3
         set_error("pmg_morph: null argument");
         return PMG_EINVAL;
     }
+    PMG_TRY(check_geometry(shape, bc, pad));
     for (int d = 0; d < 3; d++) {
         if (shape[d] <= 0) {
             set_error("pmg_morph: shape[%d] must be positive", d);

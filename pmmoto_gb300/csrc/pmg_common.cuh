@@ -49,6 +49,51 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 int prof_begin(const char *name, cudaStream_t st);
 void prof_end(int slot, double bytes, cudaStream_t st);
 
+// Validate a padded single-rank geometry: positive shape, boundary codes in
+// range, non-negative pads that leave a non-empty own region on every axis.
+inline int check_geometry(const int64_t *shape, const int32_t *bc, const int32_t *pad)
+{
+    if (!shape || !bc || !pad) {
+        set_error("null geometry argument");
+        return PMG_EINVAL;
+    }
+    for (int d = 0; d < 3; d++) {
+        if (shape[d] <= 0) {
+            set_error("shape[%d] must be positive", d);
+            return PMG_EINVAL;
+        }
+        for (int s = 0; s < 2; s++) {
+            if (bc[2 * d + s] < PMG_BC_END || bc[2 * d + s] > PMG_BC_PERIODIC) {
+                set_error("boundary code %d out of range", bc[2 * d + s]);
+                return PMG_EINVAL;
+            }
+            if (pad[2 * d + s] < 0) {
+                set_error("negative pad on axis %d", d);
+                return PMG_EINVAL;
+            }
+        }
+        if ((long long)pad[2 * d] + pad[2 * d + 1] >= shape[d]) {
+            set_error("pads of axis %d leave no own voxels", d);
+            return PMG_EINVAL;
+        }
+        if ((bc[2 * d] == PMG_BC_PERIODIC) != (bc[2 * d + 1] == PMG_BC_PERIODIC)) {
+            set_error("axis %d is periodic on one face only", d);
+            return PMG_EINVAL;
+        }
+    }
+    return PMG_OK;
+}
+
+inline int check_box6(const int64_t *shape, const int64_t *box)
+{
+    for (int d = 0; d < 3; d++)
+        if (box[2 * d] < 0 || box[2 * d + 1] > shape[d] || box[2 * d] > box[2 * d + 1]) {
+            set_error("box outside the volume on axis %d", d);
+            return PMG_EINVAL;
+        }
+    return PMG_OK;
+}
+
 inline unsigned grid_for(long long n, int block, long long cap = 152LL * 64)
 {
     long long g = (n + block - 1) / block;

@@ -31,15 +31,14 @@ __device__ __forceinline__ void index_box(const Grid1 &g, double x, double r, lo
 {
     const double a = (x - r - g.c0) / g.h, b = (x + r - g.c0) / g.h;
     double la = floor(a) - 2.0, hb = ceil(b) + 2.0;
+    const double n = (double)g.n;
     if (!(la == la) || !(hb == hb)) { // NaN radius or centre: test the whole axis
-        lo = 0;
-        hi = g.n;
-        return;
-    }
-    if (la < 0.0)
         la = 0.0;
-    if (hb > (double)g.n)
-        hb = (double)g.n;
+        hb = n;
+    }
+    // clamp before converting so that no coordinate can leave [0, n]
+    la = fmin(fmax(la, 0.0), n);
+    hb = fmin(fmax(hb, 0.0), n);
     lo = (long long)la;
     hi = (long long)hb;
     if (hi < lo)
@@ -268,6 +267,7 @@ extern "C" int pmg_update_buffer(void *img, int32_t elem_bytes, const int64_t sh
         set_error("pmg_update_buffer: null argument");
         return PMG_EINVAL;
     }
+    PMG_TRY(check_geometry(shape, bc, pad));
     return update_buffer_run(img, elem_bytes, shape, bc, pad, as_stream(stream));
 }
 

@@ -46,7 +46,8 @@ def _img_device(img):
         a = a.astype(np.int64)
     a = np.ascontiguousarray(a)
     view = a.view({1: np.uint8, 2: np.int16, 4: np.int32, 8: np.int64}[a.dtype.itemsize])
-    return _dev.to_device(view, _TORCH_BY_SIZE[a.dtype.itemsize]), "numpy"
+    t, _ = _dev.to_device(view, _TORCH_BY_SIZE[a.dtype.itemsize])
+    return t, "numpy"
 
 
 def connect_components_device(t: torch.Tensor, g):

@@ -138,7 +138,7 @@ def test_lines_match_reference_kernels():
     L = _reflib()
     ol = O.lib()
     rng = np.random.default_rng(7)
-    P = lambda a: ctypes.c_void_p(a.ctypes.data)  # noqa: E731
+    P = O._ptr
     for trial in range(400):
         n = int(rng.integers(1, 70))
         res = np.float32(rng.choice([1.0, 0.01, 1 / 3, 0.5, 233.0, 0.32325245]))
@@ -185,7 +185,7 @@ def test_lines_match_reference_kernels():
 def test_unique_pairs_and_spheres_match_reference():
     L = _reflib()
     rng = np.random.default_rng(11)
-    P = lambda a: ctypes.c_void_p(a.ctypes.data)  # noqa: E731
+    P = O._ptr
     pairs = rng.integers(0, 50, (3000, 2)).astype(np.uint64)
     out = np.zeros_like(pairs)
     m = L.ref_unique_pairs(P(pairs), pairs.shape[0], P(out))
