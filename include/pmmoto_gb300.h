@@ -76,6 +76,24 @@ int pmg_edt3d(const uint8_t *img, float *out, const int64_t shape[3],
               int32_t form, void *stream);
 
 /*
+ * pmg_edt3d without any device allocation.  No counterpart in the reference:
+ * it is an addition for callers that cannot let a library allocate device
+ * memory -- a host framework that owns all device memory through its own
+ * pool or budget, or a latency-critical loop where a pool allocation could
+ * block or fail mid-run.  Same arguments and results as pmg_edt3d; the
+ * intermediate volume lives in a fixed 64 MiB array reserved by the library
+ * on every device that loads it (held until the process exits), so volumes
+ * are limited to 16,777,216 voxels (256^3); larger ones return PMG_ERANGE
+ * with a message.  The first call on a device looks up that device's array
+ * address, so make the first call before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU (concurrent streams,
+ * threads) race and must be serialized by the caller.
+ */
+int pmg_edt3d_noalloc(const uint8_t *img, float *out, const int64_t shape[3],
+                      const float res[3], const pmg_axis_cfg cfg[3], int32_t num_hull,
+                      int32_t form, void *stream);
+
+/*
  * edt2d (euclidean_distance_transform.py:104-205): linear pass along axis 1,
  * envelope along axis 0.  img/out hold shape2[0]*shape2[1] values.
  */
