@@ -347,8 +347,9 @@ def run_reference(args):
 
 def run_case(args):
     """Single-operator cases on a seeded random medium (for ncu captures and
-    per-operator rates): 'edt' = periodic edt3d, 'cc' = connected components
-    with periodic merge, 'morph' = erosion (EDT path); N^3 voxels."""
+    per-operator rates): 'edt' = edt3d, 'cc' = connected components (with the
+    periodic merge when --bc periodic), 'morph' = erosion (EDT path); N^3
+    voxels, all faces periodic or all walls (--bc)."""
     import torch
 
     import pmmoto_gb300 as P
@@ -362,10 +363,12 @@ def run_case(args):
     g = torch.Generator(device="cuda")
     g.manual_seed(7)
     img = (torch.rand((n, n, n), device="cuda", generator=g) >= 0.35).to(torch.uint8)
-    sd = P.initialize((n - 2,) * 3, boundary_types=(("periodic", "periodic"),) * 3)
+    per = args.bc == "periodic"
+    # voxel size 1/512 (a power of two, like the drainage pack)
+    sd = P.initialize((n - 2,) * 3, box=((0.0, (n - 2) / 512.0),) * 3, boundary_types=((args.bc, args.bc),) * 3)
     geo = geo_of(sd)
     out = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
-    cfg = D.edt3d_cfg((True, True, True))
+    cfg = D.edt3d_cfg((per, per, per))
     res = np.ones(3, np.float32)
 
     def op():
@@ -392,7 +395,7 @@ def run_case(args):
     ms = e0.elapsed_time(e1) / args.steps
     prof = prof_read(L)
     peak, _ = load_peaks()
-    print(json.dumps({"case": args.case, "n": n, "ms": ms, "gvox_s": n**3 / ms / 1e6,
+    print(json.dumps({"case": args.case, "bc": args.bc, "n": n, "ms": ms, "gvox_s": n**3 / ms / 1e6,
                       "kernels": {k: {"ms_per_step": v["ms"] / args.steps, "launches": v["launches"],
                                       "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] else None,
                                       "frac": v["bytes"] / (v["ms"] / 1e3) / 1e9 / peak if v["ms"] else None}
@@ -408,6 +411,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph"])
     ap.add_argument("--n", type=int, default=512, help="volume side of the single-operator cases")
+    ap.add_argument("--bc", default="periodic", choices=["periodic", "wall"],
+                    help="boundary type of every face in the single-operator cases")
     args = ap.parse_args()
     if args.case != "drainage":
         run_case(args)

@@ -148,6 +148,7 @@ int pmg_cc_label(const void *img, int32_t elem_bytes, uint64_t *labels,
 #define PMG_SEL_OUTLET 2   /* outlet_connected_img (:299-341) */
 #define PMG_SEL_BOTH 3     /* inlet_outlet_connected_img (:203-251) */
 #define PMG_SEL_ISOLATED 4 /* isolated_img (:344-392) */
+#define PMG_SEL_BINARY 16  /* flag: the image holds only 0 and 1 (phase < 0 case) */
 
 /*
  * Keep the voxels of `img` (uint8, padded shape) whose component (periodic
@@ -156,7 +157,10 @@ int pmg_cc_label(const void *img, int32_t elem_bytes, uint64_t *labels,
  * or 0, as uint8 (out_bytes 1) or uint64 (8).  inlet_box / outlet_box are
  * {lo0, hi0, lo1, hi1, lo2, hi2} own-slab boxes of the face flagged inlet /
  * outlet (the last such face in face order, core/voxels.py:400-454), or NULL
- * / lo0 < 0 when the subdomain has none.
+ * / lo0 < 0 when the subdomain has none.  With phase >= 0, or with
+ * PMG_SEL_BINARY or-ed into mode for an image of 0s and 1s, the selection
+ * runs on 2x2x2 blocks (one value is in play, and all its voxels in a block
+ * are mutually 26-adjacent); results are the same.
  */
 int pmg_cc_select(const uint8_t *img, void *out, int32_t out_bytes,
                   const int64_t shape[3], const int32_t bc[6], const int32_t pad[6],

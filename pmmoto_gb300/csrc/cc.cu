@@ -55,12 +55,36 @@ __device__ __forceinline__ int find_root(const int *P, int x, int *err)
     return x;
 }
 
+// Root search with path halving: each visited element is re-pointed to its
+// grandparent.  Parents only ever point to smaller indices and an element's
+// ancestors stay its ancestors, so a plain store of an ancestor never breaks a
+// link; a store that overwrites a concurrent atomicMin on a former root is
+// harmless because that union retries with the value the atomic returned.
+__device__ __forceinline__ int find_root_halve(int *P, int x, int *err)
+{
+    int p = ld(P + x);
+    int it = 0;
+    while (p != x) {
+        const int g = ld(P + p);
+        if (g == p)
+            return p;
+        P[x] = g;
+        x = g;
+        p = ld(P + x);
+        if (++it > kFindCap) {
+            atomicExch(err, 1);
+            break;
+        }
+    }
+    return x;
+}
+
 // Playne-Hawick union (atomicMin links the larger root under the smaller).
 __device__ __forceinline__ void unite(int *P, int a, int b, int *err)
 {
     for (int it = 0; it < kUniteCap; it++) {
-        a = find_root(P, a, err);
-        b = find_root(P, b, err);
+        a = find_root_halve(P, a, err);
+        b = find_root_halve(P, b, err);
         if (a == b)
             return;
         if (a < b) {
@@ -158,6 +182,163 @@ __global__ void k_cc_merge(const T *__restrict__ img, int *P, Vol3 V, int *err)
     }
 }
 
+// ---- tiled labelling ------------------------------------------------------
+// Tiles of 4 x 8 x 32 voxels (C order, the last axis contiguous), one thread
+// per voxel.  Phase 1 unites equal neighbours inside the tile with a shared-
+// memory union-find whose roots are the smallest local index -- which is also
+// the smallest global index of that part of the component, because C order
+// inside a box follows the global C order.  Phase 2 unites neighbours that lie
+// in other tiles through the global parents.  Both phases use one
+// representative per 26-connected group of equal earlier neighbours.
+constexpr int kT0 = 4, kT1 = 8, kT2 = 32, kTile = kT0 * kT1 * kT2;
+
+__device__ __forceinline__ int sfind(const int *L, int x)
+{
+    int p = L[x];
+    int it = 0;
+    while (p != x && it++ < kTile) {
+        x = p;
+        p = L[x];
+    }
+    return x;
+}
+
+__device__ __forceinline__ void sunite(int *L, int a, int b)
+{
+    for (int it = 0; it < 4 * kTile; it++) {
+        a = sfind(L, a);
+        b = sfind(L, b);
+        if (a == b)
+            return;
+        if (a < b) {
+            const int old = atomicMin(L + b, a);
+            if (old == b)
+                return;
+            b = old;
+        } else {
+            const int old = atomicMin(L + a, b);
+            if (old == a)
+                return;
+            a = old;
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned cover_group(unsigned q_mask, unsigned same)
+{
+    unsigned grp = q_mask, prev = 0;
+    while (grp != prev) {
+        prev = grp;
+        unsigned g = grp;
+        while (g) {
+            const int w = __ffs(g) - 1;
+            g &= g - 1;
+            grp |= c_adj[w] & same;
+        }
+    }
+    return grp;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTile) k_cc_tile(const T *__restrict__ img, int *__restrict__ P, Vol3 V)
+{
+    __shared__ T sv[kTile];
+    __shared__ int L[kTile];
+    const int nt1 = (int)((V.s1 + kT1 - 1) / kT1), nt2 = (int)((V.s2 + kT2 - 1) / kT2);
+    const long long tile = blockIdx.x;
+    const long long ti = tile / ((long long)nt1 * nt2);
+    const int tj = (int)((tile / nt2) % nt1), tk = (int)(tile % nt2);
+    const int t = threadIdx.x;
+    const int a = t / (kT1 * kT2), b = (t / kT2) % kT1, c = t % kT2;
+    const long long i = ti * kT0 + a, j = (long long)tj * kT1 + b, k = (long long)tk * kT2 + c;
+    const bool inside = i < V.s0 && j < V.s1 && k < V.s2;
+    const long long g = (i * V.s1 + j) * V.s2 + k;
+    const T v = inside ? img[g] : (T)0;
+    sv[t] = v;
+    L[t] = v != 0 ? t : -1;
+    __syncthreads();
+    if (v != 0) {
+        unsigned same = 0;
+#pragma unroll
+        for (int q = 0; q < 13; q++) {
+            const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
+            if (aa < 0 || bb < 0 || bb >= kT1 || cc < 0 || cc >= kT2)
+                continue;
+            if (sv[(aa * kT1 + bb) * kT2 + cc] == v)
+                same |= 1u << q;
+        }
+        unsigned covered = 0;
+        while (same & ~covered) {
+            const int q = __ffs(same & ~covered) - 1;
+            sunite(L, t, ((a + c_nb[q][0]) * kT1 + b + c_nb[q][1]) * kT2 + c + c_nb[q][2]);
+            covered |= cover_group(1u << q, same);
+        }
+    }
+    __syncthreads();
+    if (v != 0)
+        L[t] = sfind(L, t);
+    __syncthreads();
+    if (inside) {
+        int out = -1;
+        if (v != 0) {
+            const int r = L[t];
+            const int ra = r / (kT1 * kT2), rb = (r / kT2) % kT1, rc = r % kT2;
+            out = (int)(((ti * kT0 + ra) * V.s1 + (long long)tj * kT1 + rb) * V.s2 + (long long)tk * kT2 + rc);
+        }
+        P[g] = out;
+    }
+}
+
+// Phase 2: unions with equal earlier neighbours in other tiles.  Neighbours in
+// the voxel's own tile (and everything 26-connected to them among the equal
+// neighbours) are already united by phase 1.
+template <typename T>
+__global__ void k_cc_cross(const T *__restrict__ img, int *P, Vol3 V, int *err)
+{
+    // volumes are below 2^31 voxels, so 32-bit index arithmetic suffices
+    const int n = (int)(V.s0 * V.s1 * V.s2);
+    const int S1 = (int)V.s1, S2 = (int)V.s2;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int r = idx / S2;
+        const int k = idx - r * S2;
+        const int i = r / S1;
+        const int j = r - i * S1;
+        const int a = i & (kT0 - 1), b = j & (kT1 - 1), c = k & (kT2 - 1);
+        if (a > 0 && b > 0 && b < kT1 - 1 && c > 0 && c < kT2 - 1)
+            continue; // every earlier neighbour is inside the tile
+        const T v = img[idx];
+        if (v == 0)
+            continue;
+        unsigned same = 0, local = 0;
+#pragma unroll
+        for (int q = 0; q < 13; q++) {
+            const int ai = i + c_nb[q][0], bj = j + c_nb[q][1], ck = k + c_nb[q][2];
+            if (ai < 0 || bj < 0 || ck < 0 || bj >= S1 || ck >= S2)
+                continue;
+            if (img[(ai * S1 + bj) * S2 + ck] != v)
+                continue;
+            same |= 1u << q;
+            const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
+            if (aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2)
+                local |= 1u << q;
+        }
+        unsigned covered = 0;
+        unsigned lm = local;
+        while (lm) { // groups reached through in-tile neighbours are done
+            const int q = __ffs(lm) - 1;
+            const unsigned grp = cover_group(1u << q, same);
+            covered |= grp;
+            lm &= ~grp;
+        }
+        while (same & ~covered) {
+            const int q = __ffs(same & ~covered) - 1;
+            const int ai = i + c_nb[q][0], bj = j + c_nb[q][1], ck = k + c_nb[q][2];
+            unite(P, idx, (ai * S1 + bj) * S2 + ck, err);
+            covered |= cover_group(1u << q, same);
+        }
+    }
+}
+
 // Seam twins: every halo voxel of a periodic feature is united with the own
 // voxel it copies, when both are nonzero (the reference pairs labels without
 // comparing values, skipping zeros).
@@ -207,8 +388,7 @@ __global__ void k_cc_twins(const T *__restrict__ img, int *P, Twins W, int *err)
 
 __global__ void k_cc_flatten(int *P, long long n, int *err)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (int)n; i += gridDim.x * blockDim.x) {
         const int p = P[i];
         if (p >= 0 && p != i)
             P[i] = find_root(P, p, err);
@@ -437,16 +617,18 @@ static int uf_build(const T *img, int *P, const int64_t *shape, const int32_t *b
     const long long n = shape[0] * shape[1] * shape[2];
     Vol3 V{shape[0], shape[1], shape[2]};
     const int block = 256;
+    const long long tiles = ((shape[0] + kT0 - 1) / kT0) * ((shape[1] + kT1 - 1) / kT1) *
+                            ((shape[2] + kT2 - 1) / kT2);
     {
-        const int ps__ = prof_begin("k_cc_init", st);
-        k_cc_init<T><<<grid_for(n, block, 1LL << 30), block, 0, st>>>(img, P, n);
+        const int ps__ = prof_begin("k_cc_tile", st);
+        k_cc_tile<T><<<(unsigned)tiles, kTile, 0, st>>>(img, P, V);
         prof_end(ps__, (double)n * (sizeof(T) + 4), st);
     }
     PMG_CHECK_LAUNCH();
     {
-        const int ps__ = prof_begin("k_cc_merge", st);
-        k_cc_merge<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P, V, err);
-        prof_end(ps__, (double)n * (sizeof(T) + 4), st);
+        const int ps__ = prof_begin("k_cc_cross", st);
+        k_cc_cross<T><<<grid_for(n, block, 152LL * 32), block, 0, st>>>(img, P, V, err);
+        prof_end(ps__, 0.0, st);
     }
     PMG_CHECK_LAUNCH();
     if (twins && any_periodic(bc)) {
@@ -880,6 +1062,411 @@ extern "C" int pmg_cc_label(const void *img, int32_t elem_bytes, uint64_t *label
 
 namespace pmg {
 
+// ---- binary selection on 2x2x2 blocks -----------------------------------------
+// When the foreground is a single value (a phase filter, or an image known to
+// hold only 0 and 1), all foreground voxels of a 2x2x2 block are mutually
+// 26-adjacent and hence in one component, so the union-find runs on blocks:
+// eight times fewer elements (the parents of a 512^3 volume fit in L2).  Two
+// neighbouring blocks are connected exactly when each has a foreground voxel in
+// the part of the block that touches the other (a face, an edge or a corner):
+// every voxel of one touching part is 26-adjacent to every voxel of the other.
+struct BGrid {
+    int s0, s1, s2;    // voxel shape
+    int b0, b1, b2;    // block shape
+};
+
+__device__ __forceinline__ bool fg_of(uint8_t v, int fgval) { return fgval >= 0 ? v == fgval : v != 0; }
+
+// touching voxels of a block for neighbour offset (d0, d1, d2): bit (x*2+y)*2+z
+__host__ __device__ inline unsigned touch_mask(int d0, int d1, int d2)
+{
+    unsigned m = 0;
+    for (int x = 0; x < 2; x++)
+        for (int y = 0; y < 2; y++)
+            for (int z = 0; z < 2; z++) {
+                if ((d0 == -1 && x != 0) || (d0 == 1 && x != 1))
+                    continue;
+                if ((d1 == -1 && y != 0) || (d1 == 1 && y != 1))
+                    continue;
+                if ((d2 == -1 && z != 0) || (d2 == 1 && z != 1))
+                    continue;
+                m |= 1u << ((x * 2 + y) * 2 + z);
+            }
+    return m;
+}
+
+// Touch masks of the 13 earlier neighbours: voxels of a block that touch
+// neighbour q, voxels of neighbour q that touch the block, and voxels of
+// neighbour r that touch neighbour q (0 when r and q are not adjacent).
+__constant__ uint8_t c_bt_self[13];
+__constant__ uint8_t c_bt_nb[13];
+__constant__ uint8_t c_bt_pair[13][13];
+
+__device__ __forceinline__ unsigned bmask_of(int q, uint64_t mlo, uint64_t mhi)
+{
+    return (unsigned)((q < 8 ? mlo >> (8 * q) : mhi >> (8 * (q - 8))) & 0xffu);
+}
+
+// Neighbours in `conn` connected to those in `q_mask` through chains of
+// touching neighbours: a union with one of them links all of them, because
+// the union of each touching pair is done by the later block of the pair.
+__device__ __forceinline__ unsigned bcover(unsigned q_mask, unsigned conn, uint64_t mlo, uint64_t mhi)
+{
+    unsigned grp = q_mask, frontier = q_mask;
+    while (frontier) {
+        const int w = __ffs(frontier) - 1;
+        frontier &= frontier - 1;
+        const unsigned mw = bmask_of(w, mlo, mhi);
+        unsigned cand = c_adj[w] & conn & ~grp;
+        while (cand) {
+            const int u = __ffs(cand) - 1;
+            cand &= cand - 1;
+            if ((mw & c_bt_pair[w][u]) && (bmask_of(u, mlo, mhi) & c_bt_pair[u][w])) {
+                grp |= 1u << u;
+                frontier |= 1u << u;
+            }
+        }
+    }
+    return grp;
+}
+
+// Phase 1 on tiles of 4 x 8 x 32 blocks (8 x 16 x 64 voxels), one thread per
+// block: block masks from the image, then a shared-memory union-find of the
+// tile whose roots are the smallest block index of each tile-local part.
+__global__ void __launch_bounds__(kTile) k_bcc_tile(const uint8_t *__restrict__ img, int *__restrict__ P,
+                                                   uint8_t *__restrict__ M, BGrid G, int fgval)
+{
+    __shared__ uint8_t sm[kTile];
+    __shared__ int L[kTile];
+    const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
+    const int tile = blockIdx.x;
+    const int ti = tile / (nt1 * nt2), tj = (tile / nt2) % nt1, tk = tile % nt2;
+    const int t = threadIdx.x;
+    const int a = t / (kT1 * kT2), b = (t / kT2) % kT1, c = t % kT2;
+    const int c0 = ti * kT0 + a, c1 = tj * kT1 + b, c2 = tk * kT2 + c;
+    const bool inside = c0 < G.b0 && c1 < G.b1 && c2 < G.b2;
+    unsigned m = 0;
+    if (inside) {
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int y = 0; y < 2; y++)
+#pragma unroll
+                for (int z = 0; z < 2; z++) {
+                    const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2 + z;
+                    if (i < G.s0 && j < G.s1 && k < G.s2 &&
+                        fg_of(img[((long long)i * G.s1 + j) * G.s2 + k], fgval))
+                        m |= 1u << ((x * 2 + y) * 2 + z);
+                }
+    }
+    sm[t] = (uint8_t)m;
+    L[t] = m ? t : -1;
+    __syncthreads();
+    if (m) {
+        unsigned conn = 0;
+        uint64_t mlo = 0, mhi = 0;
+#pragma unroll
+        for (int q = 0; q < 13; q++) {
+            const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
+            if (aa < 0 || bb < 0 || bb >= kT1 || cc < 0 || cc >= kT2)
+                continue;
+            if (!(m & c_bt_self[q]))
+                continue;
+            const unsigned mn = sm[(aa * kT1 + bb) * kT2 + cc];
+            if (mn & c_bt_nb[q]) {
+                conn |= 1u << q;
+                if (q < 8)
+                    mlo |= (uint64_t)mn << (8 * q);
+                else
+                    mhi |= (uint64_t)mn << (8 * (q - 8));
+            }
+        }
+        unsigned covered = 0;
+        while (conn & ~covered) {
+            const int q = __ffs(conn & ~covered) - 1;
+            sunite(L, t, ((a + c_nb[q][0]) * kT1 + b + c_nb[q][1]) * kT2 + c + c_nb[q][2]);
+            covered |= bcover(1u << q, conn, mlo, mhi);
+        }
+    }
+    __syncthreads();
+    if (m)
+        L[t] = sfind(L, t);
+    __syncthreads();
+    if (inside) {
+        const int bidx = (c0 * G.b1 + c1) * G.b2 + c2;
+        M[bidx] = (uint8_t)m;
+        int out = -1;
+        if (m) {
+            const int r = L[t];
+            const int ra = r / (kT1 * kT2), rb = (r / kT2) % kT1, rc = r % kT2;
+            out = ((ti * kT0 + ra) * G.b1 + tj * kT1 + rb) * G.b2 + tk * kT2 + rc;
+        }
+        P[bidx] = out;
+    }
+}
+
+// Phase 2: blocks on a tile border unite with touching earlier neighbours in
+// other tiles; neighbours reached through an in-tile neighbour are skipped.
+__global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int *err)
+{
+    const int nb = G.b0 * G.b1 * G.b2;
+    for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < nb; bi += gridDim.x * blockDim.x) {
+        const int r = bi / G.b2;
+        const int c2 = bi - r * G.b2;
+        const int c0 = r / G.b1;
+        const int c1 = r - c0 * G.b1;
+        const int a = c0 & (kT0 - 1), b = c1 & (kT1 - 1), c = c2 & (kT2 - 1);
+        if (a > 0 && b > 0 && b < kT1 - 1 && c > 0 && c < kT2 - 1)
+            continue; // every earlier neighbour is inside the tile
+        const unsigned m = M[bi];
+        if (!m)
+            continue;
+        unsigned conn = 0, local = 0;
+        uint64_t mlo = 0, mhi = 0;
+#pragma unroll
+        for (int q = 0; q < 13; q++) {
+            const int a0 = c0 + c_nb[q][0], a1 = c1 + c_nb[q][1], a2 = c2 + c_nb[q][2];
+            if (a0 < 0 || a1 < 0 || a2 < 0 || a1 >= G.b1 || a2 >= G.b2)
+                continue;
+            if (!(m & c_bt_self[q]))
+                continue;
+            const unsigned mn = M[(a0 * G.b1 + a1) * G.b2 + a2];
+            if (!(mn & c_bt_nb[q]))
+                continue;
+            conn |= 1u << q;
+            if (q < 8)
+                mlo |= (uint64_t)mn << (8 * q);
+            else
+                mhi |= (uint64_t)mn << (8 * (q - 8));
+            const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
+            if (aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2)
+                local |= 1u << q;
+        }
+        unsigned covered = 0;
+        unsigned lm = local;
+        while (lm) {
+            const int q = __ffs(lm) - 1;
+            const unsigned grp = bcover(1u << q, conn, mlo, mhi);
+            covered |= grp;
+            lm &= ~grp;
+        }
+        while (conn & ~covered) {
+            const int q = __ffs(conn & ~covered) - 1;
+            unite(P, bi, ((c0 + c_nb[q][0]) * G.b1 + c1 + c_nb[q][1]) * G.b2 + c2 + c_nb[q][2], err);
+            covered |= bcover(1u << q, conn, mlo, mhi);
+        }
+    }
+}
+
+static bool g_btables_ready[64] = {false};
+
+static int ensure_block_tables()
+{
+    int dev = 0;
+    PMG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && g_btables_ready[dev])
+        return PMG_OK;
+    int nb[13][3];
+    unsigned short adj[13];
+    host_tables(nb, adj);
+    uint8_t self[13], other[13], pair[13][13];
+    for (int q = 0; q < 13; q++) {
+        self[q] = (uint8_t)touch_mask(nb[q][0], nb[q][1], nb[q][2]);
+        other[q] = (uint8_t)touch_mask(-nb[q][0], -nb[q][1], -nb[q][2]);
+        for (int r = 0; r < 13; r++)
+            pair[r][q] = (adj[r] >> q) & 1
+                             ? (uint8_t)touch_mask(nb[q][0] - nb[r][0], nb[q][1] - nb[r][1], nb[q][2] - nb[r][2])
+                             : (uint8_t)0;
+    }
+    PMG_CUDA(cudaMemcpyToSymbol(c_bt_self, self, sizeof(self)));
+    PMG_CUDA(cudaMemcpyToSymbol(c_bt_nb, other, sizeof(other)));
+    PMG_CUDA(cudaMemcpyToSymbol(c_bt_pair, pair, sizeof(pair)));
+    if (dev >= 0 && dev < 64)
+        g_btables_ready[dev] = true;
+    return PMG_OK;
+}
+
+// periodic seams at block level: a foreground halo voxel joins the block of the
+// own voxel it copies when that voxel is foreground too
+__global__ void k_bcc_twins(const uint8_t *__restrict__ img, int *P, BGrid G, Twins W, int fgval, int *err)
+{
+    const long long n = W.s0 * W.s1 * W.s2;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        long long c[3];
+        c[2] = idx % W.s2;
+        const long long r = idx / W.s2;
+        c[1] = r % W.s1;
+        c[0] = r / W.s1;
+        bool halo = false, ok = true;
+        long long t[3];
+        for (int d = 0; d < 3; d++) {
+            t[d] = c[d];
+            const long long S = d == 0 ? W.s0 : d == 1 ? W.s1 : W.s2;
+            if (c[d] < W.own_lo[d] || c[d] >= W.own_lo[d] + W.own_len[d]) {
+                if (!W.periodic[d] || W.own_len[d] <= 0 || c[d] >= S) {
+                    ok = false;
+                } else {
+                    long long q = (c[d] - W.own_lo[d]) % W.own_len[d];
+                    if (q < 0)
+                        q += W.own_len[d];
+                    t[d] = q + W.own_lo[d];
+                    halo = true;
+                }
+            }
+        }
+        if (!halo || !ok || !fg_of(img[idx], fgval))
+            continue;
+        const long long tw = (t[0] * W.s1 + t[1]) * W.s2 + t[2];
+        if (!fg_of(img[tw], fgval))
+            continue;
+        const int ba = (int)(((c[0] >> 1) * G.b1 + (c[1] >> 1)) * G.b2 + (c[2] >> 1));
+        const int bb = (int)(((t[0] >> 1) * G.b1 + (t[1] >> 1)) * G.b2 + (t[2] >> 1));
+        unite(P, ba, bb, err);
+    }
+}
+
+__global__ void k_bcc_flatten(int *P, int nb, int *err)
+{
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int p = P[b];
+        if (p >= 0 && p != b)
+            P[b] = find_root(P, p, err);
+    }
+}
+
+__global__ void k_bcc_mark(const uint8_t *__restrict__ img, const int *__restrict__ P, BGrid G, Box bx,
+                           uint8_t *mark, uint8_t bit, int fgval)
+{
+    const long long n = bx.size();
+    const long long w = bx.hi[2] - bx.lo[2], h = bx.hi[1] - bx.lo[1];
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long k = bx.lo[2] + q % w, j = bx.lo[1] + (q / w) % h, i = bx.lo[0] + q / (w * h);
+        if (!fg_of(img[(i * G.s1 + j) * G.s2 + k], fgval))
+            continue;
+        const int p = P[((int)(i >> 1) * G.b1 + (int)(j >> 1)) * G.b2 + (int)(k >> 1)];
+        if (p >= 0 && !(mark[p] & bit))
+            atomicOr((unsigned int *)(mark + (p & ~3)), (unsigned int)bit << (8 * (p & 3)));
+    }
+}
+
+// one warp per (i, j) row
+template <typename TO>
+__global__ void k_bcc_select(const uint8_t *__restrict__ img, const int *__restrict__ P,
+                             const uint8_t *__restrict__ mark, BGrid G, int mode, int fgval,
+                             TO *__restrict__ out)
+{
+    const int rows = G.s0 * G.s1;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int r = warp; r < rows; r += nwarps) {
+        const int i = r / G.s1, j = r - (r / G.s1) * G.s1;
+        const long long base = (long long)r * G.s2;
+        const int brow = ((i >> 1) * G.b1 + (j >> 1)) * G.b2;
+        for (int k = lane; k < G.s2; k += 32) {
+            const uint8_t v = img[base + k];
+            TO o = 0;
+            if (fg_of(v, fgval)) {
+                const int p = P[brow + (k >> 1)];
+                const uint8_t mk = p >= 0 ? mark[p] : 0;
+                const bool in = mk & 1, ou = mk & 2;
+                bool keep;
+                if (mode == PMG_SEL_INLET)
+                    keep = in;
+                else if (mode == PMG_SEL_OUTLET)
+                    keep = ou;
+                else if (mode == PMG_SEL_BOTH)
+                    keep = in && ou;
+                else
+                    keep = !(in || ou);
+                if (keep)
+                    o = (TO)v;
+            }
+            out[base + k] = o;
+        }
+    }
+}
+
+// Binary selection: P and mark need one int / one byte per 2x2x2 block.
+int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
+                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+{
+    PMG_TRY(ensure_tables());
+    PMG_TRY(ensure_block_tables());
+    BGrid G;
+    G.s0 = (int)shape[0];
+    G.s1 = (int)shape[1];
+    G.s2 = (int)shape[2];
+    G.b0 = (G.s0 + 1) / 2;
+    G.b1 = (G.s1 + 1) / 2;
+    G.b2 = (G.s2 + 1) / 2;
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    PMG_CUDA(cudaMemsetAsync(mark, 0, ((size_t)nb + 3) & ~(size_t)3, st));
+    {
+        const int nt = ((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
+        const int ps__ = prof_begin("k_bcc_tile", st);
+        k_bcc_tile<<<nt, kTile, 0, st>>>(img, P, M, G, fgval);
+        prof_end(ps__, (double)n + (double)nb * 5, st);
+    }
+    PMG_CHECK_LAUNCH();
+    {
+        const int ps__ = prof_begin("k_bcc_cross", st);
+        k_bcc_cross<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(P, M, G, err);
+        prof_end(ps__, 0.0, st);
+    }
+    PMG_CHECK_LAUNCH();
+    if (any_periodic(bc)) {
+        const int ps__ = prof_begin("k_bcc_twins", st);
+        k_bcc_twins<<<grid_for(n, 256, 152LL * 32), 256, 0, st>>>(img, P, G, make_twins(shape, bc, pad), fgval, err);
+        prof_end(ps__, 0.0, st);
+        PMG_CHECK_LAUNCH();
+    }
+    {
+        const int ps__ = prof_begin("k_bcc_flatten", st);
+        k_bcc_flatten<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(P, nb, err);
+        prof_end(ps__, (double)nb * 8, st);
+    }
+    PMG_CHECK_LAUNCH();
+    const int64_t *boxes[2] = {inlet_box, outlet_box};
+    for (int w = 0; w < 2; w++) {
+        const int64_t *bxp = boxes[w];
+        if (!bxp || bxp[0] < 0)
+            continue;
+        Box b;
+        for (int d = 0; d < 3; d++) {
+            b.lo[d] = bxp[2 * d];
+            b.hi[d] = bxp[2 * d + 1];
+            if (b.lo[d] < 0 || b.hi[d] > shape[d] || b.lo[d] > b.hi[d]) {
+                set_error("connected-image selection: face box outside the volume");
+                return PMG_EINVAL;
+            }
+        }
+        if (b.size() > 0) {
+            const int ps__ = prof_begin("k_bcc_mark", st);
+            k_bcc_mark<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(img, P, G, b, mark, (uint8_t)(1 << w),
+                                                                          fgval);
+            prof_end(ps__, (double)b.size() * 5, st);
+            PMG_CHECK_LAUNCH();
+        }
+    }
+    {
+        const int ps__ = prof_begin("k_bcc_select", st);
+        if (out_bytes == 1)
+            k_bcc_select<uint8_t><<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
+                img, P, mark, G, mode, fgval, (uint8_t *)out);
+        else
+            k_bcc_select<uint64_t><<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
+                img, P, mark, G, mode, fgval, (uint64_t *)out);
+        prof_end(ps__, (double)n * (1.0 + out_bytes) + (double)nb * 5, st);
+    }
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
 // Selection with caller-provided scratch: P (n int32), mark (n bytes rounded
 // up to 4), err (one int, zeroed by the caller).  Does not synchronize.
 int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shape,
@@ -952,18 +1539,35 @@ extern "C" int pmg_cc_select(const uint8_t *img, void *out, int32_t out_bytes,
         set_error("pmg_cc_select: output element size must be 1 or 8");
         return PMG_EINVAL;
     }
+    const bool binary = (mode & PMG_SEL_BINARY) != 0;
+    mode &= ~PMG_SEL_BINARY;
+    if (mode < PMG_SEL_INLET || mode > PMG_SEL_ISOLATED) {
+        set_error("pmg_cc_select: unknown mode %d", mode);
+        return PMG_EINVAL;
+    }
     PMG_TRY(check_geometry(shape, bc, pad));
     PMG_TRY(check_vol(shape));
     cudaStream_t st = as_stream(stream);
     const long long n = shape[0] * shape[1] * shape[2];
     int *P = nullptr, *err = nullptr;
     uint8_t *mark = nullptr;
-    PMG_TRY(scratch_alloc((void **)&P, (size_t)n * 4, st));
-    PMG_TRY(scratch_alloc((void **)&mark, ((size_t)n + 3) & ~(size_t)3, st));
-    PMG_TRY(scratch_alloc((void **)&err, sizeof(int), st));
-    PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    int s = select_run(img, out, out_bytes, shape, bc, pad, inlet_box, outlet_box, mode, phase, P,
-                       mark, err, st);
+    int s;
+    if (phase >= 0 || binary) {
+        const long long nb = ((shape[0] + 1) / 2) * ((shape[1] + 1) / 2) * ((shape[2] + 1) / 2);
+        const size_t mb = ((size_t)nb + 255) & ~(size_t)255;
+        PMG_TRY(scratch_alloc((void **)&P, (size_t)nb * 4, st));
+        PMG_TRY(scratch_alloc((void **)&mark, 2 * mb, st));
+        PMG_TRY(scratch_alloc((void **)&err, sizeof(int), st));
+        PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        s = select_run_binary(img, out, out_bytes, shape, bc, pad, inlet_box, outlet_box, mode, phase >= 0 ? phase : -1,
+                              P, mark, mark + mb, err, st);
+    } else {
+        PMG_TRY(scratch_alloc((void **)&P, (size_t)n * 4, st));
+        PMG_TRY(scratch_alloc((void **)&mark, ((size_t)n + 3) & ~(size_t)3, st));
+        PMG_TRY(scratch_alloc((void **)&err, sizeof(int), st));
+        PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        s = select_run(img, out, out_bytes, shape, bc, pad, inlet_box, outlet_box, mode, phase, P, mark, err, st);
+    }
     if (s == PMG_OK)
         s = read_err(err, st);
     PMG_TRY(scratch_free(P, st));

@@ -22,28 +22,95 @@ struct Boxes {
     int32_t rpad[6];
 };
 
-__global__ void k_constrain(uint8_t *res, const uint8_t *__restrict__ nconn, long long n)
+// Bytes equal to 1 in both words -> 1, else 0 (four voxels per 32-bit word).
+__device__ __forceinline__ uint32_t both_one(uint32_t a, uint32_t b)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        if (res[i] != 1 || nconn[i] != 1)
-            res[i] = 0;
+    const uint32_t z = (a ^ 0x01010101u) | (b ^ 0x01010101u);
+    const uint32_t t = ((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z; // high bit set where the byte is nonzero
+    return (~t & 0x80808080u) >> 7;
 }
 
-// mp = (morph == 1 && w == 2) ? 1 : mp; reservoir slabs -> 1
+// res = (res == 1 && nconn == 1) ? 1 : 0, i.e. where((res != 1) | (nconn != 1), 0, res)
+__global__ void k_constrain(uint8_t *res, const uint8_t *__restrict__ nconn, long long n)
+{
+    const long long nw = n >> 4; // 16-byte vectors (both buffers are 256-byte aligned)
+    uint4 *r4 = (uint4 *)res;
+    const uint4 *c4 = (const uint4 *)nconn;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nw;
+         q += (long long)gridDim.x * blockDim.x) {
+        uint4 a = r4[q];
+        const uint4 b = c4[q];
+        a.x = both_one(a.x, b.x);
+        a.y = both_one(a.y, b.y);
+        a.z = both_one(a.z, b.z);
+        a.w = both_one(a.w, b.w);
+        r4[q] = a;
+    }
+    for (long long i = (nw << 4) + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        res[i] = (res[i] == 1 && nconn[i] == 1) ? 1 : 0;
+}
+
+// mp = (morph == 1 && w == 2) ? 1 : mp; reservoir slabs -> 1.  One warp per
+// (i, j) row, lanes along k.
 __global__ void k_drain_update(uint8_t *mp, const uint8_t *__restrict__ morph, const uint8_t *__restrict__ w,
                                long long s0, long long s1, long long s2, Boxes B)
 {
-    const long long n = s0 * s1 * s2;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const long long k = idx % s2, r = idx / s2, j = r % s1, i = r / s1;
-        uint8_t v = (morph[idx] == 1 && w[idx] == 2) ? (uint8_t)1 : mp[idx];
-        const bool res = (i < B.rpad[0]) || (i >= s0 - B.rpad[1]) || (j < B.rpad[2]) || (j >= s1 - B.rpad[3]) ||
-                         (k < B.rpad[4]) || (k >= s2 - B.rpad[5]);
-        if (res)
-            v = 1;
-        mp[idx] = v;
+    const long long rows = s0 * s1;
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = warp; r < rows; r += nwarps) {
+        const long long i = r / s1, j = r - (r / s1) * s1;
+        const bool row_res = (i < B.rpad[0]) || (i >= s0 - B.rpad[1]) || (j < B.rpad[2]) || (j >= s1 - B.rpad[3]);
+        const long long base = r * s2;
+        for (long long k = lane; k < s2; k += 32) {
+            const long long idx = base + k;
+            uint8_t v = (morph[idx] == 1 && w[idx] == 2) ? (uint8_t)1 : mp[idx];
+            if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
+                v = 1;
+            mp[idx] = v;
+        }
+    }
+}
+
+// Erosion by thresholding a precomputed squared EDT (subtraction's
+// np.where(d <= r, 0, 1), unpad being the identity without extension), wall
+// planes forced to 0 (set_wall_bcs).  One warp per (i, j) row.
+struct ErodeThr {
+    float r32;
+    double r64;
+    int cmp64;
+    double thr_sq; // >= 0: FFT-ball mode, compare the voxel-unit squared distance
+    int wall[6];
+};
+
+__global__ void k_erode_from_edt(const float *__restrict__ D, uint8_t *__restrict__ out, long long s0,
+                                 long long s1, long long s2, ErodeThr T)
+{
+    const long long rows = s0 * s1;
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = warp; r < rows; r += nwarps) {
+        const long long i = r / s1, j = r - (r / s1) * s1;
+        const bool wrow = (T.wall[0] && i == 0) || (T.wall[1] && i == s0 - 1) || (T.wall[2] && j == 0) ||
+                          (T.wall[3] && j == s1 - 1);
+        const long long base = r * s2;
+        for (long long k = lane; k < s2; k += 32) {
+            const float v = D[base + k];
+            bool within;
+            if (T.thr_sq >= 0.0) {
+                within = (double)v <= T.thr_sq;
+            } else {
+                const float dist = __fsqrt_rn(v);
+                within = T.cmp64 ? ((double)dist <= T.r64) : (dist <= T.r32);
+            }
+            uint8_t o = within ? 0 : 1;
+            if (wrow || (T.wall[4] && k == 0) || (T.wall[5] && k == s2 - 1))
+                o = 0;
+            out[base + k] = o;
+        }
     }
 }
 
@@ -52,7 +119,7 @@ struct Work {
     uint8_t *E;            // morphology scratch
     float *A, *B;
     int *P;
-    uint8_t *mark;
+    uint8_t *M, *mark; // per-block masks and marks of the binary selection
     int *err;
     unsigned long long *cnt; // scalar counter
     void *base;
@@ -62,7 +129,9 @@ static int work_alloc(Work &w, const int64_t *shape, size_t morph_bytes, cudaStr
 {
     const size_t n = (size_t)shape[0] * shape[1] * shape[2];
     const size_t a = (n + 255) & ~(size_t)255;
-    const size_t total = 3 * a + ((morph_bytes + 255) & ~(size_t)255) + a * 4 + a + 512;
+    const size_t nb = (size_t)((shape[0] + 1) / 2) * ((shape[1] + 1) / 2) * ((shape[2] + 1) / 2);
+    const size_t bb = (nb + 255) & ~(size_t)255;
+    const size_t total = 3 * a + ((morph_bytes + 255) & ~(size_t)255) + a * 4 + 2 * bb + 512;
     PMG_TRY(scratch_alloc(&w.base, total, st));
     char *p = (char *)w.base;
     w.t1 = (uint8_t *)p;
@@ -75,8 +144,10 @@ static int work_alloc(Work &w, const int64_t *shape, size_t morph_bytes, cudaStr
     p += (morph_bytes + 255) & ~(size_t)255;
     w.P = (int *)p;
     p += a * 4;
+    w.M = (uint8_t *)p;
+    p += bb;
     w.mark = (uint8_t *)p;
-    p += a;
+    p += bb;
     w.err = (int *)p;
     w.cnt = (unsigned long long *)(p + 256);
     return PMG_OK;
@@ -109,19 +180,36 @@ static int count_sync(const uint8_t *img, const int64_t *shape, const int64_t *b
 static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape, const int32_t *bc,
                            const int32_t *pad, const int32_t *ext_e, const int32_t *ext_d, const float *res,
                            double r_e, int cmp_e, double r_d, int cmp_d, int inlet, const uint8_t *mp,
-                           const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d)
+                           const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d,
+                           const float *De = nullptr)
 {
     const long long n = shape[0] * shape[1] * shape[2];
     const int64_t all[6] = {0, shape[0], 0, shape[1], 0, shape[2]};
     uint8_t *E;
     float *A, *B;
     morph_split(w, shape, bc, ext_e, E, A, B);
-    PMG_TRY(morph_run(pm, w.t1, shape, bc, pad, ext_e, res, r_e, cmp_e, 0, E, A, B, st, ball_e));
+    if (De) {
+        ErodeThr T;
+        T.r32 = (float)r_e;
+        T.r64 = r_e;
+        T.cmp64 = cmp_e;
+        T.thr_sq = ball_e;
+        for (int q = 0; q < 6; q++)
+            T.wall[q] = bc[q] == PMG_BC_WALL;
+        const int ps__ = prof_begin("k_erode_from_edt", st);
+        k_erode_from_edt<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
+            De, w.t1, shape[0], shape[1], shape[2], T);
+        prof_end(ps__, (double)n * 5, st);
+        PMG_CHECK_LAUNCH();
+    } else {
+        PMG_TRY(morph_run(pm, w.t1, shape, bc, pad, ext_e, res, r_e, cmp_e, 0, E, A, B, st, ball_e));
+    }
     uint8_t *cur = w.t1;
     if (inlet) {
         PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
-        PMG_TRY(select_run(w.t1, w.t2, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, -1, w.P, w.mark,
-                           w.err, st));
+        // the eroded image holds only 0 and 1
+        PMG_TRY(select_run_binary(w.t1, w.t2, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, -1, w.P, w.M,
+                                  w.mark, w.err, st));
         PMG_TRY(check_err(w.err, st));
         cur = w.t2;
     }
@@ -133,12 +221,12 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
             PMG_TRY(count_sync(mp, shape, all, 1, w, st, m1));
             if (m1 > 0) {
                 PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
-                PMG_TRY(select_run(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1, w.P,
-                                   w.mark, w.err, st));
+                PMG_TRY(select_run_binary(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1, w.P,
+                                          w.M, w.mark, w.err, st));
                 PMG_TRY(check_err(w.err, st));
                 {
                     const int ps__ = prof_begin("k_constrain", st);
-                    k_constrain<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(cur, w.t3, n);
+                    k_constrain<<<grid_for(n / 16 + 1, 256, 152LL * 32), 256, 0, st>>>(cur, w.t3, n);
                     prof_end(ps__, (double)n * 3, st);
                 }
                 PMG_CHECK_LAUNCH();
@@ -248,7 +336,30 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
     PMG_TRY(work_alloc(w, shape, mb, st));
     uint8_t *morph = nullptr, *wet = nullptr;
     unsigned long long *d_counts = nullptr;
-    int s = scratch_alloc((void **)&morph, (size_t)n, st);
+    // Without periodic axes the erosion's extended image is the same for every
+    // radius (no wrap extension), so its EDT is computed once and thresholded
+    // per radius -- the same values the per-radius EDT would produce.
+    const bool reuse_erosion = bc[0] != PMG_BC_PERIODIC && bc[2] != PMG_BC_PERIODIC && bc[4] != PMG_BC_PERIODIC;
+    float *De = nullptr;
+    int unit_res = -1;
+    for (int k = 0; k < n_radii; k++)
+        if (active[k]) {
+            unit_res = (ball_erode && ball_erode[k] >= 0.0) ? 1 : 0;
+            break;
+        }
+    int s = PMG_OK;
+    if (reuse_erosion && unit_res >= 0) {
+        s = scratch_alloc((void **)&De, (size_t)n * sizeof(float), st);
+        if (s == PMG_OK) {
+            uint8_t *E;
+            float *A, *B;
+            const int32_t zero_ext[6] = {0, 0, 0, 0, 0, 0};
+            morph_split(w, shape, bc, zero_ext, E, A, B);
+            s = erosion_edt_run(pm_img, De, shape, bc, pad, res, unit_res, E, A, st);
+        }
+    }
+    if (s == PMG_OK)
+        s = scratch_alloc((void **)&morph, (size_t)n, st);
     if (s == PMG_OK)
         s = scratch_alloc((void **)&wet, (size_t)n, st);
     if (s == PMG_OK)
@@ -263,22 +374,23 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
             ext_of(bc, pad, ratios + 3 * k, ext);
             // the probe radius is a numpy float64: compare in float64
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext, res, radii[k], 1, radii[k], 1, 1, mp_img,
-                                Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0);
+                                Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
+                                De);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
         if (s != PMG_OK)
             break;
         PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
-        s = select_run(mp_img, wet, 1, shape, bc, pad, nullptr, Bx.outlet, PMG_SEL_OUTLET, 2, w.P, w.mark, w.err,
-                       st);
+        s = select_run_binary(mp_img, wet, 1, shape, bc, pad, nullptr, Bx.outlet, PMG_SEL_OUTLET, 2, w.P, w.M,
+                              w.mark, w.err, st);
         if (s == PMG_OK)
             s = check_err(w.err, st);
         if (s != PMG_OK)
             break;
         {
             const int ps__ = prof_begin("k_drain_update", st);
-            k_drain_update<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(mp_img, morph, wet, shape[0], shape[1],
+            k_drain_update<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(mp_img, morph, wet, shape[0], shape[1],
                                                                     shape[2], Bx);
             prof_end(ps__, (double)n * 4, st);
         }
@@ -293,6 +405,7 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         for (int k = 0; k < n_radii; k++)
             counts[k] = (int64_t)h[(size_t)k];
     }
+    scratch_free(De, st);
     scratch_free(morph, st);
     scratch_free(wet, st);
     scratch_free(d_counts, st);

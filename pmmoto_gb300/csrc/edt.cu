@@ -34,35 +34,6 @@ namespace pmg {
 
 constexpr int kMaxHull = 8; // imported hulls per side (reference keeps <= 5)
 
-struct LineGeo {
-    long long base, stride;
-    int n;
-    int a, b; // coordinates of the line along the two other axes (d1 < d2)
-};
-
-__device__ __forceinline__ LineGeo line_addr(const Lines &L, long long li)
-{
-    LineGeo g;
-    const int a = L.b1lo + (int)(li / L.nb2);
-    const int b = L.b2lo + (int)(li - (li / L.nb2) * L.nb2);
-    g.a = a;
-    g.b = b;
-    if (L.ax == 0) { // lines over (j, k)
-        g.base = (long long)a * L.s2 + b;
-        g.stride = L.s1 * L.s2;
-        g.n = (int)L.s0;
-    } else if (L.ax == 1) { // lines over (i, k)
-        g.base = (long long)a * L.s1 * L.s2 + b;
-        g.stride = L.s2;
-        g.n = (int)L.s1;
-    } else { // lines over (i, j)
-        g.base = ((long long)a * L.s1 + b) * L.s2;
-        g.stride = 1;
-        g.n = (int)L.s2;
-    }
-    return g;
-}
-
 // ---------------------------------------------------------------------------
 // pass 0: squared_edt_1d along axis `ax`
 // ---------------------------------------------------------------------------
@@ -415,7 +386,8 @@ __device__ int boundary_hull(Stack &S, const float *line, long long st, int star
 // envelope pass along axis `ax`: fin -> fout (out of place)
 // ---------------------------------------------------------------------------
 __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
-                           float res, pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me)
+                           float res, pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me,
+                           int redo)
 {
     const long long nlines = Ls.count();
     extern __shared__ uint32_t smem_bm[];
@@ -426,6 +398,9 @@ __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fo
     for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
          li += (long long)gridDim.x * blockDim.x) {
         const LineGeo g = line_addr(Ls, li);
+        // second chance for lines the exact streaming kernel handed back
+        if (redo && !line_marked(fout, me, g, form))
+            continue;
         const float *line = fin + g.base;
         const long long st = g.stride;
         const int n = g.n;
@@ -517,15 +492,6 @@ __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fo
         float nr = has_next ? (is_lower ? given_r : isect(nxt.h, (float)nxt.v, cur.h, (float)cur.v, aniso))
                             : INFINITY;
         float *o = fout + g.base;
-        // morphology epilogue: output row of the unextended volume
-        long long mrow = 0;
-        bool mwall_row = false;
-        if (form == PMG_EDT_MORPH) {
-            const long long io = g.a - me.e0, jo = g.b - me.e1;
-            mrow = (io * me.o1 + jo) * me.o2;
-            mwall_row = (me.wall[0] && io == 0) || (me.wall[1] && io == me.o0 - 1) ||
-                        (me.wall[2] && jo == 0) || (me.wall[3] && jo == me.o1 - 1);
-        }
         for (int i = 0; i < n; i++) {
             const float fi = (float)i;
             while (nr < fi) {
@@ -537,20 +503,7 @@ __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fo
             const float dx = (float)(i - cur.v);
             float val = fadd(fmul(aniso, fmul(dx, dx)), cur.h);
             if (form == PMG_EDT_MORPH) {
-                const int ko = i - me.e2;
-                if (ko < 0 || ko >= me.o2)
-                    continue;
-                bool within;
-                if (me.thr_sq >= 0.0) {
-                    within = (double)val <= me.thr_sq;
-                } else {
-                    const float dist = __fsqrt_rn(val);
-                    within = me.cmp64 ? ((double)dist <= me.r64) : (dist <= me.r32);
-                }
-                uint8_t v = me.dilate ? (uint8_t)within : (uint8_t)!within;
-                if (mwall_row || (me.wall[4] && ko == 0) || (me.wall[5] && ko == me.o2 - 1))
-                    v = 0;
-                me.out[mrow + ko] = v;
+                morph_store(me, g, i, val);
                 continue;
             }
             if (form == PMG_EDT_DIST)
@@ -588,7 +541,7 @@ static int envelope_block(int n)
 
 int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                     const pmg_axis_cfg &cfg, int num_hull, int form, const MorphEpi &me,
-                    cudaStream_t st)
+                    cudaStream_t st, int cap)
 {
     const int n = (int)(Ls.ax == 0 ? Ls.s0 : Ls.ax == 1 ? Ls.s1 : Ls.s2);
     int block = envelope_block(n);
@@ -596,11 +549,17 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     if (smem > 48 * 1024)
         PMG_CUDA(cudaFuncSetAttribute(k_envelope, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
+    int redo = 0;
+    if (exact_path_ok(res, cfg, n)) {
+        // exact integer streaming pass; lines it cannot finish are redone below
+        PMG_TRY(launch_envelope_exact(fin, fout, Ls, res, form, me, st, cap));
+        redo = 1;
+    }
     {
-        const int ps__ = prof_begin("k_envelope", st);
-        k_envelope<<<grid_for(Ls.count(), block, 1LL << 30), block, smem, st>>>(
-        fin, fout, Ls, res, cfg, num_hull, form, me);
-        prof_end(ps__, (double)Ls.count() * n * 4 + (form == PMG_EDT_MORPH ? (double)Ls.count() * me.o2 : (double)Ls.count() * n * 4), st);
+        const int ps__ = prof_begin(redo ? "k_envelope_redo" : "k_envelope", st);
+        k_envelope<<<grid_for(Ls.count(), block, redo ? 152LL * 8 : 1LL << 30), block, smem, st>>>(
+            fin, fout, Ls, res, cfg, num_hull, form, me, redo);
+        prof_end(ps__, redo ? 0.0 : (double)Ls.count() * n * 4 + (form == PMG_EDT_MORPH ? (double)Ls.count() * me.o2 : (double)Ls.count() * n * 4), st);
     }
     PMG_CHECK_LAUNCH();
     return PMG_OK;

@@ -1,6 +1,9 @@
 // Internal interface between the EDT kernels and their users (morphology).
 #pragma once
 
+#include <climits>
+#include <cmath>
+
 #include "pmg_common.cuh"
 
 namespace pmg {
@@ -13,6 +16,35 @@ struct Lines {
     int b1lo, nb1, b2lo, nb2;
     __host__ __device__ long long count() const { return (long long)nb1 * nb2; }
 };
+
+struct LineGeo {
+    long long base, stride;
+    int n;
+    int a, b; // coordinates of the line along the two other axes (d1 < d2)
+};
+
+__device__ __forceinline__ LineGeo line_addr(const Lines &L, long long li)
+{
+    LineGeo g;
+    const int a = L.b1lo + (int)(li / L.nb2);
+    const int b = L.b2lo + (int)(li - (li / L.nb2) * L.nb2);
+    g.a = a;
+    g.b = b;
+    if (L.ax == 0) { // lines over (j, k)
+        g.base = (long long)a * L.s2 + b;
+        g.stride = L.s1 * L.s2;
+        g.n = (int)L.s0;
+    } else if (L.ax == 1) { // lines over (i, k)
+        g.base = (long long)a * L.s1 * L.s2 + b;
+        g.stride = L.s2;
+        g.n = (int)L.s1;
+    } else { // lines over (i, j)
+        g.base = ((long long)a * L.s1 + b) * L.s2;
+        g.stride = 1;
+        g.n = (int)L.s2;
+    }
+    return g;
+}
 
 __host__ inline Lines all_lines(const int64_t *shape, int ax)
 {
@@ -47,11 +79,68 @@ struct MorphEpi {
                           // with this integer bound instead (FFT-ball modes)
 };
 
+// Store of the fused morphology epilogue: "distance within the radius" at
+// position i of line g (extended coordinates) -> 0/1 of the unextended volume.
+__device__ __forceinline__ void morph_put(const MorphEpi &me, const LineGeo &g, int i, bool within)
+{
+    const long long io = g.a - me.e0, jo = g.b - me.e1;
+    const int ko = i - me.e2;
+    if (ko < 0 || ko >= me.o2)
+        return;
+    uint8_t v = me.dilate ? (uint8_t)within : (uint8_t)!within;
+    if ((me.wall[0] && io == 0) || (me.wall[1] && io == me.o0 - 1) || (me.wall[2] && jo == 0) ||
+        (me.wall[3] && jo == me.o1 - 1) || (me.wall[4] && ko == 0) || (me.wall[5] && ko == me.o2 - 1))
+        v = 0;
+    me.out[(io * me.o1 + jo) * me.o2 + ko] = v;
+}
+
+// The threshold of the epilogue on a squared distance `val`.
+__host__ __device__ __forceinline__ bool morph_within(const MorphEpi &me, float val)
+{
+    if (me.thr_sq >= 0.0)
+        return (double)val <= me.thr_sq;
+#ifdef __CUDA_ARCH__
+    const float dist = __fsqrt_rn(val);
+#else
+    const float dist = sqrtf(val); // IEEE correctly rounded, as __fsqrt_rn
+#endif
+    return me.cmp64 ? ((double)dist <= me.r64) : (dist <= me.r32);
+}
+
+__device__ __forceinline__ void morph_store(const MorphEpi &me, const LineGeo &g, int i, float val)
+{
+    morph_put(me, g, i, morph_within(me, val));
+}
+
+// Lines the exact streaming kernel hands back to the general one carry a
+// marker in their first output: NaN (float forms) or 255 (morphology).
+__device__ __forceinline__ bool line_marked(const float *fout, const MorphEpi &me, const LineGeo &g, int form)
+{
+    if (form == PMG_EDT_MORPH) {
+        const long long io = g.a - me.e0, jo = g.b - me.e1;
+        return me.out[(io * me.o1 + jo) * me.o2] == 255;
+    }
+    const float v = fout[g.base];
+    return v != v;
+}
+
+// cap: heights above cap * res^2 are treated as absent and outputs above it
+// are written as FLT_MAX (INT_MAX: no cap).
+int launch_envelope_exact(const float *fin, float *fout, const Lines &Ls, float res, int form,
+                          const MorphEpi &me, cudaStream_t st, int cap);
+bool exact_path_ok(float res, const pmg_axis_cfg &cfg, int n);
+// Largest integer T < lim with morph_within(T * a) (the threshold is monotone
+// in the squared distance), -1 when not even 0 is within, lim when T >= lim.
+int morph_threshold(const MorphEpi &me, float a, int lim);
+// Last morphology pass on exact integer heights: within iff E(x) <= T.
+int launch_env_thresh(const float *fin, const Lines &Ls, float res, int T, const MorphEpi &me,
+                      cudaStream_t st);
+
 int launch_pass0(const uint8_t *img, float *out, const Lines &Ls, float res,
                  const pmg_axis_cfg &cfg, cudaStream_t st);
 int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                     const pmg_axis_cfg &cfg, int num_hull, int form, const MorphEpi &me,
-                    cudaStream_t st);
+                    cudaStream_t st, int cap = INT_MAX);
 int edt3d_run(const uint8_t *img, float *out, float *tmp, const int64_t *shape, const float *res,
               const pmg_axis_cfg *cfg, int num_hull, int form, cudaStream_t st);
 

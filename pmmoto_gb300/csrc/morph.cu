@@ -40,27 +40,51 @@ __device__ __forceinline__ long long src_index(const ExtAxis &a, long long x, bo
     return p;
 }
 
-// E[x] = img[wrap(x)] (0 on wall planes); logical_not for addition.
+// E[x] = img[wrap(x)] (0 on wall planes); logical_not for addition.  One warp
+// per (x0, x1) row of the extended volume: the row's source row and wall state
+// are resolved once, lanes walk x2.
 __global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ ext, ExtGeo G,
                          int logical_not)
 {
     const long long X1 = G.ax[1].X, X2 = G.ax[2].X;
-    const long long total = G.ax[0].X * X1 * X2;
+    const long long rows = G.ax[0].X * X1;
     const long long S1 = G.ax[1].S, S2 = G.ax[2].S;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        const long long x2 = e % X2;
-        const long long r = e / X2;
-        const long long x1 = r % X1;
-        const long long x0 = r / X1;
-        bool zero = false;
-        const long long s0 = src_index(G.ax[0], x0, zero);
-        const long long s1 = src_index(G.ax[1], x1, zero);
-        const long long s2 = src_index(G.ax[2], x2, zero);
-        uint8_t v = zero ? (uint8_t)0 : img[(s0 * S1 + s1) * S2 + s2];
-        if (logical_not)
-            v = v == 0 ? 1 : 0;
-        ext[e] = v;
+    const ExtAxis &a2 = G.ax[2];
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long q0 = a2.own_lo + a2.ext_lo; // x2 of the first own voxel
+    for (long long r = warp; r < rows; r += nwarps) {
+        const long long x0 = r / X1, x1 = r - (r / X1) * X1;
+        bool zero_row = false;
+        const long long s0 = src_index(G.ax[0], x0, zero_row);
+        const long long s1 = src_index(G.ax[1], x1, zero_row);
+        const uint8_t *src = img + (s0 * S1 + s1) * S2;
+        uint8_t *dst = ext + r * X2;
+        for (long long x2 = lane; x2 < X2; x2 += 32) {
+            long long s2;
+            bool zero = zero_row;
+            if (a2.periodic) {
+                // the extension never exceeds the own length, so one wrap suffices
+                s2 = x2 - q0;
+                if (s2 < 0)
+                    s2 += a2.own_len;
+                else if (s2 >= a2.own_len)
+                    s2 -= a2.own_len;
+                if (s2 < 0 || s2 >= a2.own_len) // extensions beyond one period
+                    s2 = src_index(a2, x2, zero);
+                else
+                    s2 += a2.own_lo;
+            } else {
+                s2 = x2;
+                if ((a2.wall_lo && x2 == 0) || (a2.wall_hi && x2 == S2 - 1))
+                    zero = true;
+            }
+            uint8_t v = zero ? (uint8_t)0 : src[s2];
+            if (logical_not)
+                v = v == 0 ? 1 : 0;
+            dst[x2] = v;
+        }
     }
 }
 
@@ -89,7 +113,7 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
     const long long total = (long long)X[0] * X[1] * X[2];
     {
         const int ps__ = prof_begin("k_extend", st);
-        k_extend<<<grid_for(total, 256, 1LL << 30), 256, 0, st>>>(img, E, G, dilate);
+        k_extend<<<grid_for(X[0] * X[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, dilate);
         prof_end(ps__, (double)total * 2, st);
     }
     PMG_CHECK_LAUNCH();
@@ -118,18 +142,70 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
     if (thr_sq >= 0.0)
         res = unit;
 
+    // Isotropic power-of-two voxels make every squared distance an exact
+    // integer multiple of res^2, and the reference's threshold becomes
+    // "E <= T" for one integer T: the middle pass then only needs heights up
+    // to T and the last pass is a union of intervals.
+    int T = INT_MIN;
+    if (res[0] == res[1] && res[1] == res[2] && exact_path_ok(res[1], plain, (int)X[1]) &&
+        exact_path_ok(res[2], plain, (int)X[2])) {
+        const int nm = (int)(X[1] > X[2] ? X[1] : X[2]);
+        const int lim = (1 << 24) - nm * nm - 1;
+        const int t = morph_threshold(me, res[2] * res[2], lim);
+        if (t < lim)
+            T = t;
+    }
+
     PMG_TRY(launch_pass0(E, A, all_lines(X, 0), res[0], plain, st));
     Lines L1 = all_lines(X, 1); // lines over (i, k): keep i inside the unextended range
     L1.b1lo = me.e0;
     L1.nb1 = (int)shape[0];
-    PMG_TRY(launch_envelope(A, B, L1, res[1], plain, 4, PMG_EDT_SQUARED, me, st));
+    PMG_TRY(launch_envelope(A, B, L1, res[1], plain, 4, PMG_EDT_SQUARED, me, st, T == INT_MIN ? INT_MAX : T));
     Lines L2 = all_lines(X, 2); // lines over (i, j): both inside the unextended range
     L2.b1lo = me.e0;
     L2.nb1 = (int)shape[0];
     L2.b2lo = me.e1;
     L2.nb2 = (int)shape[1];
+    if (T != INT_MIN)
+        return launch_env_thresh(B, L2, res[2], T, me, st);
     PMG_TRY(launch_envelope(B, nullptr, L2, res[2], plain, 4, PMG_EDT_MORPH, me, st));
     return PMG_OK;
+}
+
+// Squared EDT of the unextended erosion image (wall planes zeroed), for
+// subdomains without periodic axes, where every radius sees this same image:
+// E is uint8 scratch of the volume, A float scratch, D receives the result.
+// unit_res selects the voxel-unit distances of the FFT-ball modes.
+int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, const float *res, int unit_res, uint8_t *E, float *A,
+                    cudaStream_t st)
+{
+    ExtGeo G;
+    for (int d = 0; d < 3; d++) {
+        ExtAxis &a = G.ax[d];
+        if (bc[2 * d] == PMG_BC_PERIODIC) {
+            set_error("erosion EDT reuse needs a subdomain without periodic axes");
+            return PMG_EINVAL;
+        }
+        a.periodic = 0;
+        a.own_lo = pad[2 * d];
+        a.own_len = (int)(shape[d] - pad[2 * d] - pad[2 * d + 1]);
+        a.ext_lo = 0;
+        a.wall_lo = bc[2 * d] == PMG_BC_WALL;
+        a.wall_hi = bc[2 * d + 1] == PMG_BC_WALL;
+        a.S = shape[d];
+        a.X = shape[d];
+    }
+    {
+        const int ps__ = prof_begin("k_extend", st);
+        k_extend<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, 0);
+        prof_end(ps__, (double)shape[0] * shape[1] * shape[2] * 2, st);
+    }
+    PMG_CHECK_LAUNCH();
+    const float unit[3] = {1.0f, 1.0f, 1.0f};
+    const float *r = unit_res ? unit : res;
+    pmg_axis_cfg plain[3] = {{0, 0, 0, 0, 1, 0, 0, 0}, {0, 0, 0, 0, 1, 0, 0, 0}, {0, 0, 0, 0, 1, 0, 0, 0}};
+    return edt3d_run(E, D, A, shape, r, plain, 4, PMG_EDT_SQUARED, st);
 }
 
 size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext)

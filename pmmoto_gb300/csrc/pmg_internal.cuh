@@ -9,11 +9,17 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
               int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq = -1.0);
 size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext);
+int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, const float *res, int unit_res, uint8_t *E, float *A,
+                    cudaStream_t st);
 
 int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shape,
                const int32_t *bc, const int32_t *pad, const int64_t *inlet_box,
                const int64_t *outlet_box, int mode, int phase, int *P, uint8_t *mark, int *err,
                cudaStream_t st);
+int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
+                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 

@@ -116,21 +116,26 @@ __global__ void k_update_buffer(T *img, Halo H)
     }
 }
 
+// One warp per row of the box; lanes walk the row's contiguous bytes.
 __global__ void k_count_eq(const uint8_t *__restrict__ img, long long s1, long long s2, long long lo0,
                            long long n0, long long lo1, long long n1, long long lo2, long long n2,
                            uint8_t value, unsigned long long *cnt)
 {
-    const long long tot = n0 * n1 * n2;
-    unsigned long long c = 0;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < tot;
-         q += (long long)gridDim.x * blockDim.x) {
-        const long long k = q % n2, j = (q / n2) % n1, i = q / (n2 * n1);
-        c += img[((lo0 + i) * s1 + lo1 + j) * s2 + lo2 + k] == value;
+    const long long rows = n0 * n1;
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned int c = 0;
+    for (long long r = warp; r < rows; r += nwarps) {
+        const long long i = r / n1, j = r - (r / n1) * n1;
+        const uint8_t *row = img + ((lo0 + i) * s1 + lo1 + j) * s2 + lo2;
+        for (long long k = lane; k < n2; k += 32)
+            c += row[k] == value;
     }
     for (int o = 16; o > 0; o >>= 1)
         c += __shfl_down_sync(0xffffffffu, c, o);
-    if ((threadIdx.x & 31) == 0 && c)
-        atomicAdd(cnt, c);
+    if (lane == 0 && c)
+        atomicAdd(cnt, (unsigned long long)c);
 }
 
 __global__ void k_max_f32(const float *__restrict__ x, long long s1, long long s2, long long lo0, long long n0,
@@ -208,7 +213,7 @@ int count_eq_async(const uint8_t *img, const int64_t *shape, const int64_t *box,
         return PMG_OK;
     {
         const int ps__ = prof_begin("k_count_eq", st);
-        k_count_eq<<<grid_for(n0 * n1 * n2, 256, 152LL * 8), 256, 0, st>>>(img, shape[1], shape[2], box[0], n0, box[2],
+        k_count_eq<<<grid_for(n0 * n1 * 32, 256, 152LL * 64), 256, 0, st>>>(img, shape[1], shape[2], box[0], n0, box[2],
                                                                       n1, box[4], n2, value, d_cnt);
         prof_end(ps__, (double)(n0 * n1 * n2), st);
     }

@@ -25,6 +25,7 @@ __all__ = ["connect_components", "gen_img_to_label_map", "phase_count", "inlet_o
            "inlet_outlet_connected_img", "isolated_img"]
 
 SEL_INLET, SEL_OUTLET, SEL_BOTH, SEL_ISOLATED = 1, 2, 3, 4
+SEL_BINARY = 16
 
 _TORCH_BY_SIZE = {1: torch.uint8, 2: torch.int16, 4: torch.int32, 8: torch.int64}
 

@@ -77,3 +77,48 @@ def test_cc_determinism(C):
     b, n2 = C.connect_components(img, sd)
     np.testing.assert_array_equal(a, b)
     assert n1 == n2
+
+
+@pytest.mark.parametrize("kinds", [("end", "end", "end"), ("periodic", "wall", "periodic"), ("periodic",) * 3])
+def test_cc_many_tiles_vs_oracle(C, kinds):
+    """Volumes spanning many 4x8x32 labelling tiles in every direction."""
+    from pmmoto_gb300.core import initialize
+    rng = np.random.default_rng(77)
+    vox = (37, 45, 101)
+    bts = tuple((k, k) for k in kinds)
+    box = tuple((0.0, v / 64) for v in vox)
+    sd = initialize(vox, box=box, boundary_types=bts)
+    g = O.Geom(vox, boundary_types=bts, box=box)
+    for p in (0.3, 0.6):
+        img = O.update_buffer(g, (rng.random(sd.voxels) < p).astype(np.uint8))
+        lbl, n = C.connect_components(img, sd)
+        want, wn = O.connect_components(img, g)
+        np.testing.assert_array_equal(lbl, want)
+        assert n == wn
+
+
+@pytest.mark.parametrize("kinds", [("end", "wall", "wall"), ("end", "periodic", "periodic"), ("end", "end", "periodic")])
+@pytest.mark.parametrize("vox", [(33, 27, 41), (21, 37, 141)])
+def test_binary_block_selection_vs_oracle(C, kinds, vox):
+    """The 2x2x2-block selection (phase filter, or the binary flag) equals the
+    voxel-level selection of the reference, odd sizes included; the second
+    shape spans several 8 x 16 x 64-voxel tiles on every axis."""
+    import torch
+    from pmmoto_gb300.core import initialize
+    from pmmoto_gb300.core.geometry import geo_of
+    rng = np.random.default_rng(5)
+    bts = tuple((k, k) for k in kinds)
+    inlet, outlet = ((True, False), (False, False), (False, False)), ((False, True), (False, False), (False, False))
+    box = tuple((0.0, v / 64) for v in vox)
+    sd = initialize(vox, box=box, boundary_types=bts, inlet=inlet, outlet=outlet)
+    g = O.Geom(vox, boundary_types=bts, box=box, inlet=inlet, outlet=outlet)
+    for p in (0.35, 0.5, 0.7):
+        img = O.update_buffer(g, (rng.random(sd.voxels) < p).astype(np.uint8))
+        t = torch.as_tensor(img, device="cuda")
+        for mode, fn in ((C.SEL_INLET, O.inlet_connected_img), (C.SEL_OUTLET, O.outlet_connected_img),
+                         (C.SEL_BOTH, O.inlet_outlet_connected_img), (C.SEL_ISOLATED, O.isolated_img)):
+            got = C.select_device(geo_of(sd), t, mode | C.SEL_BINARY).cpu().numpy()
+            np.testing.assert_array_equal(got, fn(g, img).astype(np.uint8))
+        multi = O.update_buffer(g, rng.integers(0, 3, sd.voxels).astype(np.uint8))
+        for phase in (1, 2):
+            np.testing.assert_array_equal(C.outlet_connected_img(sd, multi, phase), O.outlet_connected_img(g, multi, phase))

@@ -31,17 +31,22 @@ def test_morph_golden(M, golden, golden_meta, ci):
 
 
 @pytest.mark.parametrize("kinds", list(itertools.product(["end", "wall", "periodic"], repeat=3))[::2])
-def test_morph_random_vs_oracle(M, kinds):
+@pytest.mark.parametrize("scale", [20, 16])
+def test_morph_random_vs_oracle(M, kinds, scale):
+    """scale 16 gives power-of-two voxels (1/16), which take the exact integer
+    passes; radii 0.125 and 0.1875 are then exactly 2 and 3 voxels (ties)."""
     rng = np.random.default_rng(sum(map(ord, "".join(kinds))))
     vox = (20, 17, 23)
-    box = tuple((0.0, v / 20) for v in vox)
+    box = tuple((0.0, v / scale) for v in vox)
     bts = tuple((k, k) for k in kinds)
     from pmmoto_gb300.core import initialize
     sd = initialize(vox, box=box, boundary_types=bts)
     g = O.Geom(vox, boundary_types=bts, box=box)
     img = (rng.random(sd.voxels) > 0.3).astype(np.uint8)
     img = O.update_buffer(g, img)
-    for r in (0.05, 0.1, np.float64(0.15), 0.24):
+    for r in (0.05, 0.1, np.float64(0.15), 0.24, 0.125, np.float64(0.1875)):
+        if r < 1.0 / scale:
+            continue  # the reference rejects radii below the voxel size
         np.testing.assert_array_equal(M.erode(sd, img, r), O.erode(g, img, r))
         np.testing.assert_array_equal(M.dilate(sd, img, r), O.dilate(g, img, r))
     np.testing.assert_array_equal(M.opening(sd, img, 0.1), O.opening(g, img, 0.1))
