@@ -349,7 +349,8 @@ def run_case(args):
     """Single-operator cases on a seeded random medium (for ncu captures and
     per-operator rates): 'edt' = edt3d, 'cc' = connected components (with the
     periodic merge when --bc periodic), 'morph' = erosion (EDT path); N^3
-    voxels, all faces periodic or all walls (--bc)."""
+    voxels, all faces periodic or all walls (--bc); 'select' = inlet-connected
+    pore space of the drainage pack (its geometry, N-2 own voxels per axis)."""
     import torch
 
     import pmmoto_gb300 as P
@@ -371,8 +372,20 @@ def run_case(args):
     cfg = D.edt3d_cfg((per, per, per))
     res = np.ones(3, np.float32)
 
+    if args.case == "select":
+        # inlet-connected pore space of the drainage pack geometry (walls y/z,
+        # inlet x-), binary 2x2x2-block labelling
+        kw = geom_kwargs()
+        kw["box"] = ((0.0, (n - 2) / 512.0),) * 3
+        sd = P.initialize((n - 2,) * 3, **kw)
+        geo = geo_of(sd)
+        pm = P.domain_generation.gen_pm_spheres_domain(sd, torch.as_tensor(make_pack(1234), device="cuda"))
+        img = pm.img
+
     def op():
-        if args.case == "edt":
+        if args.case == "select":
+            CC.select_device(geo, img, CC.SEL_INLET | CC.SEL_BINARY)
+        elif args.case == "edt":
             D.edt3d_device(img, res, cfg, True, out)
         elif args.case == "cc":
             CC.connect_components_device(img, geo)
@@ -409,7 +422,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
-    ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph"])
+    ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph", "select"])
     ap.add_argument("--n", type=int, default=512, help="volume side of the single-operator cases")
     ap.add_argument("--bc", default="periodic", choices=["periodic", "wall"],
                     help="boundary type of every face in the single-operator cases")

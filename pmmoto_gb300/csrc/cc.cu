@@ -131,57 +131,6 @@ static void host_tables(int nb[13][3], unsigned short adj[13])
     }
 }
 
-template <typename T>
-__global__ void k_cc_init(const T *__restrict__ img, int *__restrict__ P, long long n)
-{
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        P[i] = img[i] != 0 ? (int)i : -1;
-}
-
-template <typename T>
-__global__ void k_cc_merge(const T *__restrict__ img, int *P, Vol3 V, int *err)
-{
-    const long long n = V.s0 * V.s1 * V.s2;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const T v = img[idx];
-        if (v == 0)
-            continue;
-        const long long k = idx % V.s2;
-        const long long r = idx / V.s2;
-        const long long j = r % V.s1;
-        const long long i = r / V.s1;
-        unsigned same = 0;
-#pragma unroll
-        for (int q = 0; q < 13; q++) {
-            const long long a = i + c_nb[q][0], b = j + c_nb[q][1], c = k + c_nb[q][2];
-            if (a < 0 || b < 0 || c < 0 || b >= V.s1 || c >= V.s2)
-                continue;
-            if (img[(a * V.s1 + b) * V.s2 + c] == v)
-                same |= 1u << q;
-        }
-        unsigned covered = 0;
-        while (same & ~covered) {
-            const int q = __ffs(same & ~covered) - 1;
-            const long long a = i + c_nb[q][0], b = j + c_nb[q][1], c = k + c_nb[q][2];
-            unite(P, (int)idx, (int)((a * V.s1 + b) * V.s2 + c), err);
-            // everything 26-connected to q inside `same` is united through q
-            unsigned grp = 1u << q, prev = 0;
-            while (grp != prev) {
-                prev = grp;
-                unsigned g = grp;
-                while (g) {
-                    const int w = __ffs(g) - 1;
-                    g &= g - 1;
-                    grp |= c_adj[w] & same;
-                }
-            }
-            covered |= grp;
-        }
-    }
-}
-
 // ---- tiled labelling ------------------------------------------------------
 // Tiles of 4 x 8 x 32 voxels (C order, the last axis contiguous), one thread
 // per voxel.  Phase 1 unites equal neighbours inside the tile with a shared-
@@ -203,11 +152,27 @@ __device__ __forceinline__ int sfind(const int *L, int x)
     return x;
 }
 
+// root search with path halving (same argument as find_root_halve)
+__device__ __forceinline__ int sfind_halve(int *L, int x)
+{
+    int p = L[x];
+    int it = 0;
+    while (p != x && it++ < kTile) {
+        const int g = L[p];
+        if (g == p)
+            return p;
+        L[x] = g;
+        x = g;
+        p = L[x];
+    }
+    return x;
+}
+
 __device__ __forceinline__ void sunite(int *L, int a, int b)
 {
     for (int it = 0; it < 4 * kTile; it++) {
-        a = sfind(L, a);
-        b = sfind(L, b);
+        a = sfind_halve(L, a);
+        b = sfind_halve(L, b);
         if (a == b)
             return;
         if (a < b) {
@@ -224,7 +189,9 @@ __device__ __forceinline__ void sunite(int *L, int a, int b)
     }
 }
 
-__device__ __forceinline__ unsigned cover_group(unsigned q_mask, unsigned same)
+// adj: shared-memory copy of c_adj (lanes index it with different values,
+// which constant memory would serialise)
+__device__ __forceinline__ unsigned cover_group(unsigned q_mask, unsigned same, const unsigned short *adj)
 {
     unsigned grp = q_mask, prev = 0;
     while (grp != prev) {
@@ -233,10 +200,16 @@ __device__ __forceinline__ unsigned cover_group(unsigned q_mask, unsigned same)
         while (g) {
             const int w = __ffs(g) - 1;
             g &= g - 1;
-            grp |= c_adj[w] & same;
+            grp |= adj[w] & same;
         }
     }
     return grp;
+}
+
+__device__ __forceinline__ void load_adj(unsigned short *s_adj)
+{
+    if (threadIdx.x < 13)
+        s_adj[threadIdx.x] = c_adj[threadIdx.x];
 }
 
 template <typename T>
@@ -244,6 +217,8 @@ __global__ void __launch_bounds__(kTile) k_cc_tile(const T *__restrict__ img, in
 {
     __shared__ T sv[kTile];
     __shared__ int L[kTile];
+    __shared__ unsigned short s_adj[13];
+    load_adj(s_adj);
     const int nt1 = (int)((V.s1 + kT1 - 1) / kT1), nt2 = (int)((V.s2 + kT2 - 1) / kT2);
     const long long tile = blockIdx.x;
     const long long ti = tile / ((long long)nt1 * nt2);
@@ -271,7 +246,7 @@ __global__ void __launch_bounds__(kTile) k_cc_tile(const T *__restrict__ img, in
         while (same & ~covered) {
             const int q = __ffs(same & ~covered) - 1;
             sunite(L, t, ((a + c_nb[q][0]) * kT1 + b + c_nb[q][1]) * kT2 + c + c_nb[q][2]);
-            covered |= cover_group(1u << q, same);
+            covered |= cover_group(1u << q, same, s_adj);
         }
     }
     __syncthreads();
@@ -295,6 +270,9 @@ __global__ void __launch_bounds__(kTile) k_cc_tile(const T *__restrict__ img, in
 template <typename T>
 __global__ void k_cc_cross(const T *__restrict__ img, int *P, Vol3 V, int *err)
 {
+    __shared__ unsigned short s_adj[13];
+    load_adj(s_adj);
+    __syncthreads();
     // volumes are below 2^31 voxels, so 32-bit index arithmetic suffices
     const int n = (int)(V.s0 * V.s1 * V.s2);
     const int S1 = (int)V.s1, S2 = (int)V.s2;
@@ -326,7 +304,7 @@ __global__ void k_cc_cross(const T *__restrict__ img, int *P, Vol3 V, int *err)
         unsigned lm = local;
         while (lm) { // groups reached through in-tile neighbours are done
             const int q = __ffs(lm) - 1;
-            const unsigned grp = cover_group(1u << q, same);
+            const unsigned grp = cover_group(1u << q, same, s_adj);
             covered |= grp;
             lm &= ~grp;
         }
@@ -334,7 +312,7 @@ __global__ void k_cc_cross(const T *__restrict__ img, int *P, Vol3 V, int *err)
             const int q = __ffs(same & ~covered) - 1;
             const int ai = i + c_nb[q][0], bj = j + c_nb[q][1], ck = k + c_nb[q][2];
             unite(P, idx, (ai * S1 + bj) * S2 + ck, err);
-            covered |= cover_group(1u << q, same);
+            covered |= cover_group(1u << q, same, s_adj);
         }
     }
 }
@@ -1110,18 +1088,32 @@ __device__ __forceinline__ unsigned bmask_of(int q, uint64_t mlo, uint64_t mhi)
 // Neighbours in `conn` connected to those in `q_mask` through chains of
 // touching neighbours: a union with one of them links all of them, because
 // the union of each touching pair is done by the later block of the pair.
-__device__ __forceinline__ unsigned bcover(unsigned q_mask, unsigned conn, uint64_t mlo, uint64_t mhi)
+struct BTabs {
+    unsigned short adj[13];
+    uint8_t pair[13][13];
+};
+
+__device__ __forceinline__ void load_btabs(BTabs &tb)
+{
+    if (threadIdx.x < 13)
+        tb.adj[threadIdx.x] = c_adj[threadIdx.x];
+    for (int q = threadIdx.x; q < 169; q += blockDim.x)
+        tb.pair[q / 13][q % 13] = c_bt_pair[q / 13][q % 13];
+}
+
+__device__ __forceinline__ unsigned bcover(unsigned q_mask, unsigned conn, uint64_t mlo, uint64_t mhi,
+                                           const BTabs &tb)
 {
     unsigned grp = q_mask, frontier = q_mask;
     while (frontier) {
         const int w = __ffs(frontier) - 1;
         frontier &= frontier - 1;
         const unsigned mw = bmask_of(w, mlo, mhi);
-        unsigned cand = c_adj[w] & conn & ~grp;
+        unsigned cand = tb.adj[w] & conn & ~grp;
         while (cand) {
             const int u = __ffs(cand) - 1;
             cand &= cand - 1;
-            if ((mw & c_bt_pair[w][u]) && (bmask_of(u, mlo, mhi) & c_bt_pair[u][w])) {
+            if ((mw & tb.pair[w][u]) && (bmask_of(u, mlo, mhi) & tb.pair[u][w])) {
                 grp |= 1u << u;
                 frontier |= 1u << u;
             }
@@ -1130,14 +1122,43 @@ __device__ __forceinline__ unsigned bcover(unsigned q_mask, unsigned conn, uint6
     return grp;
 }
 
+// Foreground of the block selection: the voxels of one value (or nonzero)
+// of a uint8 image ...
+struct SrcImg {
+    const uint8_t *img;
+    int fgval;
+    __device__ __forceinline__ bool fg(long long idx, int, int, int) const { return fg_of(img[idx], fgval); }
+};
+
+// ... or an erosion read off a capped squared EDT: voxels with E > T stay,
+// wall planes are cleared (subtraction + set_wall_bcs,
+// morphological_operators.py:171-228).
+struct SrcErode {
+    const uint16_t *E;
+    int T;
+    int s0, s1, s2;
+    int wall[6];
+    __device__ __forceinline__ bool fg(long long idx, int i, int j, int k) const
+    {
+        if ((wall[0] && i == 0) || (wall[1] && i == s0 - 1) || (wall[2] && j == 0) || (wall[3] && j == s1 - 1) ||
+            (wall[4] && k == 0) || (wall[5] && k == s2 - 1))
+            return false;
+        return (int)E[idx] > T;
+    }
+};
+
 // Phase 1 on tiles of 4 x 8 x 32 blocks (8 x 16 x 64 voxels), one thread per
-// block: block masks from the image, then a shared-memory union-find of the
+// block: block masks from the source, then a shared-memory union-find of the
 // tile whose roots are the smallest block index of each tile-local part.
-__global__ void __launch_bounds__(kTile) k_bcc_tile(const uint8_t *__restrict__ img, int *__restrict__ P,
-                                                   uint8_t *__restrict__ M, BGrid G, int fgval)
+// Every later step reads the block masks M, never the source again.
+template <class Src>
+__global__ void __launch_bounds__(kTile) k_bcc_tile(Src src, int *__restrict__ P, uint8_t *__restrict__ M,
+                                                   BGrid G)
 {
     __shared__ uint8_t sm[kTile];
     __shared__ int L[kTile];
+    __shared__ BTabs tb;
+    load_btabs(tb);
     const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
     const int tile = blockIdx.x;
     const int ti = tile / (nt1 * nt2), tj = (tile / nt2) % nt1, tk = tile % nt2;
@@ -1154,8 +1175,7 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(const uint8_t *__restrict__ 
 #pragma unroll
                 for (int z = 0; z < 2; z++) {
                     const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2 + z;
-                    if (i < G.s0 && j < G.s1 && k < G.s2 &&
-                        fg_of(img[((long long)i * G.s1 + j) * G.s2 + k], fgval))
+                    if (i < G.s0 && j < G.s1 && k < G.s2 && src.fg(((long long)i * G.s1 + j) * G.s2 + k, i, j, k))
                         m |= 1u << ((x * 2 + y) * 2 + z);
                 }
     }
@@ -1185,7 +1205,7 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(const uint8_t *__restrict__ 
         while (conn & ~covered) {
             const int q = __ffs(conn & ~covered) - 1;
             sunite(L, t, ((a + c_nb[q][0]) * kT1 + b + c_nb[q][1]) * kT2 + c + c_nb[q][2]);
-            covered |= bcover(1u << q, conn, mlo, mhi);
+            covered |= bcover(1u << q, conn, mlo, mhi, tb);
         }
     }
     __syncthreads();
@@ -1209,6 +1229,9 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(const uint8_t *__restrict__ 
 // other tiles; neighbours reached through an in-tile neighbour are skipped.
 __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int *err)
 {
+    __shared__ BTabs tb;
+    load_btabs(tb);
+    __syncthreads();
     const int nb = G.b0 * G.b1 * G.b2;
     for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < nb; bi += gridDim.x * blockDim.x) {
         const int r = bi / G.b2;
@@ -1246,14 +1269,14 @@ __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int 
         unsigned lm = local;
         while (lm) {
             const int q = __ffs(lm) - 1;
-            const unsigned grp = bcover(1u << q, conn, mlo, mhi);
+            const unsigned grp = bcover(1u << q, conn, mlo, mhi, tb);
             covered |= grp;
             lm &= ~grp;
         }
         while (conn & ~covered) {
             const int q = __ffs(conn & ~covered) - 1;
             unite(P, bi, ((c0 + c_nb[q][0]) * G.b1 + c1 + c_nb[q][1]) * G.b2 + c2 + c_nb[q][2], err);
-            covered |= bcover(1u << q, conn, mlo, mhi);
+            covered |= bcover(1u << q, conn, mlo, mhi, tb);
         }
     }
 }
@@ -1288,7 +1311,14 @@ static int ensure_block_tables()
 
 // periodic seams at block level: a foreground halo voxel joins the block of the
 // own voxel it copies when that voxel is foreground too
-__global__ void k_bcc_twins(const uint8_t *__restrict__ img, int *P, BGrid G, Twins W, int fgval, int *err)
+__device__ __forceinline__ bool mfg(const uint8_t *__restrict__ M, const BGrid &G, long long i, long long j,
+                                    long long k)
+{
+    const int b = (int)(((i >> 1) * G.b1 + (j >> 1)) * G.b2 + (k >> 1));
+    return (M[b] >> ((((int)i & 1) * 2 + ((int)j & 1)) * 2 + ((int)k & 1))) & 1;
+}
+
+__global__ void k_bcc_twins(const uint8_t *__restrict__ M, int *P, BGrid G, Twins W, int *err)
 {
     const long long n = W.s0 * W.s1 * W.s2;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
@@ -1315,10 +1345,7 @@ __global__ void k_bcc_twins(const uint8_t *__restrict__ img, int *P, BGrid G, Tw
                 }
             }
         }
-        if (!halo || !ok || !fg_of(img[idx], fgval))
-            continue;
-        const long long tw = (t[0] * W.s1 + t[1]) * W.s2 + t[2];
-        if (!fg_of(img[tw], fgval))
+        if (!halo || !ok || !mfg(M, G, c[0], c[1], c[2]) || !mfg(M, G, t[0], t[1], t[2]))
             continue;
         const int ba = (int)(((c[0] >> 1) * G.b1 + (c[1] >> 1)) * G.b2 + (c[2] >> 1));
         const int bb = (int)(((t[0] >> 1) * G.b1 + (t[1] >> 1)) * G.b2 + (t[2] >> 1));
@@ -1335,15 +1362,15 @@ __global__ void k_bcc_flatten(int *P, int nb, int *err)
     }
 }
 
-__global__ void k_bcc_mark(const uint8_t *__restrict__ img, const int *__restrict__ P, BGrid G, Box bx,
-                           uint8_t *mark, uint8_t bit, int fgval)
+__global__ void k_bcc_mark(const uint8_t *__restrict__ M, const int *__restrict__ P, BGrid G, Box bx,
+                           uint8_t *mark, uint8_t bit)
 {
     const long long n = bx.size();
     const long long w = bx.hi[2] - bx.lo[2], h = bx.hi[1] - bx.lo[1];
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
         const long long k = bx.lo[2] + q % w, j = bx.lo[1] + (q / w) % h, i = bx.lo[0] + q / (w * h);
-        if (!fg_of(img[(i * G.s1 + j) * G.s2 + k], fgval))
+        if (!mfg(M, G, i, j, k))
             continue;
         const int p = P[((int)(i >> 1) * G.b1 + (int)(j >> 1)) * G.b2 + (int)(k >> 1)];
         if (p >= 0 && !(mark[p] & bit))
@@ -1351,48 +1378,62 @@ __global__ void k_bcc_mark(const uint8_t *__restrict__ img, const int *__restric
     }
 }
 
-// one warp per (i, j) row
+// One thread per block: the block's root and marks decide all its voxels at
+// once; kept foreground voxels receive `val`, everything else 0.  A warp
+// covers 32 consecutive blocks, i.e. 64 contiguous voxels of each of the
+// block's four rows.
 template <typename TO>
-__global__ void k_bcc_select(const uint8_t *__restrict__ img, const int *__restrict__ P,
-                             const uint8_t *__restrict__ mark, BGrid G, int mode, int fgval,
-                             TO *__restrict__ out)
+__global__ void k_bcc_select(const uint8_t *__restrict__ M, const int *__restrict__ P,
+                             const uint8_t *__restrict__ mark, BGrid G, int mode, TO val, TO *__restrict__ out)
 {
-    const int rows = G.s0 * G.s1;
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int r = warp; r < rows; r += nwarps) {
-        const int i = r / G.s1, j = r - (r / G.s1) * G.s1;
-        const long long base = (long long)r * G.s2;
-        const int brow = ((i >> 1) * G.b1 + (j >> 1)) * G.b2;
-        for (int k = lane; k < G.s2; k += 32) {
-            const uint8_t v = img[base + k];
-            TO o = 0;
-            if (fg_of(v, fgval)) {
-                const int p = P[brow + (k >> 1)];
-                const uint8_t mk = p >= 0 ? mark[p] : 0;
-                const bool in = mk & 1, ou = mk & 2;
-                bool keep;
-                if (mode == PMG_SEL_INLET)
-                    keep = in;
-                else if (mode == PMG_SEL_OUTLET)
-                    keep = ou;
-                else if (mode == PMG_SEL_BOTH)
-                    keep = in && ou;
-                else
-                    keep = !(in || ou);
-                if (keep)
-                    o = (TO)v;
-            }
-            out[base + k] = o;
+    const int nb = G.b0 * G.b1 * G.b2;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int r = b / G.b2;
+        const int c2 = b - r * G.b2;
+        const int c0 = r / G.b1;
+        const int c1 = r - c0 * G.b1;
+        unsigned m = M[b];
+        if (m) {
+            const int p = P[b];
+            const uint8_t mk = p >= 0 ? mark[p] : 0;
+            const bool in = mk & 1, ou = mk & 2;
+            bool keep;
+            if (mode == PMG_SEL_INLET)
+                keep = in;
+            else if (mode == PMG_SEL_OUTLET)
+                keep = ou;
+            else if (mode == PMG_SEL_BOTH)
+                keep = in && ou;
+            else
+                keep = !(in || ou);
+            if (!keep)
+                m = 0;
         }
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int y = 0; y < 2; y++) {
+                const int i = 2 * c0 + x, j = 2 * c1 + y;
+                if (i >= G.s0 || j >= G.s1)
+                    continue;
+                TO *row = out + ((long long)i * G.s1 + j) * G.s2;
+#pragma unroll
+                for (int z = 0; z < 2; z++) {
+                    const int k = 2 * c2 + z;
+                    if (k < G.s2)
+                        row[k] = ((m >> ((x * 2 + y) * 2 + z)) & 1) ? val : (TO)0;
+                }
+            }
     }
 }
 
-// Binary selection: P and mark need one int / one byte per 2x2x2 block.
-int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
-                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
-                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+__host__ __device__ inline const uint8_t *src_elem(const SrcImg &s) { return s.img; }
+__host__ __device__ inline const uint16_t *src_elem(const SrcErode &s) { return s.E; }
+
+template <class Src>
+static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
+                           const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
+                           int val, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
 {
     PMG_TRY(ensure_tables());
     PMG_TRY(ensure_block_tables());
@@ -1409,8 +1450,8 @@ int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_
     {
         const int nt = ((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
         const int ps__ = prof_begin("k_bcc_tile", st);
-        k_bcc_tile<<<nt, kTile, 0, st>>>(img, P, M, G, fgval);
-        prof_end(ps__, (double)n + (double)nb * 5, st);
+        k_bcc_tile<Src><<<nt, kTile, 0, st>>>(src, P, M, G);
+        prof_end(ps__, (double)n * sizeof(*src_elem(src)) + (double)nb * 5, st);
     }
     PMG_CHECK_LAUNCH();
     {
@@ -1421,7 +1462,7 @@ int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_
     PMG_CHECK_LAUNCH();
     if (any_periodic(bc)) {
         const int ps__ = prof_begin("k_bcc_twins", st);
-        k_bcc_twins<<<grid_for(n, 256, 152LL * 32), 256, 0, st>>>(img, P, G, make_twins(shape, bc, pad), fgval, err);
+        k_bcc_twins<<<grid_for(n, 256, 152LL * 32), 256, 0, st>>>(M, P, G, make_twins(shape, bc, pad), err);
         prof_end(ps__, 0.0, st);
         PMG_CHECK_LAUNCH();
     }
@@ -1447,8 +1488,7 @@ int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_
         }
         if (b.size() > 0) {
             const int ps__ = prof_begin("k_bcc_mark", st);
-            k_bcc_mark<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(img, P, G, b, mark, (uint8_t)(1 << w),
-                                                                          fgval);
+            k_bcc_mark<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(M, P, G, b, mark, (uint8_t)(1 << w));
             prof_end(ps__, (double)b.size() * 5, st);
             PMG_CHECK_LAUNCH();
         }
@@ -1456,15 +1496,44 @@ int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_
     {
         const int ps__ = prof_begin("k_bcc_select", st);
         if (out_bytes == 1)
-            k_bcc_select<uint8_t><<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
-                img, P, mark, G, mode, fgval, (uint8_t *)out);
+            k_bcc_select<uint8_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(M, P, mark, G, mode, (uint8_t)val,
+                                                                               (uint8_t *)out);
         else
-            k_bcc_select<uint64_t><<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
-                img, P, mark, G, mode, fgval, (uint64_t *)out);
-        prof_end(ps__, (double)n * (1.0 + out_bytes) + (double)nb * 5, st);
+            k_bcc_select<uint64_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
+                M, P, mark, G, mode, (uint64_t)val, (uint64_t *)out);
+        prof_end(ps__, (double)n * out_bytes + (double)nb * 5, st);
     }
     PMG_CHECK_LAUNCH();
     return PMG_OK;
+}
+
+// Binary selection: P and mark need one int / one byte per 2x2x2 block.  Kept
+// voxels receive `fgval`, or 1 for fgval < 0 (an image of 0s and 1s).
+int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
+                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+{
+    SrcImg src{img, fgval};
+    return bcc_select_core(src, out, out_bytes, shape, bc, pad, inlet_box, outlet_box, mode, fgval >= 0 ? fgval : 1,
+                           P, M, mark, err, st);
+}
+
+// Erosion fused into the selection: the foreground is E > T off the wall
+// planes, with E a capped squared EDT (uint16, units of res^2) of the
+// unextended image; kept voxels receive 1.
+int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, const int32_t *bc,
+                     const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *P,
+                     uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+{
+    SrcErode src;
+    src.E = E;
+    src.T = T;
+    src.s0 = (int)shape[0];
+    src.s1 = (int)shape[1];
+    src.s2 = (int)shape[2];
+    for (int q = 0; q < 6; q++)
+        src.wall[q] = bc[q] == PMG_BC_WALL;
+    return bcc_select_core(src, out, 1, shape, bc, pad, inlet_box, outlet_box, mode, 1, P, M, mark, err, st);
 }
 
 // Selection with caller-provided scratch: P (n int32), mark (n bytes rounded

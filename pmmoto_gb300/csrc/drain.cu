@@ -12,6 +12,7 @@
 // per-pressure counts.
 #include <vector>
 
+#include "edt_internal.cuh"
 #include "pmg_internal.cuh"
 
 namespace pmg {
@@ -181,14 +182,21 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
                            const int32_t *pad, const int32_t *ext_e, const int32_t *ext_d, const float *res,
                            double r_e, int cmp_e, double r_d, int cmp_d, int inlet, const uint8_t *mp,
                            const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d,
-                           const float *De = nullptr)
+                           const float *De = nullptr, const uint16_t *KC = nullptr, int Te = -1)
 {
     const long long n = shape[0] * shape[1] * shape[2];
     const int64_t all[6] = {0, shape[0], 0, shape[1], 0, shape[2]};
     uint8_t *E;
     float *A, *B;
     morph_split(w, shape, bc, ext_e, E, A, B);
-    if (De) {
+    uint8_t *cur = w.t1;
+    if (KC && inlet) {
+        PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+        PMG_TRY(select_run_erode(KC, Te, w.t2, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, w.P, w.M, w.mark,
+                                 w.err, st));
+        PMG_TRY(check_err(w.err, st));
+        cur = w.t2;
+    } else if (De) {
         ErodeThr T;
         T.r32 = (float)r_e;
         T.r64 = r_e;
@@ -204,8 +212,7 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
     } else {
         PMG_TRY(morph_run(pm, w.t1, shape, bc, pad, ext_e, res, r_e, cmp_e, 0, E, A, B, st, ball_e));
     }
-    uint8_t *cur = w.t1;
-    if (inlet) {
+    if (inlet && cur == w.t1) {
         PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
         // the eroded image holds only 0 and 1
         PMG_TRY(select_run_binary(w.t1, w.t2, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, -1, w.P, w.M,
@@ -348,7 +355,50 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
             break;
         }
     int s = PMG_OK;
+    // Isotropic power-of-two voxels: the erosion EDT is kept as a capped
+    // integer volume (uint16, values above the largest erosion bound clamp)
+    // and each radius's erosion "E > T" is read off it inside the inlet
+    // selection -- no eroded image is written.
+    uint16_t *KC = nullptr;
+    std::vector<int> Te((size_t)n_radii, -1);
     if (reuse_erosion && unit_res >= 0) {
+        const float unit[3] = {1.0f, 1.0f, 1.0f};
+        const float *r = unit_res ? unit : res;
+        const pmg_axis_cfg plain = {0, 0, 0, 0, 1, 0, 0, 0};
+        bool ok = r[0] == r[1] && r[1] == r[2];
+        for (int d = 0; d < 3 && ok; d++)
+            ok = exact_path_ok(r[d], plain, (int)shape[d]);
+        int Tcap = 0;
+        for (int k = 0; k < n_radii && ok; k++) {
+            if (!active[k])
+                continue;
+            MorphEpi me{};
+            me.r32 = (float)radii[k];
+            me.r64 = radii[k];
+            me.cmp64 = 1;
+            me.thr_sq = ball_erode ? ball_erode[k] : -1.0;
+            Te[(size_t)k] = morph_threshold(me, r[0] * r[0], kCapMaxT + 1);
+            ok = Te[(size_t)k] >= 0 && Te[(size_t)k] <= kCapMaxT;
+            Tcap = Te[(size_t)k] > Tcap ? Te[(size_t)k] : Tcap;
+        }
+        if (ok) {
+            s = scratch_alloc((void **)&KC, (size_t)n * sizeof(uint16_t), st);
+            int nonbinary = 0;
+            if (s == PMG_OK) {
+                uint8_t *E;
+                float *A, *B;
+                const int32_t zero_ext[6] = {0, 0, 0, 0, 0, 0};
+                morph_split(w, shape, bc, zero_ext, E, A, B);
+                s = erosion_cap_run(pm_img, KC, shape, bc, pad, Tcap, E, (uint16_t *)A, (uint16_t *)B,
+                                    (int *)((char *)w.err + 128), &nonbinary, st);
+            }
+            if (s == PMG_OK && nonbinary) {
+                s = scratch_free(KC, st);
+                KC = nullptr;
+            }
+        }
+    }
+    if (s == PMG_OK && !KC && reuse_erosion && unit_res >= 0) {
         s = scratch_alloc((void **)&De, (size_t)n * sizeof(float), st);
         if (s == PMG_OK) {
             uint8_t *E;
@@ -375,7 +425,7 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
             // the probe radius is a numpy float64: compare in float64
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext, res, radii[k], 1, radii[k], 1, 1, mp_img,
                                 Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
-                                De);
+                                De, KC, Te[(size_t)k]);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
@@ -406,6 +456,7 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
             counts[k] = (int64_t)h[(size_t)k];
     }
     scratch_free(De, st);
+    scratch_free(KC, st);
     scratch_free(morph, st);
     scratch_free(wet, st);
     scratch_free(d_counts, st);

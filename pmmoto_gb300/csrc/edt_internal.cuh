@@ -136,6 +136,16 @@ int morph_threshold(const MorphEpi &me, float a, int lim);
 int launch_env_thresh(const float *fin, const Lines &Ls, float res, int T, const MorphEpi &me,
                       cudaStream_t st);
 
+// Capped integer morphology (morph_cap.cu): isotropic power-of-two voxels,
+// binary image, threshold T <= kCapMaxT; KA, KB: uint16 scratch of the
+// extended volume.
+constexpr int kCapMaxT = 1023;
+bool cap_path_ok(const float *res, const int64_t *X, int T);
+int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
+                  cudaStream_t st);
+int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, const int64_t *X, int T,
+                cudaStream_t st);
+
 int launch_pass0(const uint8_t *img, float *out, const Lines &Ls, float res,
                  const pmg_axis_cfg &cfg, cudaStream_t st);
 int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,

@@ -44,7 +44,7 @@ __device__ __forceinline__ long long src_index(const ExtAxis &a, long long x, bo
 // per (x0, x1) row of the extended volume: the row's source row and wall state
 // are resolved once, lanes walk x2.
 __global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ ext, ExtGeo G,
-                         int logical_not)
+                         int logical_not, int *nonbinary)
 {
     const long long X1 = G.ax[1].X, X2 = G.ax[2].X;
     const long long rows = G.ax[0].X * X1;
@@ -83,6 +83,8 @@ __global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ 
             uint8_t v = zero ? (uint8_t)0 : src[s2];
             if (logical_not)
                 v = v == 0 ? 1 : 0;
+            else if (v > 1 && nonbinary)
+                *nonbinary = 1;
             dst[x2] = v;
         }
     }
@@ -111,9 +113,14 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
         }
     }
     const long long total = (long long)X[0] * X[1] * X[2];
+    // last int of B: "the image holds a value above 1" (erosion only; the
+    // capped pipeline needs a binary image)
+    int *flag = dilate ? nullptr : (int *)(B + total) - 1;
+    if (flag)
+        PMG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     {
         const int ps__ = prof_begin("k_extend", st);
-        k_extend<<<grid_for(X[0] * X[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, dilate);
+        k_extend<<<grid_for(X[0] * X[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, dilate, flag);
         prof_end(ps__, (double)total * 2, st);
     }
     PMG_CHECK_LAUNCH();
@@ -154,6 +161,16 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
         const int t = morph_threshold(me, res[2] * res[2], lim);
         if (t < lim)
             T = t;
+    }
+
+    if (T != INT_MIN && cap_path_ok(res, X, T)) {
+        int nonbin = 0;
+        if (flag) {
+            PMG_CUDA(cudaMemcpyAsync(&nonbin, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+            PMG_CUDA(cudaStreamSynchronize(st));
+        }
+        if (!nonbin)
+            return morph_cap_run(E, (uint16_t *)A, (uint16_t *)B, X, T, me, st);
     }
 
     PMG_TRY(launch_pass0(E, A, all_lines(X, 0), res[0], plain, st));
@@ -198,7 +215,7 @@ int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const in
     }
     {
         const int ps__ = prof_begin("k_extend", st);
-        k_extend<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, 0);
+        k_extend<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, 0, nullptr);
         prof_end(ps__, (double)shape[0] * shape[1] * shape[2] * 2, st);
     }
     PMG_CHECK_LAUNCH();
@@ -206,6 +223,46 @@ int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const in
     const float *r = unit_res ? unit : res;
     pmg_axis_cfg plain[3] = {{0, 0, 0, 0, 1, 0, 0, 0}, {0, 0, 0, 0, 1, 0, 0, 0}, {0, 0, 0, 0, 1, 0, 0, 0}};
     return edt3d_run(E, D, A, shape, r, plain, 4, PMG_EDT_SQUARED, st);
+}
+
+// Capped integer squared EDT of the same erosion image (isotropic power-of-two
+// voxels, no periodic axes): KC = min(E, Tcap + 1) in units of res^2, uint16.
+// The pipeline needs a binary image; *nonbinary reports an image with values
+// above 1 (KC is then not written and the caller takes the float path).
+int erosion_cap_run(const uint8_t *img, uint16_t *KC, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, int Tcap, uint8_t *E, uint16_t *KA, uint16_t *KB, int *flag,
+                    int *nonbinary, cudaStream_t st)
+{
+    ExtGeo G;
+    for (int d = 0; d < 3; d++) {
+        ExtAxis &a = G.ax[d];
+        if (bc[2 * d] == PMG_BC_PERIODIC) {
+            set_error("erosion EDT reuse needs a subdomain without periodic axes");
+            return PMG_EINVAL;
+        }
+        a.periodic = 0;
+        a.own_lo = pad[2 * d];
+        a.own_len = (int)(shape[d] - pad[2 * d] - pad[2 * d + 1]);
+        a.ext_lo = 0;
+        a.wall_lo = bc[2 * d] == PMG_BC_WALL;
+        a.wall_hi = bc[2 * d + 1] == PMG_BC_WALL;
+        a.S = shape[d];
+        a.X = shape[d];
+    }
+    PMG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    {
+        const int ps__ = prof_begin("k_extend", st);
+        k_extend<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, 0, flag);
+        prof_end(ps__, (double)shape[0] * shape[1] * shape[2] * 2, st);
+    }
+    PMG_CHECK_LAUNCH();
+    int h = 0;
+    PMG_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PMG_CUDA(cudaStreamSynchronize(st));
+    *nonbinary = h;
+    if (h)
+        return PMG_OK;
+    return edt_cap_run(E, KA, KB, KC, shape, Tcap, st);
 }
 
 size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext)

@@ -1,0 +1,389 @@
+// Capped integer morphology for isotropic power-of-two voxels (sm_103a).
+//
+// With a voxel size res = 2^k on every axis the reference's float32 squared
+// distances are exact integer multiples of res^2 (src/pmmoto/filters/distance/
+// _distance.hpp:135-272 performs only exact float operations on them, see
+// edt_exact.cu), so the reference's test "sqrt(d2) <= r" (morphological_
+// operators.py:103-228) is "E <= T" for the integer squared distance E and one
+// integer bound T (morph_threshold).  Only values up to T matter, which gives
+// a different, cheaper pipeline with the same result:
+//
+//   pass A (rows, the contiguous axis): E_A = min(d^2, T + 1), d the distance
+//     to the nearest zero of the row -- one warp per row, ballots per chunk of
+//     32 voxels, uint16 output;
+//   pass B (axis 1, strided): E_B = min(E_A envelope, T + 1) -- one thread
+//     per line, lanes on adjacent lines (coalesced), lower envelope of the
+//     parabolas with E_A <= T, each output written a fixed W = floor(sqrt T)
+//     positions behind the input (no later parabola can lower a value to <= T
+//     after that), so all lanes store the same position; live parabolas lie
+//     in [i - 2W, i] and fit a 64-entry ring when T <= 1023;
+//   pass C (axis 0, strided): a height E_B <= T covers |x - v| <= floor(sqrt(
+//     T - E_B)); x is within iff some interval covers it -- one thread per
+//     line, a 64-bit window of pending positions, the result fused with the
+//     unpadding and the wall rule.
+//
+// The exact squared EDT is separable in any axis order, so doing the linear
+// pass on the contiguous axis leaves both envelope passes on strided axes,
+// where a warp reads and writes 32 adjacent voxels at a time.  The reference's
+// linear pass restarts at changes between nonzero values (multi-label
+// images), which depends on the axis: this pipeline serves binary images only.
+#include "edt_internal.cuh"
+
+namespace pmg {
+
+constexpr int kCapRing = 64;
+
+struct CapGeo {
+    int X0, X1, X2;       // extended shape
+    int j0, nj, k0, nk;   // unextended ranges of axes 1 and 2
+};
+
+// ---- pass A: rows -------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E, uint16_t *__restrict__ KA,
+                                                  long long rows, int X2, int T)
+{
+    extern __shared__ uint16_t s_dq[];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint16_t *dq = s_dq + (threadIdx.x >> 5) * X2;
+    // the row's bytes, staged first with independent loads
+    uint8_t *sb = (uint8_t *)(s_dq + (blockDim.x >> 5) * X2) + (threadIdx.x >> 5) * X2;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int big = T + 1;
+    const int nc = (X2 + 31) >> 5;
+    const int none = 1 << 20;
+    for (long long r = warp; r < rows; r += nwarps) {
+        const uint8_t *src = E + r * X2;
+#pragma unroll 4
+        for (int x = lane; x < X2; x += 32)
+            sb[x] = src[x];
+        __syncwarp();
+        // backward: distance to the next zero at or after x (65535: none)
+        int nextz = none;
+        for (int c = nc - 1; c >= 0; c--) {
+            const int x = (c << 5) + lane;
+            const bool z = x < X2 && sb[x] == 0;
+            const unsigned zm = __ballot_sync(FULL, z);
+            const unsigned ge = zm & (FULL << lane);
+            const int q = ge ? (c << 5) + __ffs(ge) - 1 : nextz;
+            if (x < X2)
+                dq[x] = (uint16_t)min(q - x, 65535);
+            if (zm)
+                nextz = (c << 5) + __ffs(zm) - 1;
+        }
+        __syncwarp();
+        // forward: distance to the previous zero, combined
+        int prevz = -none;
+        for (int c = 0; c < nc; c++) {
+            const int x = (c << 5) + lane;
+            const int dqx = x < X2 ? dq[x] : 65535;
+            const unsigned zm = __ballot_sync(FULL, x < X2 && dqx == 0);
+            const unsigned le = zm & (lane == 31 ? FULL : ((2u << lane) - 1u));
+            const int p = le ? (c << 5) + 31 - __clz(le) : prevz;
+            const int d = min(x - p, dqx);
+            if (x < X2)
+                KA[r * X2 + x] = (uint16_t)(d >= 32768 ? big : min(d * d, big));
+            if (zm)
+                prevz = (c << 5) + 31 - __clz(zm);
+        }
+        __syncwarp();
+    }
+}
+
+// ---- pass B: capped envelope along axis 1 --------------------------------------
+// Ring entries pack a height (<= T <= 1023) and a vertex (< 2048): K << 11 | v.
+__device__ __forceinline__ int cap_val(int ent, int x)
+{
+    const int d = x - (ent & 2047);
+    return (ent >> 11) + d * d;
+}
+
+// Per-line state of the capped envelope; RING (a power of two) >= 2W + 2.
+template <int RING>
+struct CapLine {
+    int *R; // ring slot s of this thread at R[s * 128]
+    int bot, top, e;
+    __device__ __forceinline__ int &at(int c) const { return R[(c & (RING - 1)) * 128]; }
+
+    // consume height K at position i (K > T: absent), then return the value
+    // at x = i - W (big when above T); x < 0 returns nothing meaningful
+    __device__ __forceinline__ int step(int i, int K, int T, int W, int big)
+    {
+        if (K <= T) {
+            while (top > bot) {
+                const int t = at(top), u = at(top - 1);
+                const int Kt = t >> 11, Vt = t & 2047, Ku = u >> 11, Vu = u & 2047;
+                const int n1 = K - Kt + (i - Vt) * (i + Vt), d1 = 2 * (i - Vt);
+                const int n2 = Kt - Ku + (Vt - Vu) * (Vt + Vu), d2 = 2 * (Vt - Vu);
+                if (n1 * d2 > n2 * d1)
+                    break;
+                if (e == top)
+                    e--;
+                top--;
+            }
+            top++;
+            at(top) = (K << 11) | i;
+            if (top == bot)
+                e = bot;
+        }
+        const int x = i - W;
+        if (x < 0)
+            return big;
+        // parabolas with v + W < x exceed T at every later position
+        while (bot <= top && (at(bot) & 2047) + W < x)
+            bot++;
+        if (e < bot)
+            e = bot;
+        if (top < bot)
+            return big;
+        int ce = at(e);
+        while (e < top) {
+            const int cn = at(e + 1);
+            if (cap_val(cn, x) > cap_val(ce, x))
+                break;
+            ce = cn;
+            e++;
+        }
+        const int Ev = cap_val(ce, x);
+        return Ev <= T ? Ev : big;
+    }
+};
+
+constexpr int kCapChunk = 8; // heights loaded ahead per line (memory-level parallelism)
+
+// AX = 1: lines over (x0 in [0, X0), x2 in [k0, k0 + nk)) along axis 1;
+// AX = 0: lines over (x1 in [j0, j0 + nj), x2 in [k0, k0 + nk)) along axis 0.
+// One thread per line; each loop trip loads the next kCapChunk heights before
+// it processes the current ones, so a thread keeps several loads in flight.
+template <int AX, int RING>
+__global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA, uint16_t *__restrict__ KB,
+                                                 CapGeo G, int T, int W)
+{
+    __shared__ int ring[RING * 128];
+    const long long nlines = (long long)(AX == 1 ? G.X0 : G.nj) * G.nk;
+    const long long st = AX == 1 ? (long long)G.X2 : (long long)G.X1 * G.X2;
+    const int n = AX == 1 ? G.X1 : G.X0;
+    const int big = T + 1;
+    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
+         li += (long long)gridDim.x * blockDim.x) {
+        const long long q = li / G.nk;
+        const int x2 = G.k0 + (int)(li - q * G.nk);
+        const long long base = AX == 1 ? q * G.X1 * G.X2 + x2 : (G.j0 + q) * G.X2 + x2;
+        const uint16_t *in = KA + base;
+        uint16_t *out = KB + base;
+        CapLine<RING> L{ring + threadIdx.x, 0, -1, 0};
+        int cur[kCapChunk];
+#pragma unroll
+        for (int u = 0; u < kCapChunk; u++)
+            cur[u] = u < n ? (int)in[u * st] : big;
+        for (int i0 = 0; i0 < n + W; i0 += kCapChunk) {
+            int nxt[kCapChunk];
+#pragma unroll
+            for (int u = 0; u < kCapChunk; u++) {
+                const int ii = i0 + kCapChunk + u;
+                nxt[u] = ii < n ? (int)in[(long long)ii * st] : big;
+            }
+#pragma unroll
+            for (int u = 0; u < kCapChunk; u++) {
+                const int i = i0 + u;
+                const int v = L.step(i, cur[u], T, W, big);
+                const int x = i - W;
+                if (x >= 0 && x < n)
+                    out[(long long)x * st] = (uint16_t)v;
+            }
+#pragma unroll
+            for (int u = 0; u < kCapChunk; u++)
+                cur[u] = nxt[u];
+        }
+    }
+}
+
+// ---- pass C: intervals along axis 0, fused epilogue ----------------------------
+__device__ __forceinline__ int isqrt_small(int m)
+{
+    int r = (int)__fsqrt_rn((float)m);
+    if (r * r > m)
+        r--;
+    else if ((r + 1) * (r + 1) <= m)
+        r++;
+    return r;
+}
+
+__global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ KB, CapGeo G, int T, int W,
+                                                  MorphEpi me)
+{
+    const long long nlines = (long long)G.nj * G.nk;
+    const long long st = (long long)G.X1 * G.X2;
+    const int n = G.X0;
+    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
+         li += (long long)gridDim.x * blockDim.x) {
+        const int x1 = G.j0 + (int)(li / G.nk);
+        const int x2 = G.k0 + (int)(li - (li / G.nk) * G.nk);
+        const uint16_t *in = KB + (long long)x1 * G.X2 + x2;
+        const long long io0 = -me.e0;
+        const long long jo = x1 - me.e1, ko = x2 - me.e2;
+        const bool wall_jk = (me.wall[2] && jo == 0) || (me.wall[3] && jo == me.o1 - 1) ||
+                             (me.wall[4] && ko == 0) || (me.wall[5] && ko == me.o2 - 1);
+        uint8_t *dst = me.out + jo * me.o2 + ko;
+        const long long ost = me.o1 * me.o2;
+        uint64_t pend = 0; // bit b: position i - b is covered
+        int reach = -1;
+        const int big = T + 1;
+        int cur[kCapChunk];
+#pragma unroll
+        for (int u = 0; u < kCapChunk; u++)
+            cur[u] = u < n ? (int)in[u * st] : big;
+        for (int i0 = 0; i0 < n + W; i0 += kCapChunk) {
+            int nxt[kCapChunk];
+#pragma unroll
+            for (int u = 0; u < kCapChunk; u++) {
+                const int ii = i0 + kCapChunk + u;
+                nxt[u] = ii < n ? (int)in[(long long)ii * st] : big;
+            }
+#pragma unroll
+            for (int u = 0; u < kCapChunk; u++) {
+                const int i = i0 + u;
+                pend <<= 1;
+                if (i < n) {
+                    const int K = cur[u];
+                    if (K <= T) {
+                        const int w = isqrt_small(T - K);
+                        pend |= (2ull << w) - 1ull;
+                        reach = max(reach, i + w);
+                    }
+                    if (reach >= i)
+                        pend |= 1ull;
+                }
+                const int x = i - W;
+                const long long io = io0 + x;
+                if (x < 0 || x >= n || io < 0 || io >= me.o0)
+                    continue;
+                const bool within = (pend >> W) & 1ull;
+                uint8_t v = me.dilate ? (uint8_t)within : (uint8_t)!within;
+                if (wall_jk || (me.wall[0] && io == 0) || (me.wall[1] && io == me.o0 - 1))
+                    v = 0;
+                dst[io * ost] = v;
+            }
+#pragma unroll
+            for (int u = 0; u < kCapChunk; u++)
+                cur[u] = nxt[u];
+        }
+    }
+}
+
+// the ring holds the live parabolas, at most 2W + 2
+template <int AX>
+static int launch_cap_mid(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, int W, long long lines,
+                          cudaStream_t st)
+{
+    const unsigned grid = grid_for(lines, 128, 1LL << 30);
+    if (2 * W + 2 <= 16)
+        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W);
+    else if (2 * W + 2 <= 32)
+        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W);
+    else
+        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W);
+    return PMG_OK;
+}
+
+bool cap_path_ok(const float *res, const int64_t *X, int T)
+{
+    if (!(res[0] == res[1] && res[1] == res[2]) || T < 0 || T > kCapMaxT)
+        return false;
+    const pmg_axis_cfg plain = {0, 0, 0, 0, 1, 0, 0, 0};
+    for (int d = 0; d < 3; d++)
+        if (!exact_path_ok(res[d], plain, (int)X[d]))
+            return false;
+    return true;
+}
+
+int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
+                  cudaStream_t st)
+{
+    int W = 0;
+    while ((W + 1) * (W + 1) <= T)
+        W++;
+    CapGeo G;
+    G.X0 = (int)X[0];
+    G.X1 = (int)X[1];
+    G.X2 = (int)X[2];
+    G.j0 = me.e1;
+    G.nj = (int)me.o1;
+    G.k0 = me.e2;
+    G.nk = (int)me.o2;
+    const long long rows = (long long)G.X0 * G.X1;
+    const long long vox = rows * G.X2;
+    {
+        const int block = 256;
+        const size_t smem = (size_t)(block / 32) * G.X2 * (sizeof(uint16_t) + 1);
+        if (smem > 48 * 1024)
+            PMG_CUDA(cudaFuncSetAttribute(k_cap_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int ps__ = prof_begin("k_cap_rows", st);
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T);
+        prof_end(ps__, (double)vox * 3, st);
+    }
+    PMG_CHECK_LAUNCH();
+    {
+        const long long lines = (long long)G.X0 * G.nk;
+        const int ps__ = prof_begin("k_cap_mid", st);
+        PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st));
+        prof_end(ps__, (double)lines * G.X1 * 4, st);
+    }
+    PMG_CHECK_LAUNCH();
+    {
+        const long long lines = (long long)G.nj * G.nk;
+        const int ps__ = prof_begin("k_cap_last", st);
+        k_cap_last<<<grid_for(lines, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me);
+        prof_end(ps__, (double)lines * G.X0 * 2 + (double)me.o0 * me.o1 * me.o2, st);
+    }
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+// Capped squared EDT of a binary image without extension: E = min(exact d^2
+// in units of res^2, T + 1) as uint16, all three passes on the same volume.
+int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, const int64_t *X, int T,
+                cudaStream_t st)
+{
+    int W = 0;
+    while ((W + 1) * (W + 1) <= T)
+        W++;
+    CapGeo G;
+    G.X0 = (int)X[0];
+    G.X1 = (int)X[1];
+    G.X2 = (int)X[2];
+    G.j0 = 0;
+    G.nj = G.X1;
+    G.k0 = 0;
+    G.nk = G.X2;
+    const long long rows = (long long)G.X0 * G.X1;
+    const long long vox = rows * G.X2;
+    {
+        const int block = 256;
+        const size_t smem = (size_t)(block / 32) * G.X2 * (sizeof(uint16_t) + 1);
+        if (smem > 48 * 1024)
+            PMG_CUDA(cudaFuncSetAttribute(k_cap_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int ps__ = prof_begin("k_cap_rows", st);
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T);
+        prof_end(ps__, (double)vox * 3, st);
+    }
+    PMG_CHECK_LAUNCH();
+    {
+        const long long lines = (long long)G.X0 * G.nk;
+        const int ps__ = prof_begin("k_cap_mid", st);
+        PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st));
+        prof_end(ps__, (double)vox * 4, st);
+    }
+    PMG_CHECK_LAUNCH();
+    {
+        const long long lines = (long long)G.nj * G.nk;
+        const int ps__ = prof_begin("k_cap_mid0", st);
+        PMG_TRY(launch_cap_mid<0>(KB, KC, G, T, W, lines, st));
+        prof_end(ps__, (double)vox * 4, st);
+    }
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+} // namespace pmg

@@ -12,6 +12,9 @@ size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_
 int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const int32_t *bc,
                     const int32_t *pad, const float *res, int unit_res, uint8_t *E, float *A,
                     cudaStream_t st);
+int erosion_cap_run(const uint8_t *img, uint16_t *KC, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, int Tcap, uint8_t *E, uint16_t *KA, uint16_t *KB, int *flag,
+                    int *nonbinary, cudaStream_t st);
 
 int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shape,
                const int32_t *bc, const int32_t *pad, const int64_t *inlet_box,
@@ -20,6 +23,9 @@ int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shap
 int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
                       const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
                       int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st);
+int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, const int32_t *bc,
+                     const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *P,
+                     uint8_t *M, uint8_t *mark, int *err, cudaStream_t st);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 
