@@ -28,79 +28,13 @@
 #include <vector>
 
 #include "pmg_common.cuh"
+#include "uf.cuh"
 
 namespace pmg {
-
-constexpr int kFindCap = 1 << 24;
-constexpr int kUniteCap = 1 << 20;
 
 struct Vol3 {
     long long s0, s1, s2;
 };
-
-__device__ __forceinline__ int ld(const int *p) { return __ldcg(p); }
-
-__device__ __forceinline__ int find_root(const int *P, int x, int *err)
-{
-    int p = ld(P + x);
-    int it = 0;
-    while (p != x) {
-        x = p;
-        p = ld(P + x);
-        if (++it > kFindCap) {
-            atomicExch(err, 1);
-            break;
-        }
-    }
-    return x;
-}
-
-// Root search with path halving: each visited element is re-pointed to its
-// grandparent.  Parents only ever point to smaller indices and an element's
-// ancestors stay its ancestors, so a plain store of an ancestor never breaks a
-// link; a store that overwrites a concurrent atomicMin on a former root is
-// harmless because that union retries with the value the atomic returned.
-__device__ __forceinline__ int find_root_halve(int *P, int x, int *err)
-{
-    int p = ld(P + x);
-    int it = 0;
-    while (p != x) {
-        const int g = ld(P + p);
-        if (g == p)
-            return p;
-        P[x] = g;
-        x = g;
-        p = ld(P + x);
-        if (++it > kFindCap) {
-            atomicExch(err, 1);
-            break;
-        }
-    }
-    return x;
-}
-
-// Playne-Hawick union (atomicMin links the larger root under the smaller).
-__device__ __forceinline__ void unite(int *P, int a, int b, int *err)
-{
-    for (int it = 0; it < kUniteCap; it++) {
-        a = find_root_halve(P, a, err);
-        b = find_root_halve(P, b, err);
-        if (a == b)
-            return;
-        if (a < b) {
-            int old = atomicMin(P + b, a);
-            if (old == b)
-                return;
-            b = old;
-        } else {
-            int old = atomicMin(P + a, b);
-            if (old == a)
-                return;
-            a = old;
-        }
-    }
-    atomicExch(err, 2);
-}
 
 // The 13 already-scanned neighbours (C order) and their mutual 26-adjacency.
 __constant__ int c_nb[13][3];
@@ -317,15 +251,7 @@ __global__ void k_cc_cross(const T *__restrict__ img, int *P, Vol3 V, int *err)
     }
 }
 
-// Seam twins: every halo voxel of a periodic feature is united with the own
-// voxel it copies, when both are nonzero (the reference pairs labels without
-// comparing values, skipping zeros).
-struct Twins {
-    long long s0, s1, s2;
-    int periodic[3];
-    int own_lo[3], own_len[3];
-};
-
+// Seam twins of the voxel labelling (see Twins).
 template <typename T>
 __global__ void k_cc_twins(const T *__restrict__ img, int *P, Twins W, int *err)
 {
@@ -429,13 +355,6 @@ __global__ void k_label_out(const int *__restrict__ P, const int *__restrict__ R
 }
 
 // ---- seam pairs for the reference's periodic numbering --------------------
-struct Box {
-    long long lo[3], hi[3];
-    __host__ __device__ long long size() const
-    {
-        return (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
-    }
-};
 
 // keys[r] = label(own/neighbour voxel r) << 32 | label(twin), rows in the
 // reference's order: own slab then neighbour slab of the feature, each
@@ -565,25 +484,6 @@ static int ensure_tables()
     if (dev >= 0 && dev < 64)
         g_tables_ready[dev] = true;
     return PMG_OK;
-}
-
-static Twins make_twins(const int64_t *shape, const int32_t *bc, const int32_t *pad)
-{
-    Twins W;
-    W.s0 = shape[0];
-    W.s1 = shape[1];
-    W.s2 = shape[2];
-    for (int d = 0; d < 3; d++) {
-        W.periodic[d] = bc[2 * d] == PMG_BC_PERIODIC;
-        W.own_lo[d] = pad[2 * d];
-        W.own_len[d] = (int)(shape[d] - pad[2 * d] - pad[2 * d + 1]);
-    }
-    return W;
-}
-
-static bool any_periodic(const int32_t *bc)
-{
-    return bc[0] == PMG_BC_PERIODIC || bc[2] == PMG_BC_PERIODIC || bc[4] == PMG_BC_PERIODIC;
 }
 
 // Union-find of a volume into P (roots = smallest index); twins optional.

@@ -52,27 +52,59 @@ __global__ void k_constrain(uint8_t *res, const uint8_t *__restrict__ nconn, lon
         res[i] = (res[i] == 1 && nconn[i] == 1) ? 1 : 0;
 }
 
-// mp = (morph == 1 && w == 2) ? 1 : mp; reservoir slabs -> 1.  One warp per
-// (i, j) row, lanes along k.
-__global__ void k_drain_update(uint8_t *mp, const uint8_t *__restrict__ morph, const uint8_t *__restrict__ w,
-                               long long s0, long long s1, long long s2, Boxes B)
+// mp = (morph == 1 && w == 2) ? 1 : mp, reservoir slabs -> 1
+// (equilibrium_distribution.py:133-179, subdomain_padded.py:285-307), fused
+// with the saturation count: the updated value is counted when it equals 2
+// inside the own box (count(own == 2), multiphase.py:56-96).  One warp per
+// (i, j) row.  Lanes take two voxels per load when rows start on
+// even addresses.
+__global__ void k_drain_update_count(uint8_t *mp, const uint8_t *__restrict__ morph, const uint8_t *__restrict__ w,
+                                     long long s0, long long s1, long long s2, Boxes B, unsigned long long *cnt)
 {
     const long long rows = s0 * s1;
     const int lane = threadIdx.x & 31;
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned int c = 0;
+    const bool pairs = (s2 & 1) == 0;
     for (long long r = warp; r < rows; r += nwarps) {
         const long long i = r / s1, j = r - (r / s1) * s1;
         const bool row_res = (i < B.rpad[0]) || (i >= s0 - B.rpad[1]) || (j < B.rpad[2]) || (j >= s1 - B.rpad[3]);
+        const bool row_own = i >= B.own[0] && i < B.own[1] && j >= B.own[2] && j < B.own[3];
         const long long base = r * s2;
-        for (long long k = lane; k < s2; k += 32) {
-            const long long idx = base + k;
-            uint8_t v = (morph[idx] == 1 && w[idx] == 2) ? (uint8_t)1 : mp[idx];
-            if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
-                v = 1;
-            mp[idx] = v;
+        if (pairs) {
+            const uint16_t *m2 = (const uint16_t *)(morph + base), *w2 = (const uint16_t *)(w + base);
+            uint16_t *p2 = (uint16_t *)(mp + base);
+            for (long long h = lane; h < (s2 >> 1); h += 32) {
+                const uint16_t mv = m2[h], wv = w2[h], pv = p2[h];
+                uint16_t o = 0;
+#pragma unroll
+                for (int b = 0; b < 2; b++) {
+                    const long long k = 2 * h + b;
+                    const uint8_t mb = (uint8_t)(mv >> (8 * b)), wb = (uint8_t)(wv >> (8 * b));
+                    uint8_t v = (mb == 1 && wb == 2) ? (uint8_t)1 : (uint8_t)(pv >> (8 * b));
+                    if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
+                        v = 1;
+                    c += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
+                    o |= (uint16_t)v << (8 * b);
+                }
+                p2[h] = o;
+            }
+        } else {
+            for (long long k = lane; k < s2; k += 32) {
+                const long long idx = base + k;
+                uint8_t v = (morph[idx] == 1 && w[idx] == 2) ? (uint8_t)1 : mp[idx];
+                if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
+                    v = 1;
+                c += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
+                mp[idx] = v;
+            }
         }
     }
+    for (int o = 16; o > 0; o >>= 1)
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    if (lane == 0 && c)
+        atomicAdd(cnt, (unsigned long long)c);
 }
 
 // Erosion by thresholding a precomputed squared EDT (subtraction's
@@ -439,13 +471,12 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         if (s != PMG_OK)
             break;
         {
-            const int ps__ = prof_begin("k_drain_update", st);
-            k_drain_update<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(mp_img, morph, wet, shape[0], shape[1],
-                                                                    shape[2], Bx);
+            const int ps__ = prof_begin("k_drain_update_count", st);
+            k_drain_update_count<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
+                mp_img, morph, wet, shape[0], shape[1], shape[2], Bx, d_counts + k);
             prof_end(ps__, (double)n * 4, st);
         }
         PMG_CHECK_LAUNCH();
-        s = count_eq_async(mp_img, shape, Bx.own, 2, d_counts + k, st);
     }
     if (s == PMG_OK && n_radii > 0) {
         std::vector<unsigned long long> h((size_t)n_radii);

@@ -113,17 +113,6 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
         }
     }
     const long long total = (long long)X[0] * X[1] * X[2];
-    // last int of B: "the image holds a value above 1" (erosion only; the
-    // capped pipeline needs a binary image)
-    int *flag = dilate ? nullptr : (int *)(B + total) - 1;
-    if (flag)
-        PMG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    {
-        const int ps__ = prof_begin("k_extend", st);
-        k_extend<<<grid_for(X[0] * X[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, dilate, flag);
-        prof_end(ps__, (double)total * 2, st);
-    }
-    PMG_CHECK_LAUNCH();
 
     pmg_axis_cfg plain = {0, 0, 0, 0, 1, 0, 0, 0};
     MorphEpi me{};
@@ -163,7 +152,24 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
             T = t;
     }
 
-    if (T != INT_MIN && cap_path_ok(res, X, T)) {
+    const bool cap = T != INT_MIN && cap_path_ok(res, X, T);
+    const bool any_per = G.ax[0].periodic || G.ax[1].periodic || G.ax[2].periodic;
+    if (cap && dilate && !any_per) // the row pass reads the image itself
+        return morph_cap_run(img, (uint16_t *)A, (uint16_t *)B, X, T, me, st, 1);
+
+    // last int of B: "the image holds a value above 1" (erosion only; the
+    // capped pipeline needs a binary image)
+    int *flag = dilate ? nullptr : (int *)(B + total) - 1;
+    if (flag)
+        PMG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    {
+        const int ps__ = prof_begin("k_extend", st);
+        k_extend<<<grid_for(X[0] * X[1] * 32, 256, 152LL * 64), 256, 0, st>>>(img, E, G, dilate, flag);
+        prof_end(ps__, (double)total * 2, st);
+    }
+    PMG_CHECK_LAUNCH();
+
+    if (cap) {
         int nonbin = 0;
         if (flag) {
             PMG_CUDA(cudaMemcpyAsync(&nonbin, flag, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -39,8 +39,18 @@ struct CapGeo {
 };
 
 // ---- pass A: rows -------------------------------------------------------------
+// raw == 0: E is the (extended) image whose zeros are the seeds.  raw == 1:
+// E is the unextended image of a dilation without periodic axes, read
+// directly -- the seeds are its nonzero voxels off the wall planes (the
+// logical_not of k_extend's image), so no extended copy is written.
+struct RowSrc {
+    int raw;
+    int X1;
+    int wall[6];
+};
+
 __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E, uint16_t *__restrict__ KA,
-                                                  long long rows, int X2, int T)
+                                                  long long rows, int X2, int T, RowSrc rs)
 {
     extern __shared__ uint16_t s_dq[];
     const unsigned FULL = 0xffffffffu;
@@ -55,9 +65,20 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
     const int none = 1 << 20;
     for (long long r = warp; r < rows; r += nwarps) {
         const uint8_t *src = E + r * X2;
+        if (rs.raw) {
+            const long long i = r / rs.X1, j = r - (r / rs.X1) * rs.X1;
+            const bool wrow = (rs.wall[0] && i == 0) || (rs.wall[1] && i == rows / rs.X1 - 1) ||
+                              (rs.wall[2] && j == 0) || (rs.wall[3] && j == rs.X1 - 1);
 #pragma unroll 4
-        for (int x = lane; x < X2; x += 32)
-            sb[x] = src[x];
+            for (int x = lane; x < X2; x += 32) {
+                const bool wall = wrow || (rs.wall[4] && x == 0) || (rs.wall[5] && x == X2 - 1);
+                sb[x] = (!wall && src[x] != 0) ? 0 : 1;
+            }
+        } else {
+#pragma unroll 4
+            for (int x = lane; x < X2; x += 32)
+                sb[x] = src[x];
+        }
         __syncwarp();
         // backward: distance to the next zero at or after x (65535: none)
         int nextz = none;
@@ -299,8 +320,13 @@ bool cap_path_ok(const float *res, const int64_t *X, int T)
 }
 
 int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
-                  cudaStream_t st)
+                  cudaStream_t st, int raw_dilate)
 {
+    RowSrc rs{};
+    rs.raw = raw_dilate;
+    rs.X1 = (int)X[1];
+    for (int q = 0; q < 6; q++)
+        rs.wall[q] = me.wall[q];
     int W = 0;
     while ((W + 1) * (W + 1) <= T)
         W++;
@@ -320,7 +346,7 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
         if (smem > 48 * 1024)
             PMG_CUDA(cudaFuncSetAttribute(k_cap_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         const int ps__ = prof_begin("k_cap_rows", st);
-        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T);
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, rs);
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();
@@ -365,7 +391,7 @@ int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, cons
         if (smem > 48 * 1024)
             PMG_CUDA(cudaFuncSetAttribute(k_cap_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         const int ps__ = prof_begin("k_cap_rows", st);
-        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T);
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, RowSrc{});
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();
