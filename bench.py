@@ -345,6 +345,108 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def grf_medium(n, sigma=4.0, porosity=0.35, seed=7):
+    """Gaussian random field medium of the large EDT + CC configuration: seeded
+    white noise N(0, 1), filtered by a periodic Gaussian of sigma voxels in
+    Fourier space, pore (1) where the field is at or below its 35th
+    percentile; n^3 uint8 on the device."""
+    import math
+
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    field = torch.randn((n, n, n), device="cuda", generator=g)
+    F = torch.fft.rfftn(field)
+    del field
+    k = torch.fft.fftfreq(n, device="cuda")
+    kz = torch.fft.rfftfreq(n, device="cuda")
+    F *= torch.exp(-2.0 * math.pi ** 2 * sigma ** 2 * (k[:, None, None] ** 2 + k[None, :, None] ** 2))
+    F *= torch.exp(-2.0 * math.pi ** 2 * sigma ** 2 * kz[None, None, :] ** 2)
+    field = torch.fft.irfftn(F, s=(n, n, n))
+    del F
+    flat = field.reshape(-1)
+    q = torch.kthvalue(flat, max(1, int(round(porosity * flat.numel())))).values
+    return (field <= q).to(torch.uint8)
+
+
+def batch_packs(count, seed=99):
+    """The batched configuration's packs: per-axis sizes drawn from {64, 96,
+    ..., 256}, box N_i / 256 (voxel size 2^-8), porosity target U[0.3, 0.5],
+    sphere radii U[0.02, 0.06], sphere count -ln(phi) V / (4/3 pi E[r^3]);
+    returns [(voxels, spheres)]."""
+    rng = np.random.default_rng(seed)
+    sizes = np.arange(64, 257, 32)
+    er3 = (0.06 ** 4 - 0.02 ** 4) / (4 * 0.04)
+    packs = []
+    for _ in range(count):
+        vox = tuple(int(v) for v in rng.choice(sizes, 3))
+        box = [v / 256.0 for v in vox]
+        vol = box[0] * box[1] * box[2]
+        phi = rng.uniform(0.3, 0.5)
+        n = max(1, int(round(-np.log(phi) * vol / (4.0 / 3.0 * np.pi * er3))))
+        sph = np.empty((n, 4))
+        for d in range(3):
+            sph[:, d] = rng.random(n) * box[d]
+        sph[:, 3] = rng.uniform(0.02, 0.06, n)
+        packs.append((vox, sph))
+    return packs
+
+
+def run_batch(args):
+    """Batched configuration: EDT + connected components + 24-radius drainage
+    for every pack, packs spread over CUDA streams (pmmoto_gb300.batch)."""
+    import torch
+
+    import pmmoto_gb300 as P
+    from pmmoto_gb300 import _lib, batch
+    from pmmoto_gb300.filters import connected_components as CC
+    from pmmoto_gb300.filters import equilibrium_distribution as ED
+
+    L = _lib.lib()
+    L.pmg_launch_count.restype = ctypes.c_longlong
+    packs = batch_packs(args.packs)
+    media = []
+    for vox, sph in packs:
+        kw = geom_kwargs()
+        kw["box"] = tuple((0.0, v / 256.0) for v in vox)
+        sd = P.initialize(vox, **kw)
+        pm = P.domain_generation.gen_pm_spheres_domain(sd, torch.as_tensor(sph, device="cuda"))
+        media.append((sd, pm))
+    r_vox = np.linspace(1, 12, 24)
+    pcs = sorted(list(2.0 / (r_vox * 2.0 ** -8)))
+    torch.cuda.synchronize()
+
+    def one(item):
+        sd, pm = item
+        medium = P.domain_generation.PorousMedia(sd, pm.img)
+        _ = medium.max_distance  # EDT of the pore space + halo update, as drainage needs it
+        labels, nlab = CC.connect_components(pm.img, sd)
+        mp = P.domain_generation.gen_mp_constant(medium, 2)
+        sat = ED.drainage(mp, pcs, mode="distance")
+        return float(sat[-1]), int(nlab)
+
+    for _ in range(args.warmup):
+        batch.map_streams(one, media, workers=args.workers)
+    torch.cuda.synchronize()
+    n0 = L.pmg_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    t0 = time.time()
+    for _ in range(args.steps):
+        res = batch.map_streams(one, media, workers=args.workers)
+    e1.record()
+    torch.cuda.synchronize()
+    wall = (time.time() - t0) / args.steps
+    launches = (L.pmg_launch_count() - n0) // args.steps
+    vox = sum(int(np.prod([v + 2 for v in p[0]])) for p in packs)
+    print(json.dumps({"case": "batch", "packs": len(packs), "workers": args.workers,
+                      "metric": "batched packs/s (EDT + CC + 24-radius drainage per pack)",
+                      "value": len(packs) / wall, "unit": "packs/s", "ms_per_batch": wall * 1e3,
+                      "gpu_ms_per_batch": e0.elapsed_time(e1) / args.steps, "voxels": vox,
+                      "gpu_launches_per_batch": launches, "final_saturation_sample": res[0][0]}), flush=True)
+
+
 def run_case(args):
     """Single-operator cases on a seeded random medium (for ncu captures and
     per-operator rates): 'edt' = edt3d, 'cc' = connected components (with the
@@ -361,9 +463,12 @@ def run_case(args):
     from pmmoto_gb300.core.geometry import geo_of
 
     n = args.n
-    g = torch.Generator(device="cuda")
-    g.manual_seed(7)
-    img = (torch.rand((n, n, n), device="cuda", generator=g) >= 0.35).to(torch.uint8)
+    if args.medium == "grf":
+        img = grf_medium(n)
+    else:
+        g = torch.Generator(device="cuda")
+        g.manual_seed(7)
+        img = (torch.rand((n, n, n), device="cuda", generator=g) >= 0.35).to(torch.uint8)
     per = args.bc == "periodic"
     # voxel size 1/512 (a power of two, like the drainage pack)
     sd = P.initialize((n - 2,) * 3, box=((0.0, (n - 2) / 512.0),) * 3, boundary_types=((args.bc, args.bc),) * 3)
@@ -408,7 +513,7 @@ def run_case(args):
     ms = e0.elapsed_time(e1) / args.steps
     prof = prof_read(L)
     peak, _ = load_peaks()
-    print(json.dumps({"case": args.case, "bc": args.bc, "n": n, "ms": ms, "gvox_s": n**3 / ms / 1e6,
+    print(json.dumps({"case": args.case, "bc": args.bc, "medium": args.medium, "n": n, "ms": ms, "gvox_s": n**3 / ms / 1e6,
                       "kernels": {k: {"ms_per_step": v["ms"] / args.steps, "launches": v["launches"],
                                       "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] else None,
                                       "frac": v["bytes"] / (v["ms"] / 1e3) / 1e9 / peak if v["ms"] else None}
@@ -422,12 +527,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
-    ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph", "select"])
+    ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph", "select", "batch"])
+    ap.add_argument("--packs", type=int, default=256, help="packs of the batched case")
+    ap.add_argument("--workers", type=int, default=8, help="host threads / CUDA streams of the batched case")
     ap.add_argument("--n", type=int, default=512, help="volume side of the single-operator cases")
     ap.add_argument("--bc", default="periodic", choices=["periodic", "wall"],
                     help="boundary type of every face in the single-operator cases")
+    ap.add_argument("--medium", default="random", choices=["random", "grf"],
+                    help="single-operator cases: uniform random (65%% pore) or the Gaussian random field "
+                         "(sigma 4 voxels, porosity 0.35) of the large EDT + CC configuration")
     args = ap.parse_args()
-    if args.case != "drainage":
+    if args.case == "batch":
+        run_batch(args)
+    elif args.case != "drainage":
         run_case(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -985,9 +985,6 @@ __device__ __forceinline__ unsigned bmask_of(int q, uint64_t mlo, uint64_t mhi)
     return (unsigned)((q < 8 ? mlo >> (8 * q) : mhi >> (8 * (q - 8))) & 0xffu);
 }
 
-// Neighbours in `conn` connected to those in `q_mask` through chains of
-// touching neighbours: a union with one of them links all of them, because
-// the union of each touching pair is done by the later block of the pair.
 struct BTabs {
     unsigned short adj[13];
     uint8_t pair[13][13];
@@ -1001,25 +998,47 @@ __device__ __forceinline__ void load_btabs(BTabs &tb)
         tb.pair[q / 13][q % 13] = c_bt_pair[q / 13][q % 13];
 }
 
-__device__ __forceinline__ unsigned bcover(unsigned q_mask, unsigned conn, uint64_t mlo, uint64_t mhi,
-                                           const BTabs &tb)
+// Neighbours in `conn` that touch neighbour w (one step), w included: a union
+// with w links them too, because the union of each touching pair is done by
+// the later block of the pair.
+__device__ __forceinline__ unsigned bcover1(int w, unsigned conn, uint64_t mlo, uint64_t mhi, const BTabs &tb)
 {
-    unsigned grp = q_mask, frontier = q_mask;
-    while (frontier) {
-        const int w = __ffs(frontier) - 1;
-        frontier &= frontier - 1;
-        const unsigned mw = bmask_of(w, mlo, mhi);
-        unsigned cand = tb.adj[w] & conn & ~grp;
-        while (cand) {
-            const int u = __ffs(cand) - 1;
-            cand &= cand - 1;
-            if ((mw & tb.pair[w][u]) && (bmask_of(u, mlo, mhi) & tb.pair[u][w])) {
-                grp |= 1u << u;
-                frontier |= 1u << u;
-            }
-        }
+    unsigned grp = 1u << w;
+    const unsigned mw = bmask_of(w, mlo, mhi);
+    unsigned cand = tb.adj[w] & conn;
+    while (cand) {
+        const int u = __ffs(cand) - 1;
+        cand &= cand - 1;
+        if ((mw & tb.pair[w][u]) && (bmask_of(u, mlo, mhi) & tb.pair[u][w]))
+            grp |= 1u << u;
     }
     return grp;
+}
+
+// Everything in `conn` connected to neighbour w through chains of touching
+// neighbours (the closure of bcover1): worth its cost where a union is a
+// global-memory atomic.
+__device__ __forceinline__ unsigned bcover(int w, unsigned conn, uint64_t mlo, uint64_t mhi, const BTabs &tb)
+{
+    unsigned grp = 1u << w, frontier = 1u << w;
+    while (frontier) {
+        const int v = __ffs(frontier) - 1;
+        frontier &= frontier - 1;
+        const unsigned add = bcover1(v, conn & ~grp, mlo, mhi, tb) & ~grp;
+        grp |= add;
+        frontier |= add;
+    }
+    return grp;
+}
+
+// Neighbour (-1, 0, 0) (index 4 in c_nb order) is 26-adjacent to all twelve
+// other earlier neighbours, so it is taken first: in a dense region one union
+// with it covers every other one.
+constexpr int kCentre = 4;
+
+__device__ __forceinline__ int next_cover(unsigned rest)
+{
+    return ((rest >> kCentre) & 1u) ? kCentre : __ffs(rest) - 1;
 }
 
 // Foreground of the block selection: the voxels of one value (or nonzero)
@@ -1103,9 +1122,10 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(Src src, int *__restrict__ P
         }
         unsigned covered = 0;
         while (conn & ~covered) {
-            const int q = __ffs(conn & ~covered) - 1;
+            const unsigned rest = conn & ~covered;
+            const int q = next_cover(rest);
             sunite(L, t, ((a + c_nb[q][0]) * kT1 + b + c_nb[q][1]) * kT2 + c + c_nb[q][2]);
-            covered |= bcover(1u << q, conn, mlo, mhi, tb);
+            covered |= bcover1(q, rest, mlo, mhi, tb);
         }
     }
     __syncthreads();
@@ -1165,18 +1185,18 @@ __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int 
             if (aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2)
                 local |= 1u << q;
         }
+        // in-tile neighbours were united in phase 1, and so was everything
+        // touching them
         unsigned covered = 0;
-        unsigned lm = local;
-        while (lm) {
-            const int q = __ffs(lm) - 1;
-            const unsigned grp = bcover(1u << q, conn, mlo, mhi, tb);
-            covered |= grp;
-            lm &= ~grp;
+        while (local & ~covered) {
+            const int q = next_cover(local & ~covered);
+            covered |= bcover(q, conn & ~covered, mlo, mhi, tb);
         }
         while (conn & ~covered) {
-            const int q = __ffs(conn & ~covered) - 1;
+            const unsigned rest = conn & ~covered;
+            const int q = next_cover(rest);
             unite(P, bi, ((c0 + c_nb[q][0]) * G.b1 + c1 + c_nb[q][1]) * G.b2 + c2 + c_nb[q][2], err);
-            covered |= bcover(1u << q, conn, mlo, mhi, tb);
+            covered |= bcover(q, rest, mlo, mhi, tb);
         }
     }
 }

@@ -98,11 +98,12 @@ def test_cc_many_tiles_vs_oracle(C, kinds):
 
 
 @pytest.mark.parametrize("kinds", [("end", "wall", "wall"), ("end", "periodic", "periodic"), ("end", "end", "periodic")])
-@pytest.mark.parametrize("vox", [(33, 27, 41), (21, 37, 141)])
+@pytest.mark.parametrize("vox", [(33, 27, 41), (21, 37, 141), (5, 6, 2200)])
 def test_binary_block_selection_vs_oracle(C, kinds, vox):
     """The 2x2x2-block selection (phase filter, or the binary flag) equals the
     voxel-level selection of the reference, odd sizes included; the second
-    shape spans several 8 x 16 x 64-voxel tiles on every axis."""
+    shape spans several 8 x 16 x 64-voxel tiles on every axis, the third has
+    rows longer than 2048 voxels."""
     import torch
     from pmmoto_gb300.core import initialize
     from pmmoto_gb300.core.geometry import geo_of
