@@ -22,6 +22,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <climits>
 #include <array>
 #include <unordered_map>
 #include <unordered_set>
@@ -908,6 +909,9 @@ static int check_vol(const int64_t *shape)
     return PMG_OK;
 }
 
+int cc_label_u8(const uint8_t *img, uint64_t *labels, const int64_t *shape, const int32_t *bc, const int32_t *pad,
+                int64_t *count, cudaStream_t st);
+
 } // namespace pmg
 
 using namespace pmg;
@@ -925,7 +929,7 @@ extern "C" int pmg_cc_label(const void *img, int32_t elem_bytes, uint64_t *label
     cudaStream_t st = as_stream(stream);
     switch (elem_bytes) {
     case 1:
-        return cc_label_t((const uint8_t *)img, labels, shape, bc, pad, count, st);
+        return cc_label_u8((const uint8_t *)img, labels, shape, bc, pad, count, st);
     case 2:
         return cc_label_t((const uint16_t *)img, labels, shape, bc, pad, count, st);
     case 4:
@@ -1350,13 +1354,8 @@ __global__ void k_bcc_select(const uint8_t *__restrict__ M, const int *__restric
 __host__ __device__ inline const uint8_t *src_elem(const SrcImg &s) { return s.img; }
 __host__ __device__ inline const uint16_t *src_elem(const SrcErode &s) { return s.E; }
 
-template <class Src>
-static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
-                           const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
-                           int val, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+static BGrid bgrid_of(const int64_t *shape)
 {
-    PMG_TRY(ensure_tables());
-    PMG_TRY(ensure_block_tables());
     BGrid G;
     G.s0 = (int)shape[0];
     G.s1 = (int)shape[1];
@@ -1364,9 +1363,21 @@ static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64
     G.b0 = (G.s0 + 1) / 2;
     G.b1 = (G.s1 + 1) / 2;
     G.b2 = (G.s2 + 1) / 2;
+    return G;
+}
+
+// Block union-find of the source: tiles, cross-tile unions, periodic seams
+// (twins), flattening.  P[b] = root block (the smallest block index of the
+// component), -1 for empty blocks; M[b] = block mask.
+template <class Src>
+static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, const int32_t *pad, bool twins,
+                     int *P, uint8_t *M, int *err, cudaStream_t st)
+{
+    PMG_TRY(ensure_tables());
+    PMG_TRY(ensure_block_tables());
+    const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
     const long long n = shape[0] * shape[1] * shape[2];
-    PMG_CUDA(cudaMemsetAsync(mark, 0, ((size_t)nb + 3) & ~(size_t)3, st));
     {
         const int nt = ((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
         const int ps__ = prof_begin("k_bcc_tile", st);
@@ -1380,7 +1391,7 @@ static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64
         prof_end(ps__, 0.0, st);
     }
     PMG_CHECK_LAUNCH();
-    if (any_periodic(bc)) {
+    if (twins && any_periodic(bc)) {
         const int ps__ = prof_begin("k_bcc_twins", st);
         k_bcc_twins<<<grid_for(n, 256, 152LL * 32), 256, 0, st>>>(M, P, G, make_twins(shape, bc, pad), err);
         prof_end(ps__, 0.0, st);
@@ -1392,6 +1403,19 @@ static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64
         prof_end(ps__, (double)nb * 8, st);
     }
     PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+template <class Src>
+static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
+                           const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
+                           int val, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+{
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    PMG_CUDA(cudaMemsetAsync(mark, 0, ((size_t)nb + 3) & ~(size_t)3, st));
+    PMG_TRY(bcc_build(src, shape, bc, pad, true, P, M, err, st));
     const int64_t *boxes[2] = {inlet_box, outlet_box};
     for (int w = 0; w < 2; w++) {
         const int64_t *bxp = boxes[w];
@@ -1454,6 +1478,235 @@ int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, 
     for (int q = 0; q < 6; q++)
         src.wall[q] = bc[q] == PMG_BC_WALL;
     return bcc_select_core(src, out, 1, shape, bc, pad, inlet_box, outlet_box, mode, 1, P, M, mark, err, st);
+}
+
+// ---- binary labelling on blocks -----------------------------------------------
+// connect_components (connected_components.py:32-62; cc3d numbers components
+// 1..N in the order of their first voxel in C order) for an image with a
+// single nonzero value: the block union-find gives the components, and the
+// first voxel of each one is found and ranked without a per-voxel parent
+// array.  The first voxel of a block is its lowest set mask bit (bit order
+// x, y, z follows C order); the first voxel of a component lies in the
+// component's first block plane (the plane of its root, the smallest block
+// index), so only blocks of that plane compete for it.
+
+__global__ void k_nz_range(const uint8_t *__restrict__ img, long long n, unsigned *lohi)
+{
+    unsigned lo = 255, hi = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned v = img[i];
+        if (v) {
+            lo = min(lo, v);
+            hi = max(hi, v);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_down_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_down_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(lohi, lo);
+        atomicMax(lohi + 1, hi);
+    }
+}
+
+__global__ void k_fill_i32(int *a, long long n, int v)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+
+__device__ __forceinline__ int block_first_voxel(const BGrid &G, int b, unsigned m)
+{
+    const int c2 = b % G.b2, c1 = (b / G.b2) % G.b1, c0 = b / (G.b2 * G.b1);
+    const int bit = __ffs(m) - 1;
+    const int x = bit >> 2, y = (bit >> 1) & 1, z = bit & 1;
+    return ((2 * c0 + x) * G.s1 + 2 * c1 + y) * G.s2 + 2 * c2 + z;
+}
+
+// F[root] = first voxel of the component
+__global__ void k_blk_first(const int *__restrict__ P, const uint8_t *__restrict__ M, BGrid G, int *F)
+{
+    const int nb = G.b0 * G.b1 * G.b2;
+    const int plane = G.b1 * G.b2;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const unsigned m = M[b];
+        if (!m)
+            continue;
+        const int r = P[b];
+        if (r < 0 || b / plane != r / plane)
+            continue;
+        const int f = block_first_voxel(G, b, m);
+        if (f < F[r])
+            atomicMin(F + r, f);
+    }
+}
+
+// bit f of `bits` set for every component's first voxel f
+__global__ void k_blk_first_bits(const int *__restrict__ P, const uint8_t *__restrict__ M, const int *__restrict__ F,
+                                 int nb, unsigned *bits)
+{
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
+        if (M[b] && P[b] == b) {
+            const int f = F[b];
+            atomicOr(bits + (f >> 5), 1u << (f & 31));
+        }
+}
+
+// set bits per tile of 32 words (1024 voxels)
+__global__ void k_bits_count(const unsigned *__restrict__ bits, long long nwords, int *cnt)
+{
+    const long long ntiles = (nwords + 31) / 32;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntiles;
+         t += (long long)gridDim.x * blockDim.x) {
+        int c = 0;
+        const long long w1 = min(nwords, 32 * t + 32);
+        for (long long w = 32 * t; w < w1; w++)
+            c += __popc(bits[w]);
+        cnt[t] = c;
+    }
+}
+
+// root blocks: F[root] <- 1 + rank of its first voxel among all first voxels
+__global__ void k_root_label(const int *__restrict__ P, const uint8_t *__restrict__ M, int *F, int nb,
+                             const unsigned *__restrict__ bits, const int *__restrict__ offs)
+{
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        if (!M[b] || P[b] != b)
+            continue;
+        const int f = F[b];
+        const int w = f >> 5;
+        int r = offs[f >> 10] + __popc(bits[w] & ((1u << (f & 31)) - 1u));
+        for (int u = (f >> 10) * 32; u < w; u++)
+            r += __popc(bits[u]);
+        F[b] = r + 1;
+    }
+}
+
+// labels of every voxel: a block's label on its foreground voxels, 0 elsewhere
+__global__ void k_blk_label_out(const int *__restrict__ P, const uint8_t *__restrict__ M, const int *__restrict__ F,
+                                BGrid G, uint64_t *__restrict__ labels)
+{
+    const int nb = G.b0 * G.b1 * G.b2;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int r = b / G.b2;
+        const int c2 = b - r * G.b2;
+        const int c0 = r / G.b1;
+        const int c1 = r - c0 * G.b1;
+        const unsigned m = M[b];
+        const uint64_t lab = m ? (uint64_t)F[P[b]] : 0;
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int y = 0; y < 2; y++) {
+                const int i = 2 * c0 + x, j = 2 * c1 + y;
+                if (i >= G.s0 || j >= G.s1)
+                    continue;
+                uint64_t *row = labels + ((long long)i * G.s1 + j) * G.s2;
+#pragma unroll
+                for (int z = 0; z < 2; z++) {
+                    const int k = 2 * c2 + z;
+                    if (k < G.s2)
+                        row[k] = ((m >> ((x * 2 + y) * 2 + z)) & 1u) ? lab : 0;
+                }
+            }
+    }
+}
+
+// 1: the image holds one nonzero value (or none), so blocks can label it
+static int single_value(const uint8_t *img, long long n, int *yes, cudaStream_t st)
+{
+    unsigned *lohi = nullptr;
+    PMG_TRY(scratch_alloc((void **)&lohi, 2 * sizeof(unsigned), st));
+    const unsigned init[2] = {255u, 0u};
+    PMG_CUDA(cudaMemcpyAsync(lohi, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    {
+        const int ps__ = prof_begin("k_nz_range", st);
+        k_nz_range<<<grid_for(n, 256, 152LL * 16), 256, 0, st>>>(img, n, lohi);
+        prof_end(ps__, (double)n, st);
+    }
+    PMG_CHECK_LAUNCH();
+    unsigned h[2] = {0, 0};
+    PMG_CUDA(cudaMemcpyAsync(h, lohi, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PMG_CUDA(cudaStreamSynchronize(st));
+    PMG_TRY(scratch_free(lohi, st));
+    *yes = h[1] == 0 || h[0] == h[1];
+    return PMG_OK;
+}
+
+int cc_label_blocks(const uint8_t *img, uint64_t *labels, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, int64_t *count, cudaStream_t st)
+{
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    const long long nwords = (n + 31) / 32, ntiles = (nwords + 31) / 32;
+    int *P = nullptr, *F = nullptr, *err = nullptr, *cnt = nullptr, *offs = nullptr;
+    uint8_t *M = nullptr;
+    unsigned *bits = nullptr;
+    PMG_TRY(scratch_alloc((void **)&P, (size_t)nb * 4, st));
+    PMG_TRY(scratch_alloc((void **)&F, (size_t)nb * 4, st));
+    PMG_TRY(scratch_alloc((void **)&M, (size_t)nb, st));
+    PMG_TRY(scratch_alloc((void **)&err, sizeof(int), st));
+    PMG_TRY(scratch_alloc((void **)&bits, (size_t)nwords * 4, st));
+    PMG_TRY(scratch_alloc((void **)&cnt, (size_t)ntiles * 4 + 4, st));
+    PMG_TRY(scratch_alloc((void **)&offs, (size_t)ntiles * 4 + 4, st));
+    PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    PMG_CUDA(cudaMemsetAsync(bits, 0, (size_t)nwords * 4, st));
+    SrcImg src{img, -1};
+    PMG_TRY(bcc_build(src, shape, bc, pad, false, P, M, err, st));
+    {
+        const int ps__ = prof_begin("k_blk_first", st);
+        k_fill_i32<<<grid_for(nb, 256, 152LL * 32), 256, 0, st>>>(F, nb, INT_MAX);
+        k_blk_first<<<grid_for(nb, 256, 152LL * 32), 256, 0, st>>>(P, M, G, F);
+        k_blk_first_bits<<<grid_for(nb, 256, 152LL * 32), 256, 0, st>>>(P, M, F, nb, bits);
+        k_bits_count<<<grid_for(ntiles, 256, 152LL * 32), 256, 0, st>>>(bits, nwords, cnt);
+        prof_end(ps__, (double)nb * 13, st);
+    }
+    PMG_CHECK_LAUNCH();
+    size_t tb = 0;
+    PMG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, offs, (int)ntiles + 1, st));
+    void *tmp = nullptr;
+    PMG_TRY(scratch_alloc(&tmp, tb, st));
+    PMG_CUDA(cudaMemsetAsync(cnt + ntiles, 0, 4, st));
+    PMG_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, offs, (int)ntiles + 1, st));
+    {
+        const int ps__ = prof_begin("k_blk_label_out", st);
+        k_root_label<<<grid_for(nb, 256, 152LL * 32), 256, 0, st>>>(P, M, F, nb, bits, offs);
+        k_blk_label_out<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(P, M, F, G, labels);
+        prof_end(ps__, (double)n * 8 + (double)nb * 9, st);
+    }
+    PMG_CHECK_LAUNCH();
+    int total = 0;
+    PMG_CUDA(cudaMemcpyAsync(&total, offs + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int s = read_err(err, st);
+    PMG_TRY(scratch_free(tmp, st));
+    PMG_TRY(scratch_free(P, st));
+    PMG_TRY(scratch_free(F, st));
+    PMG_TRY(scratch_free(M, st));
+    PMG_TRY(scratch_free(err, st));
+    PMG_TRY(scratch_free(bits, st));
+    PMG_TRY(scratch_free(cnt, st));
+    PMG_TRY(scratch_free(offs, st));
+    if (s != PMG_OK)
+        return s;
+    *count = total;
+    if (any_periodic(bc))
+        return periodic_renumber(labels, shape, bc, pad, total, count, st);
+    return PMG_OK;
+}
+
+int cc_label_u8(const uint8_t *img, uint64_t *labels, const int64_t *shape, const int32_t *bc, const int32_t *pad,
+                int64_t *count, cudaStream_t st)
+{
+    const long long n = shape[0] * shape[1] * shape[2];
+    int yes = 0;
+    PMG_TRY(single_value(img, n, &yes, st));
+    if (yes)
+        return cc_label_blocks(img, labels, shape, bc, pad, count, st);
+    return cc_label_t(img, labels, shape, bc, pad, count, st);
 }
 
 // Selection with caller-provided scratch: P (n int32), mark (n bytes rounded

@@ -60,7 +60,18 @@ def test_cc_random_vs_oracle(C, kinds):
         want, wn = O.connect_components(img, g)
         np.testing.assert_array_equal(lbl, want)
         assert n == wn
+        # one nonzero value other than 1 (block labelling) and several values
+        # (voxel labelling)
+        single = (3 * img).astype(np.uint8)
+        lbl, n = C.connect_components(single, sd)
+        want, wn = O.connect_components(single, g)
+        np.testing.assert_array_equal(lbl, want)
+        assert n == wn
         multi = O.update_buffer(g, rng.integers(0, 3, sd.voxels).astype(np.uint8))
+        lbl, n = C.connect_components(multi, sd)
+        want, wn = O.connect_components(multi, g)
+        np.testing.assert_array_equal(lbl, want)
+        assert n == wn
         for phase in (None, 1, 2):
             np.testing.assert_array_equal(C.inlet_connected_img(sd, multi, phase), O.inlet_connected_img(g, multi, phase))
             np.testing.assert_array_equal(C.outlet_connected_img(sd, multi, phase), O.outlet_connected_img(g, multi, phase))
