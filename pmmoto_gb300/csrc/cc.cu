@@ -1060,13 +1060,12 @@ struct SrcErode {
     const uint16_t *E;
     int T;
     int s0, s1, s2;
-    int wall[6];
+    unsigned walls; // bit q: face q (axis q / 2, low / high) is a wall
     __device__ __forceinline__ bool fg(long long idx, int i, int j, int k) const
     {
-        if ((wall[0] && i == 0) || (wall[1] && i == s0 - 1) || (wall[2] && j == 0) || (wall[3] && j == s1 - 1) ||
-            (wall[4] && k == 0) || (wall[5] && k == s2 - 1))
-            return false;
-        return (int)E[idx] > T;
+        const unsigned on = (i == 0) | ((i == s0 - 1) << 1) | ((j == 0) << 2) | ((j == s1 - 1) << 3) |
+                            ((k == 0) << 4) | ((k == s2 - 1) << 5);
+        return !(on & walls) && (int)E[idx] > T;
     }
 };
 
@@ -1075,7 +1074,7 @@ struct SrcErode {
 // tile whose roots are the smallest block index of each tile-local part.
 // Every later step reads the block masks M, never the source again.
 template <class Src>
-__global__ void __launch_bounds__(kTile) k_bcc_tile(Src src, int *__restrict__ P, uint8_t *__restrict__ M,
+__global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict__ P, uint8_t *__restrict__ M,
                                                    BGrid G)
 {
     __shared__ uint8_t sm[kTile];
@@ -1091,6 +1090,9 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(Src src, int *__restrict__ P
     const bool inside = c0 < G.b0 && c1 < G.b1 && c2 < G.b2;
     unsigned m = 0;
     if (inside) {
+        const long long sy = G.s2, sx = (long long)G.s1 * G.s2;
+        const long long base = (2LL * c0 * G.s1 + 2 * c1) * sy + 2 * c2;
+        const bool whole = 2 * c0 + 1 < G.s0 && 2 * c1 + 1 < G.s1 && 2 * c2 + 1 < G.s2;
 #pragma unroll
         for (int x = 0; x < 2; x++)
 #pragma unroll
@@ -1098,7 +1100,7 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(Src src, int *__restrict__ P
 #pragma unroll
                 for (int z = 0; z < 2; z++) {
                     const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2 + z;
-                    if (i < G.s0 && j < G.s1 && k < G.s2 && src.fg(((long long)i * G.s1 + j) * G.s2 + k, i, j, k))
+                    if ((whole || (i < G.s0 && j < G.s1 && k < G.s2)) && src.fg(base + x * sx + y * sy + z, i, j, k))
                         m |= 1u << ((x * 2 + y) * 2 + z);
                 }
     }
@@ -1108,6 +1110,7 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(Src src, int *__restrict__ P
     if (m) {
         unsigned conn = 0;
         uint64_t mlo = 0, mhi = 0;
+        bool full = m == 0xffu; // this block and every connected neighbour full
 #pragma unroll
         for (int q = 0; q < 13; q++) {
             const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
@@ -1118,13 +1121,16 @@ __global__ void __launch_bounds__(kTile) k_bcc_tile(Src src, int *__restrict__ P
             const unsigned mn = sm[(aa * kT1 + bb) * kT2 + cc];
             if (mn & c_bt_nb[q]) {
                 conn |= 1u << q;
+                full = full && mn == 0xffu;
                 if (q < 8)
                     mlo |= (uint64_t)mn << (8 * q);
                 else
                     mhi |= (uint64_t)mn << (8 * (q - 8));
             }
         }
-        unsigned covered = 0;
+        // dense fast path: full blocks touch whenever they are 26-adjacent, and
+        // the centre neighbour is adjacent to every other one
+        unsigned covered = (full && ((conn >> kCentre) & 1u)) ? conn & ~(1u << kCentre) : 0u;
         while (conn & ~covered) {
             const unsigned rest = conn & ~covered;
             const int q = next_cover(rest);
@@ -1170,6 +1176,7 @@ __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int 
             continue;
         unsigned conn = 0, local = 0;
         uint64_t mlo = 0, mhi = 0;
+        bool full = m == 0xffu;
 #pragma unroll
         for (int q = 0; q < 13; q++) {
             const int a0 = c0 + c_nb[q][0], a1 = c1 + c_nb[q][1], a2 = c2 + c_nb[q][2];
@@ -1181,6 +1188,7 @@ __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int 
             if (!(mn & c_bt_nb[q]))
                 continue;
             conn |= 1u << q;
+            full = full && mn == 0xffu;
             if (q < 8)
                 mlo |= (uint64_t)mn << (8 * q);
             else
@@ -1192,6 +1200,13 @@ __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int 
         // in-tile neighbours were united in phase 1, and so was everything
         // touching them
         unsigned covered = 0;
+        if (full && ((conn >> kCentre) & 1u)) {
+            // dense fast path (see k_bcc_tile): any in-tile neighbour already
+            // links all of them; otherwise the centre does
+            if (local)
+                continue;
+            covered = conn & ~(1u << kCentre);
+        }
         while (local & ~covered) {
             const int q = next_cover(local & ~covered);
             covered |= bcover(q, conn & ~covered, mlo, mhi, tb);
@@ -1475,8 +1490,9 @@ int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, 
     src.s0 = (int)shape[0];
     src.s1 = (int)shape[1];
     src.s2 = (int)shape[2];
+    src.walls = 0;
     for (int q = 0; q < 6; q++)
-        src.wall[q] = bc[q] == PMG_BC_WALL;
+        src.walls |= (bc[q] == PMG_BC_WALL ? 1u : 0u) << q;
     return bcc_select_core(src, out, 1, shape, bc, pad, inlet_box, outlet_box, mode, 1, P, M, mark, err, st);
 }
 

@@ -195,23 +195,29 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
         uint16_t *out = KB + base;
         CapLine<RING> L{ring + threadIdx.x, 0, -1, 0};
         int cur[kCapChunk];
+        const uint16_t *pin = in; // next height to prefetch
 #pragma unroll
-        for (int u = 0; u < kCapChunk; u++)
-            cur[u] = u < n ? (int)in[u * st] : big;
+        for (int u = 0; u < kCapChunk; u++) {
+            cur[u] = u < n ? (int)*pin : big;
+            pin += st;
+        }
+        uint16_t *po = out; // output position x = i - W
         for (int i0 = 0; i0 < n + W; i0 += kCapChunk) {
             int nxt[kCapChunk];
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++) {
-                const int ii = i0 + kCapChunk + u;
-                nxt[u] = ii < n ? (int)in[(long long)ii * st] : big;
+                nxt[u] = i0 + kCapChunk + u < n ? (int)*pin : big;
+                pin += st;
             }
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++) {
                 const int i = i0 + u;
                 const int v = L.step(i, cur[u], T, W, big);
                 const int x = i - W;
-                if (x >= 0 && x < n)
-                    out[(long long)x * st] = (uint16_t)v;
+                if (x >= 0 && x < n) {
+                    *po = (uint16_t)v;
+                    po += st;
+                }
             }
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++)
@@ -234,57 +240,66 @@ __device__ __forceinline__ int isqrt_small(int m)
 __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ KB, CapGeo G, int T, int W,
                                                   MorphEpi me)
 {
+    // half-width of the interval of every height K <= T: floor(sqrt(T - K))
+    __shared__ uint8_t s_w[kCapMaxT + 1];
+    for (int q = threadIdx.x; q <= T; q += blockDim.x)
+        s_w[q] = (uint8_t)isqrt_small(T - q);
+    __syncthreads();
     const long long nlines = (long long)G.nj * G.nk;
     const long long st = (long long)G.X1 * G.X2;
     const int n = G.X0;
+    // positions x of the line that lie in the unextended volume
+    const int xlo = max(0, me.e0), xhi = min(n, me.e0 + (int)me.o0);
     for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
          li += (long long)gridDim.x * blockDim.x) {
         const int x1 = G.j0 + (int)(li / G.nk);
         const int x2 = G.k0 + (int)(li - (li / G.nk) * G.nk);
         const uint16_t *in = KB + (long long)x1 * G.X2 + x2;
-        const long long io0 = -me.e0;
         const long long jo = x1 - me.e1, ko = x2 - me.e2;
         const bool wall_jk = (me.wall[2] && jo == 0) || (me.wall[3] && jo == me.o1 - 1) ||
                              (me.wall[4] && ko == 0) || (me.wall[5] && ko == me.o2 - 1);
-        uint8_t *dst = me.out + jo * me.o2 + ko;
         const long long ost = me.o1 * me.o2;
+        uint8_t *dst = me.out + jo * me.o2 + ko + (long long)(xlo - me.e0) * ost; // output of x = xlo
+        // wall planes of axis 0 (unextended coordinates 0 and o0 - 1)
+        const int xw0 = me.wall[0] ? me.e0 : -1, xw1 = me.wall[1] ? me.e0 + (int)me.o0 - 1 : -1;
+        const uint8_t in_v = me.dilate ? 1 : 0, out_v = me.dilate ? 0 : 1;
         uint64_t pend = 0; // bit b: position i - b is covered
         int reach = -1;
         const int big = T + 1;
         int cur[kCapChunk];
+        const uint16_t *pin = in;
 #pragma unroll
-        for (int u = 0; u < kCapChunk; u++)
-            cur[u] = u < n ? (int)in[u * st] : big;
+        for (int u = 0; u < kCapChunk; u++) {
+            cur[u] = u < n ? (int)*pin : big;
+            pin += st;
+        }
         for (int i0 = 0; i0 < n + W; i0 += kCapChunk) {
             int nxt[kCapChunk];
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++) {
-                const int ii = i0 + kCapChunk + u;
-                nxt[u] = ii < n ? (int)in[(long long)ii * st] : big;
+                nxt[u] = i0 + kCapChunk + u < n ? (int)*pin : big;
+                pin += st;
             }
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++) {
                 const int i = i0 + u;
                 pend <<= 1;
-                if (i < n) {
-                    const int K = cur[u];
-                    if (K <= T) {
-                        const int w = isqrt_small(T - K);
-                        pend |= (2ull << w) - 1ull;
-                        reach = max(reach, i + w);
-                    }
-                    if (reach >= i)
-                        pend |= 1ull;
+                const int K = cur[u]; // big past the end of the line
+                if (K <= T) {
+                    const int w = s_w[K];
+                    pend |= (2ull << w) - 1ull;
+                    reach = max(reach, i + w);
                 }
+                if (reach >= i && i < n)
+                    pend |= 1ull;
                 const int x = i - W;
-                const long long io = io0 + x;
-                if (x < 0 || x >= n || io < 0 || io >= me.o0)
+                if (x < xlo || x >= xhi)
                     continue;
-                const bool within = (pend >> W) & 1ull;
-                uint8_t v = me.dilate ? (uint8_t)within : (uint8_t)!within;
-                if (wall_jk || (me.wall[0] && io == 0) || (me.wall[1] && io == me.o0 - 1))
+                uint8_t v = ((pend >> W) & 1ull) ? in_v : out_v;
+                if (wall_jk || x == xw0 || x == xw1)
                     v = 0;
-                dst[io * ost] = v;
+                *dst = v;
+                dst += ost;
             }
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++)
