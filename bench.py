@@ -142,6 +142,17 @@ def prof_read(L):
     return {keys[i]: {"ms": ms[i], "bytes": by[i], "launches": n[i]} for i in range(cnt.value)}
 
 
+def max_over_ranks(x, dist, device):
+    """Largest x over the ranks: the job's time is its slowest replica's."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -206,9 +217,7 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     prof = prof_read(L)
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
     sat = [float(c / np.prod(sd.domain.voxels)) / phi for c in counts]
 
@@ -239,9 +248,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     assert sat_e == sat, "end-to-end path disagrees with the resident path"
 
     if rank != 0:

@@ -1323,9 +1323,11 @@ __global__ void k_bcc_mark(const uint8_t *__restrict__ M, const int *__restrict_
 // block's four rows.
 template <typename TO>
 __global__ void k_bcc_select(const uint8_t *__restrict__ M, const int *__restrict__ P,
-                             const uint8_t *__restrict__ mark, BGrid G, int mode, TO val, TO *__restrict__ out)
+                             const uint8_t *__restrict__ mark, BGrid G, int mode, TO val, TO *__restrict__ out,
+                             unsigned long long *kept)
 {
     const int nb = G.b0 * G.b1 * G.b2;
+    unsigned int cnt = 0; // kept voxels (mask bits exist only for voxels inside the volume)
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         const int r = b / G.b2;
         const int c2 = b - r * G.b2;
@@ -1348,6 +1350,7 @@ __global__ void k_bcc_select(const uint8_t *__restrict__ M, const int *__restric
             if (!keep)
                 m = 0;
         }
+        cnt += __popc(m);
 #pragma unroll
         for (int x = 0; x < 2; x++)
 #pragma unroll
@@ -1363,6 +1366,12 @@ __global__ void k_bcc_select(const uint8_t *__restrict__ M, const int *__restric
                         row[k] = ((m >> ((x * 2 + y) * 2 + z)) & 1) ? val : (TO)0;
                 }
             }
+    }
+    if (kept) {
+        for (int o = 16; o > 0; o >>= 1)
+            cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+        if ((threadIdx.x & 31) == 0 && cnt)
+            atomicAdd(kept, (unsigned long long)cnt);
     }
 }
 
@@ -1424,7 +1433,8 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
 template <class Src>
 static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
                            const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
-                           int val, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+                           int val, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st,
+                           unsigned long long *kept)
 {
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
@@ -1456,10 +1466,10 @@ static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64
         const int ps__ = prof_begin("k_bcc_select", st);
         if (out_bytes == 1)
             k_bcc_select<uint8_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(M, P, mark, G, mode, (uint8_t)val,
-                                                                               (uint8_t *)out);
+                                                                               (uint8_t *)out, kept);
         else
             k_bcc_select<uint64_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
-                M, P, mark, G, mode, (uint64_t)val, (uint64_t *)out);
+                M, P, mark, G, mode, (uint64_t)val, (uint64_t *)out, kept);
         prof_end(ps__, (double)n * out_bytes + (double)nb * 5, st);
     }
     PMG_CHECK_LAUNCH();
@@ -1470,11 +1480,12 @@ static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64
 // voxels receive `fgval`, or 1 for fgval < 0 (an image of 0s and 1s).
 int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
                       const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
-                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st,
+                      unsigned long long *kept)
 {
     SrcImg src{img, fgval};
     return bcc_select_core(src, out, out_bytes, shape, bc, pad, inlet_box, outlet_box, mode, fgval >= 0 ? fgval : 1,
-                           P, M, mark, err, st);
+                           P, M, mark, err, st, kept);
 }
 
 // Erosion fused into the selection: the foreground is E > T off the wall
@@ -1482,7 +1493,7 @@ int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_
 // unextended image; kept voxels receive 1.
 int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, const int32_t *bc,
                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *P,
-                     uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
+                     uint8_t *M, uint8_t *mark, int *err, cudaStream_t st, unsigned long long *kept)
 {
     SrcErode src;
     src.E = E;
@@ -1493,7 +1504,7 @@ int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, 
     src.walls = 0;
     for (int q = 0; q < 6; q++)
         src.walls |= (bc[q] == PMG_BC_WALL ? 1u : 0u) << q;
-    return bcc_select_core(src, out, 1, shape, bc, pad, inlet_box, outlet_box, mode, 1, P, M, mark, err, st);
+    return bcc_select_core(src, out, 1, shape, bc, pad, inlet_box, outlet_box, mode, 1, P, M, mark, err, st, kept);
 }
 
 // ---- binary labelling on blocks -----------------------------------------------
@@ -1818,7 +1829,7 @@ extern "C" int pmg_cc_select(const uint8_t *img, void *out, int32_t out_bytes,
         PMG_TRY(scratch_alloc((void **)&err, sizeof(int), st));
         PMG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
         s = select_run_binary(img, out, out_bytes, shape, bc, pad, inlet_box, outlet_box, mode, phase >= 0 ? phase : -1,
-                              P, mark, mark + mb, err, st);
+                              P, mark, mark + mb, err, st, nullptr);
     } else {
         PMG_TRY(scratch_alloc((void **)&P, (size_t)n * 4, st));
         PMG_TRY(scratch_alloc((void **)&mark, ((size_t)n + 3) & ~(size_t)3, st));

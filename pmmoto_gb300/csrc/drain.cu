@@ -59,13 +59,14 @@ __global__ void k_constrain(uint8_t *res, const uint8_t *__restrict__ nconn, lon
 // (i, j) row.  Lanes take two voxels per load when rows start on
 // even addresses.
 __global__ void k_drain_update_count(uint8_t *mp, const uint8_t *__restrict__ morph, const uint8_t *__restrict__ w,
-                                     long long s0, long long s1, long long s2, Boxes B, unsigned long long *cnt)
+                                     long long s0, long long s1, long long s2, Boxes B, unsigned long long *cnt,
+                                     unsigned long long *ones)
 {
     const long long rows = s0 * s1;
     const int lane = threadIdx.x & 31;
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    unsigned int c = 0;
+    unsigned int c = 0, c1 = 0; // value 2 in the own box; value 1 anywhere
     const bool pairs = (s2 & 1) == 0;
     for (long long r = warp; r < rows; r += nwarps) {
         const long long i = r / s1, j = r - (r / s1) * s1;
@@ -86,6 +87,7 @@ __global__ void k_drain_update_count(uint8_t *mp, const uint8_t *__restrict__ mo
                     if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
                         v = 1;
                     c += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
+                    c1 += v == 1;
                     o |= (uint16_t)v << (8 * b);
                 }
                 p2[h] = o;
@@ -97,14 +99,19 @@ __global__ void k_drain_update_count(uint8_t *mp, const uint8_t *__restrict__ mo
                 if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
                     v = 1;
                 c += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
+                c1 += v == 1;
                 mp[idx] = v;
             }
         }
     }
-    for (int o = 16; o > 0; o >>= 1)
+    for (int o = 16; o > 0; o >>= 1) {
         c += __shfl_down_sync(0xffffffffu, c, o);
+        c1 += __shfl_down_sync(0xffffffffu, c1, o);
+    }
     if (lane == 0 && c)
         atomicAdd(cnt, (unsigned long long)c);
+    if (lane == 0 && c1)
+        atomicAdd(ones, (unsigned long long)c1);
 }
 
 // Erosion by thresholding a precomputed squared EDT (subtraction's
@@ -214,18 +221,23 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
                            const int32_t *pad, const int32_t *ext_e, const int32_t *ext_d, const float *res,
                            double r_e, int cmp_e, double r_d, int cmp_d, int inlet, const uint8_t *mp,
                            const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d,
-                           const float *De = nullptr, const uint16_t *KC = nullptr, int Te = -1)
+                           const float *De = nullptr, const uint16_t *KC = nullptr, int Te = -1,
+                           bool m1_counted = false)
 {
+    // m1_counted: w.cnt[1] already holds count(mp == 1) (the drainage update
+    // counts it); the inlet selection counts its kept voxels into w.cnt[0], and
+    // both come back with one copy
     const long long n = shape[0] * shape[1] * shape[2];
     const int64_t all[6] = {0, shape[0], 0, shape[1], 0, shape[2]};
     uint8_t *E;
     float *A, *B;
     morph_split(w, shape, bc, ext_e, E, A, B);
     uint8_t *cur = w.t1;
+    PMG_CUDA(cudaMemsetAsync(w.cnt, 0, sizeof(unsigned long long), st));
     if (KC && inlet) {
         PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
         PMG_TRY(select_run_erode(KC, Te, w.t2, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, w.P, w.M, w.mark,
-                                 w.err, st));
+                                 w.err, st, w.cnt));
         PMG_TRY(check_err(w.err, st));
         cur = w.t2;
     } else if (De) {
@@ -248,16 +260,25 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
         PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
         // the eroded image holds only 0 and 1
         PMG_TRY(select_run_binary(w.t1, w.t2, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, -1, w.P, w.M,
-                                  w.mark, w.err, st));
+                                  w.mark, w.err, st, w.cnt));
         PMG_TRY(check_err(w.err, st));
         cur = w.t2;
     }
-    long long c1 = 0;
-    PMG_TRY(count_sync(cur, shape, all, 1, w, st, c1));
+    long long c1 = 0, m1 = -1;
+    if (inlet) {
+        unsigned long long h[2] = {0, 0};
+        PMG_CUDA(cudaMemcpyAsync(h, w.cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+        PMG_CUDA(cudaStreamSynchronize(st));
+        c1 = (long long)h[0];
+        if (m1_counted)
+            m1 = (long long)h[1];
+    } else {
+        PMG_TRY(count_sync(cur, shape, all, 1, w, st, c1));
+    }
     if (c1 > 0) {
         if (mp) {
-            long long m1 = 0;
-            PMG_TRY(count_sync(mp, shape, all, 1, w, st, m1));
+            if (m1 < 0)
+                PMG_TRY(count_sync(mp, shape, all, 1, w, st, m1));
             if (m1 > 0) {
                 PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
                 PMG_TRY(select_run_binary(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1, w.P,
@@ -450,6 +471,12 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         s = cudaMemsetAsync(d_counts, 0, sizeof(unsigned long long) * (size_t)(n_radii + 1), st) == cudaSuccess
                 ? PMG_OK
                 : PMG_ECUDA;
+    // count(mp == 1) for the first radius; the update kernel keeps it current
+    const int64_t whole[6] = {0, shape[0], 0, shape[1], 0, shape[2]};
+    if (s == PMG_OK)
+        s = cudaMemsetAsync(w.cnt + 1, 0, sizeof(unsigned long long), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    if (s == PMG_OK)
+        s = count_eq_async(mp_img, shape, whole, 1, w.cnt + 1, st);
     for (int k = 0; k < n_radii && s == PMG_OK; k++) {
         if (active[k]) {
             int32_t ext[6];
@@ -457,7 +484,7 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
             // the probe radius is a numpy float64: compare in float64
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext, res, radii[k], 1, radii[k], 1, 1, mp_img,
                                 Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
-                                De, KC, Te[(size_t)k]);
+                                De, KC, Te[(size_t)k], true);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
@@ -471,9 +498,10 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         if (s != PMG_OK)
             break;
         {
+            PMG_CUDA(cudaMemsetAsync(w.cnt + 1, 0, sizeof(unsigned long long), st));
             const int ps__ = prof_begin("k_drain_update_count", st);
             k_drain_update_count<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
-                mp_img, morph, wet, shape[0], shape[1], shape[2], Bx, d_counts + k);
+                mp_img, morph, wet, shape[0], shape[1], shape[2], Bx, d_counts + k, w.cnt + 1);
             prof_end(ps__, (double)n * 4, st);
         }
         PMG_CHECK_LAUNCH();

@@ -22,10 +22,11 @@ int select_run(const uint8_t *img, void *out, int out_bytes, const int64_t *shap
                cudaStream_t st);
 int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
                       const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
-                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st);
+                      int fgval, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st,
+                      unsigned long long *kept = nullptr);
 int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, const int32_t *bc,
                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *P,
-                     uint8_t *M, uint8_t *mark, int *err, cudaStream_t st);
+                     uint8_t *M, uint8_t *mark, int *err, cudaStream_t st, unsigned long long *kept = nullptr);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 
