@@ -236,6 +236,22 @@ int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
                  const double *ball_erode, const double *ball_dilate, int64_t *counts,
                  void *stream);
 
+/*
+ * pmg_drainage with dilation radii that differ from the erosion radii: the
+ * extended contact-angle method (equilibrium_distribution.py:230-289,
+ * dilation radius = erosion radius * |cos(theta)|).  radii_dilate (host,
+ * float64) and ratios_dilate (ceil(r/res) per axis per radius) may be NULL,
+ * which gives pmg_drainage.  The contact_angle method (:182-228) is
+ * pmg_drainage with its own probe radii.
+ */
+int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
+                     const int32_t bc[6], const int32_t pad[6], const int32_t rpad[6],
+                     const int64_t own_box[6], const int64_t inlet_box[6],
+                     const int64_t outlet_box[6], const float res[3], int32_t n_radii,
+                     const double *radii, const int32_t *active, const int32_t *ratios,
+                     const double *ball_erode, const double *ball_dilate, int64_t *counts,
+                     const double *radii_dilate, const int32_t *ratios_dilate, void *stream);
+
 /* Number of kernels this library has launched in the process. */
 long long pmg_launch_count(void);
 

@@ -635,8 +635,10 @@ def max_distance(geom: Geom, pm_img):
     return float(np.amax(d))
 
 
-def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1, mode="distance", dmax=None):
-    """drainage + _standard_method (equilibrium_distribution.py:25-179).
+def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1, mode="distance", dmax=None, contact_angle=0,
+             method="standard"):
+    """drainage with _standard_method, _contact_angle_method or
+    _extended_contact_angle_method (equilibrium_distribution.py:25-289).
 
     Returns (saturations, final multiphase image)."""
     if isinstance(capillary_pressures, (int, float)):
@@ -646,14 +648,21 @@ def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1, mode="distance", 
     mp_img = np.where(pm_img == 1, 2, 0).astype(np.uint8)
     phi = porosity(geom, pm_img)
     sat = np.zeros(len(capillary_pressures))
+    theta = contact_angle if method != "standard" else 0
     for n, pc in enumerate(capillary_pressures):
-        radius = 0 if pc == 0 else 2.0 * gamma / pc * np.cos(np.deg2rad(0))
-        if radius < min(geom.resolution):
+        # Multiphase.get_probe_radius (multiphase.py:98-116)
+        radius = 0 if pc == 0 else 2.0 * gamma / pc * np.cos(np.deg2rad(theta))
+        if method == "extended_contact_angle":
+            radius = [radius, radius * np.abs(np.cos(np.deg2rad(theta)))]
+            lo, hi = min(radius), max(radius)
+        else:
+            lo = hi = radius
+        if lo < min(geom.resolution):
             morph = np.zeros_like(pm_img, dtype=np.uint8)
         else:
             if dmax is None:
                 dmax = max_distance(geom, pm_img)
-            if radius > dmax:
+            if hi > dmax:
                 morph = np.zeros_like(pm_img, dtype=np.uint8)
             else:
                 morph = porosimetry(geom, pm_img, radius, inlet=True, mp_img=mp_img, mode=mode)

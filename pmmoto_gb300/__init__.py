@@ -8,7 +8,7 @@ hand-written sm_103a CUDA kernels through the C ABI in
 ``include/pmmoto_gb300.h``, one subdomain on one GPU.
 """
 
-from . import core, domain_generation, filters  # noqa: F401
+from . import core, domain_generation, filters, io, particles  # noqa: F401
 from .core import BoundaryType, initialize  # noqa: F401
 
-__all__ = ["initialize", "BoundaryType", "core", "domain_generation", "filters"]
+__all__ = ["initialize", "BoundaryType", "core", "domain_generation", "filters", "io", "particles"]

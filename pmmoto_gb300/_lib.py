@@ -53,6 +53,7 @@ def _declare(L):
         "pmg_max_f32": [P, P, P, P, P],
         "pmg_porosimetry": [P, P, P, P, P, P, P, P, f64, i32, P, f64, i32, P, i32, f64, f64, P],
         "pmg_drainage": [P, P, P, P, P, P, P, P, P, P, i32, P, P, P, P, P, P, P],
+        "pmg_drainage_ext": [P, P, P, P, P, P, P, P, P, P, i32, P, P, P, P, P, P, P, P, P],
         "pmg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
     }
     for name, args in sig.items():

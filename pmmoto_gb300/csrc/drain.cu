@@ -235,10 +235,8 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
     uint8_t *cur = w.t1;
     PMG_CUDA(cudaMemsetAsync(w.cnt, 0, sizeof(unsigned long long), st));
     if (KC && inlet) {
-        PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
         PMG_TRY(select_run_erode(KC, Te, w.t2, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, w.P, w.M, w.mark,
                                  w.err, st, w.cnt));
-        PMG_TRY(check_err(w.err, st));
         cur = w.t2;
     } else if (De) {
         ErodeThr T;
@@ -257,11 +255,9 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
         PMG_TRY(morph_run(pm, w.t1, shape, bc, pad, ext_e, res, r_e, cmp_e, 0, E, A, B, st, ball_e));
     }
     if (inlet && cur == w.t1) {
-        PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
         // the eroded image holds only 0 and 1
         PMG_TRY(select_run_binary(w.t1, w.t2, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, -1, w.P, w.M,
                                   w.mark, w.err, st, w.cnt));
-        PMG_TRY(check_err(w.err, st));
         cur = w.t2;
     }
     long long c1 = 0, m1 = -1;
@@ -280,10 +276,8 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
             if (m1 < 0)
                 PMG_TRY(count_sync(mp, shape, all, 1, w, st, m1));
             if (m1 > 0) {
-                PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
                 PMG_TRY(select_run_binary(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1, w.P,
                                           w.M, w.mark, w.err, st));
-                PMG_TRY(check_err(w.err, st));
                 {
                     const int ps__ = prof_begin("k_constrain", st);
                     k_constrain<<<grid_for(n / 16 + 1, 256, 152LL * 32), 256, 0, st>>>(cur, w.t3, n);
@@ -349,20 +343,27 @@ extern "C" int pmg_porosimetry(const uint8_t *pm_img, const uint8_t *mp_img, uin
     }
     Work w{};
     PMG_TRY(work_alloc(w, shape, max_morph_bytes(shape, bc, ext_e, ext_d), st));
+    PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
     int s = porosimetry_run(pm_img, out, shape, bc, pad, ext_e, ext_d, res, r_erode, cmp_erode, r_dilate,
                             cmp_dilate, inlet, mp_img, Bx, w, st, ball_erode, ball_dilate);
+    if (s == PMG_OK)
+        s = check_err(w.err, st);
     int s2 = scratch_free(w.base, st);
     return s != PMG_OK ? s : s2;
 }
 
-extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
-                            const int32_t bc[6], const int32_t pad[6], const int32_t rpad[6],
-                            const int64_t own_box[6], const int64_t inlet_box[6],
-                            const int64_t outlet_box[6], const float res[3], int32_t n_radii,
-                            const double *radii, const int32_t *active, const int32_t *ratios,
-                            const double *ball_erode, const double *ball_dilate, int64_t *counts,
-                            void *stream)
+extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
+                                const int32_t bc[6], const int32_t pad[6], const int32_t rpad[6],
+                                const int64_t own_box[6], const int64_t inlet_box[6],
+                                const int64_t outlet_box[6], const float res[3], int32_t n_radii,
+                                const double *radii, const int32_t *active, const int32_t *ratios,
+                                const double *ball_erode, const double *ball_dilate, int64_t *counts,
+                                const double *radii_dilate, const int32_t *ratios_dilate, void *stream)
 {
+    if (!radii_dilate)
+        radii_dilate = radii;
+    if (!ratios_dilate)
+        ratios_dilate = ratios;
     PMG_TRY(check_common(shape, bc, pad));
     if (!pm_img || !mp_img || !rpad || !own_box || !res || !counts || n_radii < 0 ||
         (n_radii > 0 && (!radii || !active || !ratios))) {
@@ -388,12 +389,17 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
     for (int k = 0; k < n_radii; k++) {
         int32_t ext[6];
         ext_of(bc, pad, ratios + 3 * k, ext);
-        const size_t b = morph_scratch_bytes(shape, bc, ext);
+        size_t b = morph_scratch_bytes(shape, bc, ext);
+        if (b > mb)
+            mb = b;
+        ext_of(bc, pad, ratios_dilate + 3 * k, ext);
+        b = morph_scratch_bytes(shape, bc, ext);
         if (b > mb)
             mb = b;
     }
     Work w{};
     PMG_TRY(work_alloc(w, shape, mb, st));
+    PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
     uint8_t *morph = nullptr, *wet = nullptr;
     unsigned long long *d_counts = nullptr;
     // Without periodic axes the erosion's extended image is the same for every
@@ -479,10 +485,12 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         s = count_eq_async(mp_img, shape, whole, 1, w.cnt + 1, st);
     for (int k = 0; k < n_radii && s == PMG_OK; k++) {
         if (active[k]) {
-            int32_t ext[6];
+            int32_t ext[6], ext_d[6];
             ext_of(bc, pad, ratios + 3 * k, ext);
-            // the probe radius is a numpy float64: compare in float64
-            s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext, res, radii[k], 1, radii[k], 1, 1, mp_img,
+            ext_of(bc, pad, ratios_dilate + 3 * k, ext_d);
+            // the probe radii are numpy float64: compare in float64
+            s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext_d, res, radii[k], 1, radii_dilate[k], 1, 1,
+                                mp_img,
                                 Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
                                 De, KC, Te[(size_t)k], true);
         } else {
@@ -490,11 +498,8 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         }
         if (s != PMG_OK)
             break;
-        PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
         s = select_run_binary(mp_img, wet, 1, shape, bc, pad, nullptr, Bx.outlet, PMG_SEL_OUTLET, 2, w.P, w.M,
                               w.mark, w.err, st);
-        if (s == PMG_OK)
-            s = check_err(w.err, st);
         if (s != PMG_OK)
             break;
         {
@@ -506,6 +511,10 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
         }
         PMG_CHECK_LAUNCH();
     }
+    // union-find iteration caps are checked once per curve: the status word
+    // is only ever set, never cleared, during the sweep
+    if (s == PMG_OK)
+        s = check_err(w.err, st);
     if (s == PMG_OK && n_radii > 0) {
         std::vector<unsigned long long> h((size_t)n_radii);
         PMG_CUDA(cudaMemcpyAsync(h.data(), d_counts, sizeof(unsigned long long) * (size_t)n_radii,
@@ -521,4 +530,16 @@ extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_
     scratch_free(d_counts, st);
     int s2 = scratch_free(w.base, st);
     return s != PMG_OK ? s : s2;
+}
+
+extern "C" int pmg_drainage(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape[3],
+                            const int32_t bc[6], const int32_t pad[6], const int32_t rpad[6],
+                            const int64_t own_box[6], const int64_t inlet_box[6],
+                            const int64_t outlet_box[6], const float res[3], int32_t n_radii,
+                            const double *radii, const int32_t *active, const int32_t *ratios,
+                            const double *ball_erode, const double *ball_dilate, int64_t *counts,
+                            void *stream)
+{
+    return pmg_drainage_ext(pm_img, mp_img, shape, bc, pad, rpad, own_box, inlet_box, outlet_box, res, n_radii,
+                            radii, active, ratios, ball_erode, ball_dilate, counts, nullptr, nullptr, stream);
 }

@@ -10,7 +10,7 @@ from .. import _dev, _ops
 from ..core.geometry import geo_of
 from . import multiphase, porousmedia
 
-__all__ = ["gen_pm_spheres_domain", "gen_mp_constant"]
+__all__ = ["gen_pm_spheres_domain", "gen_pm_shape", "gen_mp_constant"]
 
 
 def gen_pm_spheres_domain(subdomain, spheres, kd: bool = False, invert: bool = False):
@@ -28,6 +28,20 @@ def gen_pm_spheres_domain(subdomain, spheres, kd: bool = False, invert: bool = F
     img = t if isinstance(spheres, torch.Tensor) else t.cpu().numpy()
     img = subdomain.set_wall_bcs(img)
     return porousmedia.gen_pm(subdomain, img)
+
+
+def gen_pm_shape(subdomain, shapes, kd: bool = False):
+    """gen_pm_shape (_domain_generation.pyx:30-92) for a sphere list (from
+    ``particles.initialize_spheres``, periodic images included) or an (N, 4)
+    array: 1 at voxel centres outside every sphere, 0 inside; no halo update
+    and no wall rule.  numpy arrays / lists give numpy, CUDA tensors stay on
+    the device."""
+    arr = shapes.return_np_array() if hasattr(shapes, "return_np_array") else shapes
+    g = geo_of(subdomain)
+    t = _ops.spheres_device(arr, subdomain.coords)
+    if tuple(t.shape) != g.shape:
+        raise ValueError("subdomain coords do not match its voxels")
+    return t if isinstance(arr, torch.Tensor) else t.cpu().numpy()
 
 
 def gen_mp_constant(porous_media, fluid_phase: int = 1):

@@ -31,51 +31,61 @@ def _radius(pc, gamma, contact_angle):
     return 2.0 * gamma / pc * np.cos(np.deg2rad(contact_angle))
 
 
-def drainage_counts(multiphase, radii, mode="distance"):
+def drainage_counts(multiphase, radii, mode="distance", radii_dilate=None):
     """Run the drainage sweep for the given probe radii on the device; returns
-    (per-radius own-region phase-2 counts, final multiphase CUDA tensor)."""
+    (per-radius own-region phase-2 counts, final multiphase CUDA tensor).
+    radii_dilate: dilation radii when they differ from the erosion radii
+    (extended contact-angle method)."""
     sd = multiphase.subdomain
     g = geo_of(sd)
     pm, _ = morph.to_u8(multiphase.porous_media.img)
     mp, _ = morph.to_u8(multiphase.img)
     mp = mp.clone()
     n = len(radii)
+    if radii_dilate is None:
+        radii_dilate = radii
     active = np.zeros(n, dtype=np.int32)
     ratios = np.zeros((max(n, 1), 3), dtype=np.int32)
+    ratios_d = np.zeros((max(n, 1), 3), dtype=np.int32)
     rad = np.zeros(max(n, 1), dtype=np.float64)
+    rad_d = np.zeros(max(n, 1), dtype=np.float64)
     be = np.full(max(n, 1), -1.0)
     bd = np.full(max(n, 1), -1.0)
     min_res = min(sd.domain.resolution)
-    for k, r in enumerate(radii):
+    for k, (r, rd) in enumerate(zip(radii, radii_dilate)):
         rad[k] = float(r)
-        if r < min_res or r > multiphase.porous_media.max_distance:
+        rad_d[k] = float(rd)
+        if min(r, rd) < min_res or max(r, rd) > multiphase.porous_media.max_distance:
             continue
-        morph.check_radii(sd, [r, r])
+        morph.check_radii(sd, [r, rd])
         active[k] = 1
         ratios[k] = morph.gen_struct_element(g.res, r)[0]
+        ratios_d[k] = morph.gen_struct_element(g.res, rd)[0]
         if mode == "morph":
             be[k] = morph.ball_sq(g.res, r)
         if mode in ("morph", "hybrid"):
-            bd[k] = morph.ball_sq(g.res, r)
+            bd[k] = morph.ball_sq(g.res, rd)
     from .connected_components import _box
 
     counts = np.zeros(max(n, 1), dtype=np.int64)
     rpad = np.ascontiguousarray([g.rpad[d][s] for d in range(3) for s in (0, 1)], dtype=np.int32)
     res32 = np.ascontiguousarray([np.float32(r) for r in g.res], dtype=np.float32)
     own = np.ascontiguousarray([v for lohi in g.own_box() for v in lohi], dtype=np.int64)
-    st = lib().pmg_drainage(_dev.ptr(pm), _dev.ptr(mp), host_ptr(i64_array(pm.shape)), host_ptr(g.bc_codes()),
-                            host_ptr(g.pad_flat()), host_ptr(rpad), host_ptr(own),
-                            host_ptr(_box(g.face_slab("inlet"))), host_ptr(_box(g.face_slab("outlet"))),
-                            host_ptr(res32), n, host_ptr(rad), host_ptr(active), host_ptr(ratios), host_ptr(be),
-                            host_ptr(bd), host_ptr(counts), _dev.stream_ptr(pm.device))
+    st = lib().pmg_drainage_ext(_dev.ptr(pm), _dev.ptr(mp), host_ptr(i64_array(pm.shape)), host_ptr(g.bc_codes()),
+                                host_ptr(g.pad_flat()), host_ptr(rpad), host_ptr(own),
+                                host_ptr(_box(g.face_slab("inlet"))), host_ptr(_box(g.face_slab("outlet"))),
+                                host_ptr(res32), n, host_ptr(rad), host_ptr(active), host_ptr(ratios), host_ptr(be),
+                                host_ptr(bd), host_ptr(counts), host_ptr(rad_d), host_ptr(ratios_d),
+                                _dev.stream_ptr(pm.device))
     check(st, "drainage")
     return counts[:n], mp
 
 
 def drainage(multiphase, capillary_pressures, gamma=1, contact_angle=0, method="standard", mode="hybrid",
              save=False, out_folder="drainage_out"):
-    """Wetting-phase saturation at each capillary pressure (standard method,
-    equilibrium_distribution.py:25-179).  multiphase.img is updated."""
+    """Wetting-phase saturation at each capillary pressure
+    (equilibrium_distribution.py:25-289: standard, contact_angle and
+    extended_contact_angle methods).  multiphase.img is updated."""
     if isinstance(capillary_pressures, (int, float)):
         capillary_pressures = [capillary_pressures]
     elif isinstance(capillary_pressures, list):
@@ -87,15 +97,21 @@ def drainage(multiphase, capillary_pressures, gamma=1, contact_angle=0, method="
         if contact_angle != 0:
             raise ValueError("The standard approach requires a zero contact angle!")
     elif method in ("contact_angle", "extended_contact_angle"):
-        raise NotImplementedError(f"drainage method {method!r} is not part of the GPU build")
+        if contact_angle == 0:
+            logging.warning("The contact angle is zero. This will yield same results as the standard approach.")
     else:
         raise ValueError(f"{method} is not implemented. ")
     if mode not in MODES:
         raise ValueError(f"mode {mode} must be one of {MODES}")
     if save:
         raise NotImplementedError("saving VTK images is not part of the GPU build")
+    # probe radii as Multiphase.get_probe_radius forms them (float64); the
+    # extended method (Schulz and Wargo, :230-289) dilates by r |cos(theta)|
     radii = [_radius(pc, gamma, contact_angle) for pc in capillary_pressures]
-    counts, mp = drainage_counts(multiphase, radii, mode)
+    radii_d = None
+    if method == "extended_contact_angle":
+        radii_d = [r * np.abs(np.cos(np.deg2rad(contact_angle))) for r in radii]
+    counts, mp = drainage_counts(multiphase, radii, mode, radii_d)
     total = np.prod(multiphase.subdomain.domain.voxels)
     phi = multiphase.porous_media.porosity
     sat = np.zeros(len(capillary_pressures))

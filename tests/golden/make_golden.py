@@ -184,6 +184,12 @@ def main():
     put("drain_sat_hybrid", pm.filters.equilibrium_distribution.drainage(mp_h, pcs, mode="hybrid"))
     mp_m = pm.domain_generation.gen_mp_constant(pmo, 2)
     put("drain_sat_morph", pm.filters.equilibrium_distribution.drainage(mp_m, pcs, mode="morph"))
+    # contact-angle methods (equilibrium_distribution.py:182-289), 30 degrees
+    for meth, key in (("contact_angle", "drain_sat_ca"), ("extended_contact_angle", "drain_sat_eca")):
+        mp_c = pm.domain_generation.gen_mp_constant(pmo, 2)
+        put(key, pm.filters.equilibrium_distribution.drainage(mp_c, pcs, contact_angle=30.0, method=meth,
+                                                              mode="distance"))
+        put(key + "_img", mp_c.img)
     meta["drain_geom"] = geom_meta(vox, (E, W, W), box, inlet, outlet)
 
     # ---- ink bottle (tests/applications/test_drainage_inkbottle.py) -------------
@@ -221,6 +227,42 @@ def main():
                            "porosity": float(np.count_nonzero(own) / own.size),
                            "edt3d_max": float(e3.max())}
     meta["c1_full"] = full
+
+    # ---- periodic sphere images, ownership, trimming, gen_pm_shape --------------
+    from pmmoto.domain_generation import _domain_generation as dgen
+
+    r3 = np.random.default_rng(77)
+    vox, box = (24, 20, 28), ((0.0, 1.2), (0.0, 1.0), (0.0, 1.4))
+    cases = []
+    for ci, bts in enumerate([(P, P, P), (P, E, W)]):
+        sd = pm.initialize(vox, box=box, boundary_types=bts)
+        sph = np.c_[r3.random((40, 3)) * np.array([b[1] for b in box]), r3.uniform(0.05, 0.2, 40)]
+        put(f"psph_{ci}_in", sph)
+        for key, kw in (("per", dict(add_periodic=True)), ("plain", {}),
+                        ("trim", dict(add_periodic=True, trim_intersecting=True)),
+                        ("within", dict(trim_within=True))):
+            lst = pm.particles.initialize_spheres(sd, sph, **kw)
+            put(f"psph_{ci}_{key}", np.asarray(lst.return_np_array(return_own=True)))
+            put(f"psph_{ci}_{key}_count", np.array([lst.size(), lst.get_own_count()]))
+            if key == "per":
+                put(f"psph_{ci}_img", dgen.gen_pm_shape(sd, lst))
+        cases.append(geom_meta(vox, bts, box))
+    meta["psph_cases"] = cases
+
+    # ---- sphere-pack file reader on a synthetic pack ----------------------------
+    import tempfile
+
+    text = "0.0 1.5\n-0.5 0.5\n0.0 2.0\n" + "".join(
+        f"{x:.6f} {y:.6f} {z:.6f} {r:.6f}\n" for x, y, z, r in
+        np.c_[r3.random((7, 3)) * np.array([1.5, 1.0, 2.0]) - np.array([0.0, 0.5, 0.0]), r3.uniform(0.1, 0.3, 7)])
+    with tempfile.NamedTemporaryFile("w", suffix=".out", delete=False) as f:
+        f.write(text)
+        fname = f.name
+    sph_r, dom_r = pm.io.data_read.read_sphere_pack_xyzr_domain(fname)
+    os.unlink(fname)
+    put("pack_read_spheres", sph_r)
+    put("pack_read_domain", np.asarray(dom_r))
+    meta["pack_text"] = text
 
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **out)
     with open(os.path.join(HERE, "golden_meta.json"), "w") as f:

@@ -66,6 +66,12 @@ def test_drainage_golden(P, golden, golden_meta):
         mp = P.domain_generation.gen_mp_constant(pm, 2)
         np.testing.assert_array_equal(P.filters.equilibrium_distribution.drainage(mp, pcs, mode=mode),
                                       golden[f"drain_sat_{mode}"])
+    # contact-angle methods at 30 degrees (the extended one dilates by r cos(theta))
+    for meth, key in (("contact_angle", "drain_sat_ca"), ("extended_contact_angle", "drain_sat_eca")):
+        mp = P.domain_generation.gen_mp_constant(pm, 2)
+        sat = P.filters.equilibrium_distribution.drainage(mp, pcs, contact_angle=30.0, method=meth, mode="distance")
+        np.testing.assert_array_equal(sat, golden[key])
+        np.testing.assert_array_equal(mp.img, golden[key + "_img"])
 
 
 def test_inkbottle(P, golden, golden_meta):
@@ -100,3 +106,12 @@ def test_drainage_random_vs_oracle(P, seed):
     want, want_img = O.drainage(g, pm.img, pcs)
     np.testing.assert_array_equal(sat, want)
     np.testing.assert_array_equal(mp.img, want_img)
+
+
+@pytest.mark.parametrize("ci", range(2))
+def test_gen_pm_shape_periodic_images_golden(P, golden, golden_meta, ci):
+    """Voxelisation of a sphere list with periodic images (gen_pm_shape)."""
+    sd = sd_from_meta(golden_meta["psph_cases"][ci])
+    lst = P.particles.initialize_spheres(sd, golden[f"psph_{ci}_in"], add_periodic=True)
+    np.testing.assert_array_equal(P.domain_generation.gen_pm_shape(sd, lst), golden[f"psph_{ci}_img"])
+

@@ -87,6 +87,10 @@ def test_inlet_outlet_and_drainage_golden(golden, golden_meta):
     np.testing.assert_array_equal(O.isolated_img(g, img), golden["drain_iso_img"])
     sat, mp_img = O.drainage(g, img, list(golden["drain_pcs"]))
     np.testing.assert_array_equal(sat, golden["drain_sat"])
+    for meth, key in (("contact_angle", "drain_sat_ca"), ("extended_contact_angle", "drain_sat_eca")):
+        sat, mp_img_c = O.drainage(g, img, list(golden["drain_pcs"]), contact_angle=30.0, method=meth)
+        np.testing.assert_array_equal(sat, golden[key])
+        np.testing.assert_array_equal(mp_img_c, golden[key + "_img"])
     np.testing.assert_array_equal(mp_img, golden["drain_mp_img"])
     np.testing.assert_array_equal(O.porosimetry(g, img, 0.1, inlet=True), golden["drain_por_r"])
     np.testing.assert_array_equal(O.pore_size_distribution(g, img, [0.03, 0.06, 0.09, 0.12]), golden["drain_psd"])
