@@ -1051,6 +1051,12 @@ struct SrcImg {
     const uint8_t *img;
     int fgval;
     __device__ __forceinline__ bool fg(long long idx, int, int, int) const { return fg_of(img[idx], fgval); }
+    // voxels idx and idx + 1 (idx even) with one 16-bit load: bit 0, bit 1
+    __device__ __forceinline__ unsigned fg2(long long idx, int, int, int) const
+    {
+        const unsigned v = *(const uint16_t *)(img + idx);
+        return (unsigned)fg_of((uint8_t)v, fgval) | ((unsigned)fg_of((uint8_t)(v >> 8), fgval) << 1);
+    }
 };
 
 // ... or an erosion read off a capped squared EDT: voxels with E > T stay,
@@ -1066,6 +1072,16 @@ struct SrcErode {
         const unsigned on = (i == 0) | ((i == s0 - 1) << 1) | ((j == 0) << 2) | ((j == s1 - 1) << 3) |
                             ((k == 0) << 4) | ((k == s2 - 1) << 5);
         return !(on & walls) && (int)E[idx] > T;
+    }
+    // voxels idx and idx + 1 (idx even, k + 1 < s2) with one 32-bit load
+    __device__ __forceinline__ unsigned fg2(long long idx, int i, int j, int k) const
+    {
+        const unsigned v = *(const uint32_t *)(E + idx);
+        const unsigned row = (i == 0) | ((i == s0 - 1) << 1) | ((j == 0) << 2) | ((j == s1 - 1) << 3);
+        const unsigned on0 = row | ((k == 0) << 4) | ((k == s2 - 1) << 5);
+        const unsigned on1 = row | ((k + 1 == s2 - 1) << 5);
+        return (unsigned)(!(on0 & walls) && (int)(v & 0xffffu) > T) |
+               ((unsigned)(!(on1 & walls) && (int)(v >> 16) > T) << 1);
     }
 };
 
@@ -1093,16 +1109,26 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
         const long long sy = G.s2, sx = (long long)G.s1 * G.s2;
         const long long base = (2LL * c0 * G.s1 + 2 * c1) * sy + 2 * c2;
         const bool whole = 2 * c0 + 1 < G.s0 && 2 * c1 + 1 < G.s1 && 2 * c2 + 1 < G.s2;
+        if (whole && !(G.s2 & 1)) {
+            // even rows: every voxel pair (z = 0, 1) starts on an even index
 #pragma unroll
-        for (int x = 0; x < 2; x++)
+            for (int x = 0; x < 2; x++)
 #pragma unroll
-            for (int y = 0; y < 2; y++)
+                for (int y = 0; y < 2; y++)
+                    m |= src.fg2(base + x * sx + y * sy, 2 * c0 + x, 2 * c1 + y, 2 * c2) << ((x * 2 + y) * 2);
+        } else {
 #pragma unroll
-                for (int z = 0; z < 2; z++) {
-                    const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2 + z;
-                    if ((whole || (i < G.s0 && j < G.s1 && k < G.s2)) && src.fg(base + x * sx + y * sy + z, i, j, k))
-                        m |= 1u << ((x * 2 + y) * 2 + z);
-                }
+            for (int x = 0; x < 2; x++)
+#pragma unroll
+                for (int y = 0; y < 2; y++)
+#pragma unroll
+                    for (int z = 0; z < 2; z++) {
+                        const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2 + z;
+                        if ((whole || (i < G.s0 && j < G.s1 && k < G.s2)) &&
+                            src.fg(base + x * sx + y * sy + z, i, j, k))
+                            m |= 1u << ((x * 2 + y) * 2 + z);
+                    }
+        }
     }
     sm[t] = (uint8_t)m;
     L[t] = m ? t : -1;
@@ -1157,20 +1183,51 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
 
 // Phase 2: blocks on a tile border unite with touching earlier neighbours in
 // other tiles; neighbours reached through an in-tile neighbour are skipped.
+// Border blocks of a tile (the only ones with earlier neighbours in other
+// tiles), numbered densely so that every lane of a warp has one: the a = 0
+// plane (kT1 x kT2), then the b = 0 and b = kT1 - 1 rows of the other planes,
+// then the c = 0 and c = kT2 - 1 ends of the remaining rows.
+constexpr int kBorderPlane = kT1 * kT2;
+constexpr int kBorderRows = (kT0 - 1) * 2 * kT2;
+constexpr int kBorderEnds = (kT0 - 1) * (kT1 - 2) * 2;
+constexpr int kBorder = kBorderPlane + kBorderRows + kBorderEnds;
+
+__device__ __forceinline__ void border_block(int q, int &a, int &b, int &c)
+{
+    if (q < kBorderPlane) {
+        a = 0;
+        b = q / kT2;
+        c = q % kT2;
+    } else if (q < kBorderPlane + kBorderRows) {
+        const int r = q - kBorderPlane;
+        a = 1 + r / (2 * kT2);
+        b = ((r / kT2) & 1) ? kT1 - 1 : 0;
+        c = r % kT2;
+    } else {
+        const int r = q - kBorderPlane - kBorderRows;
+        a = 1 + r / (2 * (kT1 - 2));
+        b = 1 + (r % (2 * (kT1 - 2))) / 2;
+        c = (r & 1) ? kT2 - 1 : 0;
+    }
+}
+
 __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int *err)
 {
     __shared__ BTabs tb;
     load_btabs(tb);
     __syncthreads();
-    const int nb = G.b0 * G.b1 * G.b2;
-    for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < nb; bi += gridDim.x * blockDim.x) {
-        const int r = bi / G.b2;
-        const int c2 = bi - r * G.b2;
-        const int c0 = r / G.b1;
-        const int c1 = r - c0 * G.b1;
-        const int a = c0 & (kT0 - 1), b = c1 & (kT1 - 1), c = c2 & (kT2 - 1);
-        if (a > 0 && b > 0 && b < kT1 - 1 && c > 0 && c < kT2 - 1)
-            continue; // every earlier neighbour is inside the tile
+    const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
+    const long long items = (long long)((G.b0 + kT0 - 1) / kT0) * nt1 * nt2 * kBorder;
+    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int tile = (int)(it / kBorder);
+        int a, b, c;
+        border_block((int)(it - (long long)tile * kBorder), a, b, c);
+        const int c0 = (tile / (nt1 * nt2)) * kT0 + a, c1 = ((tile / nt2) % nt1) * kT1 + b,
+                  c2 = (tile % nt2) * kT2 + c;
+        if (c0 >= G.b0 || c1 >= G.b1 || c2 >= G.b2)
+            continue;
+        const int bi = (c0 * G.b1 + c1) * G.b2 + c2;
         const unsigned m = M[bi];
         if (!m)
             continue;
@@ -1411,7 +1468,9 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
     PMG_CHECK_LAUNCH();
     {
         const int ps__ = prof_begin("k_bcc_cross", st);
-        k_bcc_cross<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(P, M, G, err);
+        const long long border = (long long)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) *
+                                 ((G.b2 + kT2 - 1) / kT2) * kBorder;
+        k_bcc_cross<<<grid_for(border, 256, 152LL * 64), 256, 0, st>>>(P, M, G, err);
         prof_end(ps__, 0.0, st);
     }
     PMG_CHECK_LAUNCH();
