@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "pmg_common.cuh"
+#include "pmg_internal.cuh"
 #include "uf.cuh"
 
 namespace pmg {
@@ -533,6 +534,10 @@ static int read_err(int *err, cudaStream_t st)
     int h = 0;
     PMG_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     PMG_CUDA(cudaStreamSynchronize(st));
+    if (h == 3) {
+        set_error("connected components: a growing-set selection lost voxels between steps");
+        return PMG_EINVAL;
+    }
     if (h != 0) {
         set_error("connected components: union-find iteration cap reached (code %d)", h);
         return PMG_EITER;
@@ -983,6 +988,11 @@ __host__ __device__ inline unsigned touch_mask(int d0, int d1, int d2)
 __constant__ uint8_t c_bt_self[13];
 __constant__ uint8_t c_bt_nb[13];
 __constant__ uint8_t c_bt_pair[13][13];
+// all 26 neighbours: offsets, voxels of a block touching neighbour q, voxels of
+// neighbour q touching the block
+__constant__ signed char c_g_d[26][3];
+__constant__ uint8_t c_g_self[26];
+__constant__ uint8_t c_g_nb[26];
 
 __device__ __forceinline__ unsigned bmask_of(int q, uint64_t mlo, uint64_t mhi)
 {
@@ -1085,6 +1095,38 @@ struct SrcErode {
     }
 };
 
+// Mask of block (c0, c1, c2): bit (x * 2 + y) * 2 + z for a foreground voxel
+// (2 c0 + x, 2 c1 + y, 2 c2 + z) inside the volume.
+template <class Src>
+__device__ __forceinline__ unsigned block_mask(const Src &src, const BGrid &G, int c0, int c1, int c2)
+{
+    unsigned m = 0;
+    const long long sy = G.s2, sx = (long long)G.s1 * G.s2;
+    const long long base = (2LL * c0 * G.s1 + 2 * c1) * sy + 2 * c2;
+    const bool whole = 2 * c0 + 1 < G.s0 && 2 * c1 + 1 < G.s1 && 2 * c2 + 1 < G.s2;
+    if (whole && !(G.s2 & 1)) {
+        // even rows: every voxel pair (z = 0, 1) starts on an even index
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int y = 0; y < 2; y++)
+                m |= src.fg2(base + x * sx + y * sy, 2 * c0 + x, 2 * c1 + y, 2 * c2) << ((x * 2 + y) * 2);
+    } else {
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int y = 0; y < 2; y++)
+#pragma unroll
+                for (int z = 0; z < 2; z++) {
+                    const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2 + z;
+                    if ((whole || (i < G.s0 && j < G.s1 && k < G.s2)) &&
+                        src.fg(base + x * sx + y * sy + z, i, j, k))
+                        m |= 1u << ((x * 2 + y) * 2 + z);
+                }
+    }
+    return m;
+}
+
 // Phase 1 on tiles of 4 x 8 x 32 blocks (8 x 16 x 64 voxels), one thread per
 // block: block masks from the source, then a shared-memory union-find of the
 // tile whose roots are the smallest block index of each tile-local part.
@@ -1104,32 +1146,7 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
     const int a = t / (kT1 * kT2), b = (t / kT2) % kT1, c = t % kT2;
     const int c0 = ti * kT0 + a, c1 = tj * kT1 + b, c2 = tk * kT2 + c;
     const bool inside = c0 < G.b0 && c1 < G.b1 && c2 < G.b2;
-    unsigned m = 0;
-    if (inside) {
-        const long long sy = G.s2, sx = (long long)G.s1 * G.s2;
-        const long long base = (2LL * c0 * G.s1 + 2 * c1) * sy + 2 * c2;
-        const bool whole = 2 * c0 + 1 < G.s0 && 2 * c1 + 1 < G.s1 && 2 * c2 + 1 < G.s2;
-        if (whole && !(G.s2 & 1)) {
-            // even rows: every voxel pair (z = 0, 1) starts on an even index
-#pragma unroll
-            for (int x = 0; x < 2; x++)
-#pragma unroll
-                for (int y = 0; y < 2; y++)
-                    m |= src.fg2(base + x * sx + y * sy, 2 * c0 + x, 2 * c1 + y, 2 * c2) << ((x * 2 + y) * 2);
-        } else {
-#pragma unroll
-            for (int x = 0; x < 2; x++)
-#pragma unroll
-                for (int y = 0; y < 2; y++)
-#pragma unroll
-                    for (int z = 0; z < 2; z++) {
-                        const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2 + z;
-                        if ((whole || (i < G.s0 && j < G.s1 && k < G.s2)) &&
-                            src.fg(base + x * sx + y * sy + z, i, j, k))
-                            m |= 1u << ((x * 2 + y) * 2 + z);
-                    }
-        }
-    }
+    const unsigned m = inside ? block_mask(src, G, c0, c1, c2) : 0u;
     sm[t] = (uint8_t)m;
     L[t] = m ? t : -1;
     __syncthreads();
@@ -1300,6 +1317,24 @@ static int ensure_block_tables()
     PMG_CUDA(cudaMemcpyToSymbol(c_bt_self, self, sizeof(self)));
     PMG_CUDA(cudaMemcpyToSymbol(c_bt_nb, other, sizeof(other)));
     PMG_CUDA(cudaMemcpyToSymbol(c_bt_pair, pair, sizeof(pair)));
+    signed char gd[26][3];
+    uint8_t gself[26], gnb[26];
+    int q26 = 0;
+    for (int d0 = -1; d0 <= 1; d0++)
+        for (int d1 = -1; d1 <= 1; d1++)
+            for (int d2 = -1; d2 <= 1; d2++) {
+                if (!d0 && !d1 && !d2)
+                    continue;
+                gd[q26][0] = (signed char)d0;
+                gd[q26][1] = (signed char)d1;
+                gd[q26][2] = (signed char)d2;
+                gself[q26] = (uint8_t)touch_mask(d0, d1, d2);
+                gnb[q26] = (uint8_t)touch_mask(-d0, -d1, -d2);
+                q26++;
+            }
+    PMG_CUDA(cudaMemcpyToSymbol(c_g_d, gd, sizeof(gd)));
+    PMG_CUDA(cudaMemcpyToSymbol(c_g_self, gself, sizeof(gself)));
+    PMG_CUDA(cudaMemcpyToSymbol(c_g_nb, gnb, sizeof(gnb)));
     if (dev >= 0 && dev < 64)
         g_btables_ready[dev] = true;
     return PMG_OK;
@@ -1359,7 +1394,7 @@ __global__ void k_bcc_flatten(int *P, int nb, int *err)
 }
 
 __global__ void k_bcc_mark(const uint8_t *__restrict__ M, const int *__restrict__ P, BGrid G, Box bx,
-                           uint8_t *mark, uint8_t bit)
+                           uint8_t *mark, uint8_t bit, int *err)
 {
     const long long n = bx.size();
     const long long w = bx.hi[2] - bx.lo[2], h = bx.hi[1] - bx.lo[1];
@@ -1368,7 +1403,9 @@ __global__ void k_bcc_mark(const uint8_t *__restrict__ M, const int *__restrict_
         const long long k = bx.lo[2] + q % w, j = bx.lo[1] + (q / w) % h, i = bx.lo[0] + q / (w * h);
         if (!mfg(M, G, i, j, k))
             continue;
-        const int p = P[((int)(i >> 1) * G.b1 + (int)(j >> 1)) * G.b2 + (int)(k >> 1)];
+        int p = ld(P + ((int)(i >> 1) * G.b1 + (int)(j >> 1)) * G.b2 + (int)(k >> 1));
+        if (p >= 0)
+            p = find_root(P, p, err);
         if (p >= 0 && !(mark[p] & bit))
             atomicOr((unsigned int *)(mark + (p & ~3)), (unsigned int)bit << (8 * (p & 3)));
     }
@@ -1379,9 +1416,8 @@ __global__ void k_bcc_mark(const uint8_t *__restrict__ M, const int *__restrict_
 // covers 32 consecutive blocks, i.e. 64 contiguous voxels of each of the
 // block's four rows.
 template <typename TO>
-__global__ void k_bcc_select(const uint8_t *__restrict__ M, const int *__restrict__ P,
-                             const uint8_t *__restrict__ mark, BGrid G, int mode, TO val, TO *__restrict__ out,
-                             unsigned long long *kept)
+__global__ void k_bcc_select(const uint8_t *__restrict__ M, int *P, const uint8_t *__restrict__ mark, BGrid G,
+                             int mode, TO val, TO *__restrict__ out, unsigned long long *kept, int *err)
 {
     const int nb = G.b0 * G.b1 * G.b2;
     unsigned int cnt = 0; // kept voxels (mask bits exist only for voxels inside the volume)
@@ -1392,7 +1428,14 @@ __global__ void k_bcc_select(const uint8_t *__restrict__ M, const int *__restric
         const int c1 = r - c0 * G.b1;
         unsigned m = M[b];
         if (m) {
-            const int p = P[b];
+            // the root, and the parent flattened to it
+            int p = ld(P + b);
+            if (p >= 0 && p != b) {
+                const int q = find_root(P, p, err);
+                if (q != p)
+                    P[b] = q;
+                p = q;
+            }
             const uint8_t mk = p >= 0 ? mark[p] : 0;
             const bool in = mk & 1, ou = mk & 2;
             bool keep;
@@ -1452,7 +1495,7 @@ static BGrid bgrid_of(const int64_t *shape)
 // component), -1 for empty blocks; M[b] = block mask.
 template <class Src>
 static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, const int32_t *pad, bool twins,
-                     int *P, uint8_t *M, int *err, cudaStream_t st)
+                     int *P, uint8_t *M, int *err, cudaStream_t st, bool flatten = true)
 {
     PMG_TRY(ensure_tables());
     PMG_TRY(ensure_block_tables());
@@ -1480,26 +1523,41 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
         prof_end(ps__, 0.0, st);
         PMG_CHECK_LAUNCH();
     }
-    {
+    if (flatten) {
         const int ps__ = prof_begin("k_bcc_flatten", st);
         k_bcc_flatten<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(P, nb, err);
         prof_end(ps__, (double)nb * 8, st);
+        PMG_CHECK_LAUNCH();
     }
-    PMG_CHECK_LAUNCH();
     return PMG_OK;
 }
 
-template <class Src>
-static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
-                           const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
-                           int val, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st,
-                           unsigned long long *kept)
+// Inlet / outlet boxes (lo0, hi0, lo1, hi1, lo2, hi2; null or lo0 < 0 for
+// none) must lie inside the volume.
+static int check_boxes(const int64_t *shape, const int64_t *inlet_box, const int64_t *outlet_box)
+{
+    const int64_t *boxes[2] = {inlet_box, outlet_box};
+    for (int w = 0; w < 2; w++) {
+        const int64_t *bxp = boxes[w];
+        if (!bxp || bxp[0] < 0)
+            continue;
+        for (int d = 0; d < 3; d++)
+            if (bxp[2 * d] < 0 || bxp[2 * d + 1] > shape[d] || bxp[2 * d] > bxp[2 * d + 1]) {
+                set_error("connected-image selection: face box outside the volume");
+                return PMG_EINVAL;
+            }
+    }
+    return PMG_OK;
+}
+
+// Marks of the roots of blocks with foreground in the inlet (bit 0) and
+// outlet (bit 1) boxes; parents need not be flat.
+static int bcc_marks(const int64_t *shape, const int64_t *inlet_box, const int64_t *outlet_box, const int *P,
+                     const uint8_t *M, uint8_t *mark, int *err, cudaStream_t st)
 {
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
-    const long long n = shape[0] * shape[1] * shape[2];
     PMG_CUDA(cudaMemsetAsync(mark, 0, ((size_t)nb + 3) & ~(size_t)3, st));
-    PMG_TRY(bcc_build(src, shape, bc, pad, true, P, M, err, st));
     const int64_t *boxes[2] = {inlet_box, outlet_box};
     for (int w = 0; w < 2; w++) {
         const int64_t *bxp = boxes[w];
@@ -1509,30 +1567,55 @@ static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64
         for (int d = 0; d < 3; d++) {
             b.lo[d] = bxp[2 * d];
             b.hi[d] = bxp[2 * d + 1];
-            if (b.lo[d] < 0 || b.hi[d] > shape[d] || b.lo[d] > b.hi[d]) {
-                set_error("connected-image selection: face box outside the volume");
-                return PMG_EINVAL;
-            }
         }
         if (b.size() > 0) {
             const int ps__ = prof_begin("k_bcc_mark", st);
-            k_bcc_mark<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(M, P, G, b, mark, (uint8_t)(1 << w));
+            k_bcc_mark<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(M, P, G, b, mark, (uint8_t)(1 << w),
+                                                                          err);
             prof_end(ps__, (double)b.size() * 5, st);
             PMG_CHECK_LAUNCH();
         }
     }
-    {
-        const int ps__ = prof_begin("k_bcc_select", st);
-        if (out_bytes == 1)
-            k_bcc_select<uint8_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(M, P, mark, G, mode, (uint8_t)val,
-                                                                               (uint8_t *)out, kept);
-        else
-            k_bcc_select<uint64_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
-                M, P, mark, G, mode, (uint64_t)val, (uint64_t *)out, kept);
-        prof_end(ps__, (double)n * out_bytes + (double)nb * 5, st);
-    }
+    return PMG_OK;
+}
+
+// The selection from parents P (flattened on the way), masks M and marks.
+static int bcc_select_out(void *out, int out_bytes, const int64_t *shape, int mode, int val, int *P,
+                          const uint8_t *M, const uint8_t *mark, int *err, cudaStream_t st,
+                          unsigned long long *kept)
+{
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    const int ps__ = prof_begin("k_bcc_select", st);
+    if (out_bytes == 1)
+        k_bcc_select<uint8_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(M, P, mark, G, mode, (uint8_t)val,
+                                                                           (uint8_t *)out, kept, err);
+    else
+        k_bcc_select<uint64_t><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(M, P, mark, G, mode, (uint64_t)val,
+                                                                            (uint64_t *)out, kept, err);
+    prof_end(ps__, (double)n * out_bytes + (double)nb * 5, st);
     PMG_CHECK_LAUNCH();
     return PMG_OK;
+}
+
+static int bcc_mark_select(void *out, int out_bytes, const int64_t *shape, const int64_t *inlet_box,
+                           const int64_t *outlet_box, int mode, int val, int *P, const uint8_t *M, uint8_t *mark,
+                           int *err, cudaStream_t st, unsigned long long *kept)
+{
+    PMG_TRY(bcc_marks(shape, inlet_box, outlet_box, P, M, mark, err, st));
+    return bcc_select_out(out, out_bytes, shape, mode, val, P, M, mark, err, st, kept);
+}
+
+template <class Src>
+static int bcc_select_core(const Src &src, void *out, int out_bytes, const int64_t *shape, const int32_t *bc,
+                           const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
+                           int val, int *P, uint8_t *M, uint8_t *mark, int *err, cudaStream_t st,
+                           unsigned long long *kept)
+{
+    PMG_TRY(check_boxes(shape, inlet_box, outlet_box));
+    PMG_TRY(bcc_build(src, shape, bc, pad, true, P, M, err, st, false));
+    return bcc_mark_select(out, out_bytes, shape, inlet_box, outlet_box, mode, val, P, M, mark, err, st, kept);
 }
 
 // Binary selection: P and mark need one int / one byte per 2x2x2 block.  Kept
@@ -1564,6 +1647,292 @@ int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, 
     for (int q = 0; q < 6; q++)
         src.walls |= (bc[q] == PMG_BC_WALL ? 1u : 0u) << q;
     return bcc_select_core(src, out, 1, shape, bc, pad, inlet_box, outlet_box, mode, 1, P, M, mark, err, st, kept);
+}
+
+// ---- selection of a growing set -----------------------------------------------
+// Along a drainage curve two selected sets only ever grow: the eroded pore
+// space (its threshold falls with the radius) and the non-wetting phase (the
+// update turns wetting voxels non-wetting, never back).  Components of a
+// growing set only merge, so after one full block union-find a step re-reads
+// the block masks, lists the blocks whose mask grew, and unites each of them
+// with every touching neighbour; a pair of blocks that starts to touch always
+// has a grown member, and every other block keeps its parent.  The parents
+// keep pointing to smaller indices, so roots stay the smallest block of each
+// component and the flattened parents, marks and selection are those of a
+// full union-find of the same set.
+
+// New masks; a block whose mask changed is listed (warp-aggregated append)
+// and, if it was empty, becomes its own root.  A mask that lost voxels is an
+// error (code 3): the set did not grow.
+template <class Src>
+__global__ void k_grow_masks(Src src, uint8_t *__restrict__ M, int *__restrict__ P, BGrid G, int *list,
+                             int *count, int *err)
+{
+    const int nb = G.b0 * G.b1 * G.b2;
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < nb; base += gridDim.x * blockDim.x) {
+        const int b = base + threadIdx.x;
+        bool changed = false;
+        if (b < nb) {
+            // the old mask and the source are loaded independently
+            const int r = b / G.b2;
+            const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+            const unsigned old = M[b];
+            const unsigned m = block_mask(src, G, c0, c1, c2);
+            if (m != old) {
+                if (old & ~m)
+                    atomicExch(err, 3);
+                M[b] = (uint8_t)m;
+                if (!old)
+                    P[b] = b;
+                changed = true;
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, changed);
+        if (bal) {
+            int pos = 0;
+            if (lane == 0)
+                pos = atomicAdd(count, __popc(bal));
+            pos = __shfl_sync(0xffffffffu, pos, 0);
+            if (changed)
+                list[pos + __popc(bal & ((1u << lane) - 1u))] = b;
+        }
+    }
+}
+
+// Each listed block unites with all touching neighbours (26 directions).  The
+// parents were flattened after the previous step, so a neighbour whose parent
+// equals the block's own starting parent is already in its component and is
+// skipped with one load; every other touching neighbour goes through unite.
+__global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, const int *__restrict__ list,
+                             const int *__restrict__ count, int *err)
+{
+    const int cnt = *count;
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
+        const int b = list[it];
+        const int r = b / G.b2;
+        const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+        const unsigned m = M[b];
+        const int pb = ld(P + b);
+        unsigned todo = 0; // touching neighbours in another component at the start of the step
+#pragma unroll
+        for (int q = 0; q < 26; q++) {
+            if (!(m & c_g_self[q]))
+                continue;
+            const int a0 = c0 + c_g_d[q][0], a1 = c1 + c_g_d[q][1], a2 = c2 + c_g_d[q][2];
+            if (a0 < 0 || a1 < 0 || a2 < 0 || a0 >= G.b0 || a1 >= G.b1 || a2 >= G.b2)
+                continue;
+            const int o = (a0 * G.b1 + a1) * G.b2 + a2;
+            if ((M[o] & c_g_nb[q]) && ld(P + o) != pb)
+                todo |= 1u << q;
+        }
+        while (todo) {
+            const int q = __ffs(todo) - 1;
+            todo &= todo - 1;
+            unite(P, b, ((c0 + c_g_d[q][0]) * G.b1 + c1 + c_g_d[q][1]) * G.b2 + c2 + c_g_d[q][2], err);
+        }
+    }
+}
+
+size_t grow_sel_bytes(const int64_t *shape)
+{
+    const BGrid G = bgrid_of(shape);
+    const size_t nb = (size_t)G.b0 * G.b1 * G.b2;
+    const size_t a = (nb + 255) & ~(size_t)255;
+    return a * 4 + a + a + a * 4 + 256;
+}
+
+void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape)
+{
+    const BGrid G = bgrid_of(shape);
+    const size_t nb = (size_t)G.b0 * G.b1 * G.b2;
+    const size_t a = (nb + 255) & ~(size_t)255;
+    char *p = (char *)mem;
+    g.P = (int *)p;
+    p += a * 4;
+    g.M = (uint8_t *)p;
+    p += a;
+    g.mark = (uint8_t *)p;
+    p += a;
+    g.list = (int *)p;
+    p += a * 4;
+    g.count = (int *)p;
+    g.built = false;
+}
+
+// One step of a growing selection up to the marks: the full block union-find
+// the first time, afterwards the grown blocks only.
+template <class Src>
+static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int32_t *bc, const int32_t *pad,
+                     const int64_t *inlet_box, const int64_t *outlet_box, int *err, cudaStream_t st)
+{
+    PMG_TRY(check_boxes(shape, inlet_box, outlet_box));
+    if (!g.built) {
+        PMG_TRY(bcc_build(src, shape, bc, pad, true, g.P, g.M, err, st, false));
+        g.built = true;
+        return bcc_marks(shape, inlet_box, outlet_box, g.P, g.M, g.mark, err, st);
+    }
+    PMG_TRY(ensure_tables());
+    PMG_TRY(ensure_block_tables());
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    PMG_CUDA(cudaMemsetAsync(g.count, 0, sizeof(int), st));
+    {
+        const int ps__ = prof_begin("k_grow_masks", st);
+        k_grow_masks<Src><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(src, g.M, g.P, G, g.list, g.count, err);
+        prof_end(ps__, (double)n * sizeof(*src_elem(src)) + (double)nb, st);
+    }
+    PMG_CHECK_LAUNCH();
+    {
+        const int ps__ = prof_begin("k_grow_unite", st);
+        k_grow_unite<<<152 * 16, 256, 0, st>>>(g.P, g.M, G, g.list, g.count, err);
+        prof_end(ps__, 0.0, st);
+    }
+    PMG_CHECK_LAUNCH();
+    if (any_periodic(bc)) {
+        const int ps__ = prof_begin("k_bcc_twins", st);
+        k_bcc_twins<<<grid_for(n, 256, 152LL * 32), 256, 0, st>>>(g.M, g.P, G, make_twins(shape, bc, pad), err);
+        prof_end(ps__, 0.0, st);
+        PMG_CHECK_LAUNCH();
+    }
+    return bcc_marks(shape, inlet_box, outlet_box, g.P, g.M, g.mark, err, st);
+}
+
+template <class Src>
+static int grow_select_core(GrowSel &g, const Src &src, void *out, const int64_t *shape, const int32_t *bc,
+                            const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode,
+                            int val, int *err, cudaStream_t st, unsigned long long *kept)
+{
+    PMG_TRY(grow_step(g, src, shape, bc, pad, inlet_box, outlet_box, err, st));
+    return bcc_select_out(out, 1, shape, mode, val, g.P, g.M, g.mark, err, st, kept);
+}
+
+static SrcErode erode_src(const uint16_t *E, int T, const int64_t *shape, const int32_t *bc)
+{
+    SrcErode src;
+    src.E = E;
+    src.T = T;
+    src.s0 = (int)shape[0];
+    src.s1 = (int)shape[1];
+    src.s2 = (int)shape[2];
+    src.walls = 0;
+    for (int q = 0; q < 6; q++)
+        src.walls |= (bc[q] == PMG_BC_WALL ? 1u : 0u) << q;
+    return src;
+}
+
+// Root of block b with its parent flattened to it (-1 for an empty block).
+__device__ __forceinline__ int root_flatten(int *P, int b, int *err)
+{
+    int p = ld(P + b);
+    if (p >= 0 && p != b) {
+        const int q = find_root(P, p, err);
+        if (q != p)
+            P[b] = q;
+        p = q;
+    }
+    return p;
+}
+
+// Inlet selections of two growing sets A and B in one pass: out = 1 where A
+// is inlet-connected and, when *b_count > 0, B is inlet-connected too
+// (porosimetry.py:130-148: img_results kept where n_connected == 1 once the
+// phase exists); kept counts A's inlet-connected voxels before the
+// constraint.  Both parent arrays are flattened on the way.
+__global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, const uint8_t *__restrict__ markA,
+                                   const uint8_t *__restrict__ MB, int *PB, const uint8_t *__restrict__ markB,
+                                   const unsigned long long *__restrict__ b_count, BGrid G,
+                                   uint8_t *__restrict__ out, unsigned long long *kept, int *err)
+{
+    const int nb = G.b0 * G.b1 * G.b2;
+    const bool constrain = *b_count > 0;
+    unsigned int cnt = 0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int r = b / G.b2;
+        const int c2 = b - r * G.b2;
+        const int c0 = r / G.b1;
+        const int c1 = r - c0 * G.b1;
+        unsigned m = MA[b];
+        const unsigned mb = MB[b];
+        if (m) {
+            const int ra = root_flatten(PA, b, err);
+            if (ra < 0 || !(markA[ra] & 1))
+                m = 0;
+        }
+        unsigned keepB = 0;
+        if (mb) {
+            const int rb = root_flatten(PB, b, err);
+            if (rb >= 0 && (markB[rb] & 1))
+                keepB = mb;
+        }
+        cnt += __popc(m);
+        if (constrain)
+            m &= keepB;
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int y = 0; y < 2; y++) {
+                const int i = 2 * c0 + x, j = 2 * c1 + y;
+                if (i >= G.s0 || j >= G.s1)
+                    continue;
+                uint8_t *row = out + ((long long)i * G.s1 + j) * G.s2;
+#pragma unroll
+                for (int z = 0; z < 2; z++) {
+                    const int k = 2 * c2 + z;
+                    if (k < G.s2)
+                        row[k] = (uint8_t)((m >> ((x * 2 + y) * 2 + z)) & 1);
+                }
+            }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt)
+        atomicAdd(kept, (unsigned long long)cnt);
+}
+
+int grow_marks_erode(GrowSel &g, const uint16_t *E, int T, const int64_t *shape, const int32_t *bc,
+                     const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st)
+{
+    return grow_step(g, erode_src(E, T, shape, bc), shape, bc, pad, inlet_box, nullptr, err, st);
+}
+
+int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st)
+{
+    SrcImg src{img, fgval};
+    return grow_step(g, src, shape, bc, pad, inlet_box, nullptr, err, st);
+}
+
+int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
+                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept)
+{
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    const int ps__ = prof_begin("k_grow_pair_select", st);
+    k_grow_pair_select<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(a.M, a.P, a.mark, b.M, b.P, b.mark, b_count,
+                                                                      G, out, kept, err);
+    prof_end(ps__, (double)n + (double)nb * 10, st);
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
+int select_grow_binary(GrowSel &g, const uint8_t *img, int fgval, void *out, const int64_t *shape,
+                       const int32_t *bc, const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box,
+                       int mode, int *err, cudaStream_t st, unsigned long long *kept)
+{
+    SrcImg src{img, fgval};
+    return grow_select_core(g, src, out, shape, bc, pad, inlet_box, outlet_box, mode, fgval >= 0 ? fgval : 1, err,
+                            st, kept);
+}
+
+int select_grow_erode(GrowSel &g, const uint16_t *E, int T, void *out, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *err,
+                      cudaStream_t st, unsigned long long *kept)
+{
+    return grow_select_core(g, erode_src(E, T, shape, bc), out, shape, bc, pad, inlet_box, outlet_box, mode, 1, err,
+                            st, kept);
 }
 
 // ---- binary labelling on blocks -----------------------------------------------

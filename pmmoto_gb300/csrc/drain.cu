@@ -222,7 +222,7 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
                            double r_e, int cmp_e, double r_d, int cmp_d, int inlet, const uint8_t *mp,
                            const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d,
                            const float *De = nullptr, const uint16_t *KC = nullptr, int Te = -1,
-                           bool m1_counted = false)
+                           bool m1_counted = false, GrowSel *g_er = nullptr, GrowSel *g_nw = nullptr)
 {
     // m1_counted: w.cnt[1] already holds count(mp == 1) (the drainage update
     // counts it); the inlet selection counts its kept voxels into w.cnt[0], and
@@ -234,9 +234,30 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
     morph_split(w, shape, bc, ext_e, E, A, B);
     uint8_t *cur = w.t1;
     PMG_CUDA(cudaMemsetAsync(w.cnt, 0, sizeof(unsigned long long), st));
+    if (g_er && g_nw && KC && inlet && mp && m1_counted) {
+        // both selections grow along the curve: one pass writes the eroded
+        // inlet-connected space constrained by the inlet-connected
+        // non-wetting phase (when that phase exists, counted in w.cnt[1])
+        PMG_TRY(grow_marks_erode(*g_er, KC, Te, shape, bc, pad, Bx.inlet, w.err, st));
+        PMG_TRY(grow_marks_binary(*g_nw, mp, 1, shape, bc, pad, Bx.inlet, w.err, st));
+        PMG_TRY(grow_pair_select(*g_er, *g_nw, w.cnt + 1, w.t2, shape, w.err, st, w.cnt));
+        unsigned long long c1 = 0;
+        PMG_CUDA(cudaMemcpyAsync(&c1, w.cnt, sizeof(c1), cudaMemcpyDeviceToHost, st));
+        PMG_CUDA(cudaStreamSynchronize(st));
+        if (c1 == 0) {
+            PMG_CUDA(cudaMemsetAsync(out, 0, (size_t)n, st));
+            return PMG_OK;
+        }
+        morph_split(w, shape, bc, ext_d, E, A, B);
+        return morph_run(w.t2, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st, ball_d);
+    }
     if (KC && inlet) {
-        PMG_TRY(select_run_erode(KC, Te, w.t2, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, w.P, w.M, w.mark,
-                                 w.err, st, w.cnt));
+        if (g_er)
+            PMG_TRY(select_grow_erode(*g_er, KC, Te, w.t2, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, w.err,
+                                      st, w.cnt));
+        else
+            PMG_TRY(select_run_erode(KC, Te, w.t2, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, w.P, w.M,
+                                     w.mark, w.err, st, w.cnt));
         cur = w.t2;
     } else if (De) {
         ErodeThr T;
@@ -276,8 +297,12 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
             if (m1 < 0)
                 PMG_TRY(count_sync(mp, shape, all, 1, w, st, m1));
             if (m1 > 0) {
-                PMG_TRY(select_run_binary(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1, w.P,
-                                          w.M, w.mark, w.err, st));
+                if (g_nw)
+                    PMG_TRY(select_grow_binary(*g_nw, mp, 1, w.t3, shape, bc, pad, Bx.inlet, nullptr,
+                                               PMG_SEL_INLET, w.err, st));
+                else
+                    PMG_TRY(select_run_binary(mp, w.t3, 1, shape, bc, pad, Bx.inlet, nullptr, PMG_SEL_INLET, 1,
+                                              w.P, w.M, w.mark, w.err, st));
                 {
                     const int ps__ = prof_begin("k_constrain", st);
                     k_constrain<<<grid_for(n / 16 + 1, 256, 152LL * 32), 256, 0, st>>>(cur, w.t3, n);
@@ -467,6 +492,28 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
             s = erosion_edt_run(pm_img, De, shape, bc, pad, res, unit_res, E, A, st);
         }
     }
+    // The non-wetting phase only grows along the curve, and so does the eroded
+    // pore space when the thresholds of the active radii never rise: both
+    // selections keep their block union-find from one radius to the next.
+    GrowSel g_er, g_nw;
+    bool grow_er = KC != nullptr;
+    {
+        int last = INT_MAX;
+        for (int k = 0; k < n_radii && grow_er; k++)
+            if (active[k]) {
+                grow_er = Te[(size_t)k] <= last;
+                last = Te[(size_t)k];
+            }
+    }
+    void *grow_mem = nullptr;
+    const size_t gb = grow_sel_bytes(shape);
+    if (s == PMG_OK)
+        s = scratch_alloc(&grow_mem, gb * (grow_er ? 2 : 1), st);
+    if (s == PMG_OK) {
+        grow_sel_init(g_nw, grow_mem, shape);
+        if (grow_er)
+            grow_sel_init(g_er, (char *)grow_mem + gb, shape);
+    }
     if (s == PMG_OK)
         s = scratch_alloc((void **)&morph, (size_t)n, st);
     if (s == PMG_OK)
@@ -492,7 +539,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext_d, res, radii[k], 1, radii_dilate[k], 1, 1,
                                 mp_img,
                                 Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
-                                De, KC, Te[(size_t)k], true);
+                                De, KC, Te[(size_t)k], true, grow_er ? &g_er : nullptr, &g_nw);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
@@ -523,6 +570,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
         for (int k = 0; k < n_radii; k++)
             counts[k] = (int64_t)h[(size_t)k];
     }
+    scratch_free(grow_mem, st);
     scratch_free(De, st);
     scratch_free(KC, st);
     scratch_free(morph, st);

@@ -27,6 +27,35 @@ int select_run_binary(const uint8_t *img, void *out, int out_bytes, const int64_
 int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, const int32_t *bc,
                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *P,
                      uint8_t *M, uint8_t *mark, int *err, cudaStream_t st, unsigned long long *kept = nullptr);
+
+// Selection of a set that only grows from one call to the next (same shape,
+// boundaries and boxes): the block union-find is kept and only blocks whose
+// mask grew are united again.  Scratch of grow_sel_bytes(shape) bytes.
+struct GrowSel {
+    int *P = nullptr;
+    uint8_t *M = nullptr;
+    uint8_t *mark = nullptr;
+    int *list = nullptr;
+    int *count = nullptr;
+    bool built = false;
+};
+size_t grow_sel_bytes(const int64_t *shape);
+void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape);
+int select_grow_binary(GrowSel &g, const uint8_t *img, int fgval, void *out, const int64_t *shape,
+                       const int32_t *bc, const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box,
+                       int mode, int *err, cudaStream_t st, unsigned long long *kept = nullptr);
+int select_grow_erode(GrowSel &g, const uint16_t *E, int T, void *out, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *err,
+                      cudaStream_t st, unsigned long long *kept = nullptr);
+// The step of a growing selection up to the inlet marks (no output) ...
+int grow_marks_erode(GrowSel &g, const uint16_t *E, int T, const int64_t *shape, const int32_t *bc,
+                     const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
+int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,
+                      const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
+// ... and the inlet selection of a constrained by b (when *b_count > 0) in one
+// pass; kept counts a's inlet-connected voxels.
+int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
+                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 

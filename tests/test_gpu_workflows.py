@@ -108,6 +108,32 @@ def test_drainage_random_vs_oracle(P, seed):
     np.testing.assert_array_equal(mp.img, want_img)
 
 
+@pytest.mark.parametrize("case", ["many_radii", "unsorted_array", "periodic"])
+def test_drainage_growing_selections_vs_oracle(P, case):
+    """Many radii: the eroded space and the non-wetting phase keep their
+    block union-find from radius to radius; an unsorted pressure array (the
+    reference sorts lists only) makes the erosion thresholds rise and fall."""
+    rng = np.random.default_rng({"many_radii": 71, "unsorted_array": 72, "periodic": 73}[case])
+    vox = (64, 48, 40)
+    box = tuple((0.0, v / 32) for v in vox)
+    bts = (("end", "end"), ("wall", "wall"), ("wall", "wall"))
+    if case == "periodic":
+        bts = (("end", "end"), ("periodic", "periodic"), ("periodic", "periodic"))
+    inlet, outlet = ((True, False), (False, False), (False, False)), ((False, True), (False, False), (False, False))
+    sd = P.initialize(vox, box=box, boundary_types=bts, inlet=inlet, outlet=outlet)
+    g = O.Geom(vox, boundary_types=bts, box=box, inlet=inlet, outlet=outlet)
+    sph = np.c_[rng.random((260, 3)) * np.array([b[1] for b in box]), rng.uniform(0.03, 0.12, 260)]
+    pm = P.domain_generation.gen_pm_spheres_domain(sd, sph)
+    pcs = sorted(list(2.0 / (np.linspace(1, 9, 17) / 32)))
+    if case == "unsorted_array":
+        pcs = np.array(pcs)[rng.permutation(len(pcs))]
+    mp = P.domain_generation.gen_mp_constant(pm, 2)
+    sat = P.filters.equilibrium_distribution.drainage(mp, pcs, mode="distance")
+    want, want_img = O.drainage(g, pm.img, pcs)
+    np.testing.assert_array_equal(sat, want)
+    np.testing.assert_array_equal(mp.img, want_img)
+
+
 @pytest.mark.parametrize("ci", range(2))
 def test_gen_pm_shape_periodic_images_golden(P, golden, golden_meta, ci):
     """Voxelisation of a sphere list with periodic images (gen_pm_shape)."""
