@@ -1777,13 +1777,15 @@ static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
     const long long n = shape[0] * shape[1] * shape[2];
-    PMG_CUDA(cudaMemsetAsync(g.count, 0, sizeof(int), st));
-    {
+    if (g.pending) {
+        g.pending = false;
+    } else {
+        PMG_CUDA(cudaMemsetAsync(g.count, 0, sizeof(int), st));
         const int ps__ = prof_begin("k_grow_masks", st);
         k_grow_masks<Src><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(src, g.M, g.P, G, g.list, g.count, err);
         prof_end(ps__, (double)n * sizeof(*src_elem(src)) + (double)nb, st);
+        PMG_CHECK_LAUNCH();
     }
-    PMG_CHECK_LAUNCH();
     {
         const int ps__ = prof_begin("k_grow_unite", st);
         k_grow_unite<<<152 * 16, 256, 0, st>>>(g.P, g.M, G, g.list, g.count, err);
@@ -1933,6 +1935,146 @@ int select_grow_erode(GrowSel &g, const uint16_t *E, int T, void *out, const int
 {
     return grow_select_core(g, erode_src(E, T, shape, bc), out, shape, bc, pad, inlet_box, outlet_box, mode, 1, err,
                             st, kept);
+}
+
+int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc, const int32_t *pad,
+                     const int64_t *inlet_box, const int64_t *outlet_box, int *P, uint8_t *M, uint8_t *mark,
+                     int *err, cudaStream_t st)
+{
+    PMG_TRY(check_boxes(shape, inlet_box, outlet_box));
+    SrcImg src{img, fgval};
+    PMG_TRY(bcc_build(src, shape, bc, pad, true, P, M, err, st, false));
+    return bcc_marks(shape, inlet_box, outlet_box, P, M, mark, err, st);
+}
+
+// ---- drainage update on blocks -------------------------------------------------
+// mp = 1 where morph == 1 on a wetting voxel (2) connected to the outlet,
+// reservoir slabs -> 1 (equilibrium_distribution.py:133-179,
+// subdomain_padded.py:285-307), fused with the saturation counts (value 2
+// inside the own box, multiphase.py:56-96; value 1 anywhere).  One thread per
+// 2x2x2 block: the wetting phase's outlet connection comes from its block
+// union-find (outlet mark bit 1), so no selected image is written.  With Mn,
+// the block masks of the non-wetting phase (value 1) are brought up to date
+// and grown blocks are listed for its next growing-selection step.
+__global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ morph, int *Pw,
+                                      const uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
+                                      Boxes B, uint8_t *Mn, int *Pn, int *list, int *count,
+                                      unsigned long long *cnt2, unsigned long long *cnt1, int *err)
+{
+    const int nb = G.b0 * G.b1 * G.b2;
+    const int lane = threadIdx.x & 31;
+    unsigned int c2 = 0, c1 = 0;
+    const bool pairs = !(G.s2 & 1);
+    for (int base = blockIdx.x * blockDim.x; base < nb; base += gridDim.x * blockDim.x) {
+        const int b = base + threadIdx.x;
+        bool changed = false;
+        if (b < nb) {
+            const int r = b / G.b2;
+            const int c2b = b - r * G.b2, c0 = r / G.b1, c1b = r - (r / G.b1) * G.b1;
+            unsigned wet = Mw[b];
+            if (wet) {
+                const int rw = root_flatten(Pw, b, err);
+                if (rw < 0 || !(markw[rw] & 2))
+                    wet = 0;
+            }
+            unsigned nwm = 0;
+#pragma unroll
+            for (int x = 0; x < 2; x++)
+#pragma unroll
+                for (int y = 0; y < 2; y++) {
+                    const int i = 2 * c0 + x, j = 2 * c1b + y;
+                    if (i >= G.s0 || j >= G.s1)
+                        continue;
+                    const long long row = ((long long)i * G.s1 + j) * G.s2;
+                    const bool row_res = i < B.rpad[0] || i >= G.s0 - B.rpad[1] || j < B.rpad[2] ||
+                                         j >= G.s1 - B.rpad[3];
+                    const bool row_own = i >= B.own[0] && i < B.own[1] && j >= B.own[2] && j < B.own[3];
+                    const int k0 = 2 * c2b;
+                    unsigned pv, mv;
+                    if (pairs) {
+                        pv = *(const uint16_t *)(mp + row + k0);
+                        mv = *(const uint16_t *)(morph + row + k0);
+                    } else {
+                        pv = mp[row + k0];
+                        mv = morph[row + k0];
+                        if (k0 + 1 < G.s2) {
+                            pv |= (unsigned)mp[row + k0 + 1] << 8;
+                            mv |= (unsigned)morph[row + k0 + 1] << 8;
+                        }
+                    }
+                    unsigned o = 0;
+#pragma unroll
+                    for (int z = 0; z < 2; z++) {
+                        const int k = k0 + z;
+                        const int bit = (x * 2 + y) * 2 + z;
+                        uint8_t v = (uint8_t)(pv >> (8 * z));
+                        if (((mv >> (8 * z)) & 0xffu) == 1 && ((wet >> bit) & 1))
+                            v = 1;
+                        if (row_res || k < B.rpad[4] || k >= G.s2 - B.rpad[5])
+                            v = 1;
+                        if (k < G.s2) {
+                            c2 += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
+                            c1 += v == 1;
+                            nwm |= (unsigned)(v == 1) << bit;
+                        }
+                        o |= (unsigned)v << (8 * z);
+                    }
+                    if (pairs) {
+                        *(uint16_t *)(mp + row + k0) = (uint16_t)o;
+                    } else {
+                        mp[row + k0] = (uint8_t)o;
+                        if (k0 + 1 < G.s2)
+                            mp[row + k0 + 1] = (uint8_t)(o >> 8);
+                    }
+                }
+            if (Mn) {
+                const unsigned old = Mn[b];
+                if (nwm != old) {
+                    if (old & ~nwm)
+                        atomicExch(err, 3);
+                    Mn[b] = (uint8_t)nwm;
+                    if (!old)
+                        Pn[b] = b;
+                    changed = true;
+                }
+            }
+        }
+        if (Mn) {
+            const unsigned bal = __ballot_sync(0xffffffffu, changed);
+            if (bal) {
+                int pos = 0;
+                if (lane == 0)
+                    pos = atomicAdd(count, __popc(bal));
+                pos = __shfl_sync(0xffffffffu, pos, 0);
+                if (changed)
+                    list[pos + __popc(bal & ((1u << lane) - 1u))] = b;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        c2 += __shfl_down_sync(0xffffffffu, c2, o);
+        c1 += __shfl_down_sync(0xffffffffu, c1, o);
+    }
+    if (lane == 0 && c2)
+        atomicAdd(cnt2, (unsigned long long)c2);
+    if (lane == 0 && c1)
+        atomicAdd(cnt1, (unsigned long long)c1);
+}
+
+int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, const uint8_t *M,
+                        const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
+                        unsigned long long *cnt1, int *err, cudaStream_t st)
+{
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    const int ps__ = prof_begin("k_drain_update_blocks", st);
+    k_drain_update_blocks<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
+        mp, morph, P, M, mark, G, B, g_nw ? g_nw->M : nullptr, g_nw ? g_nw->P : nullptr,
+        g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err);
+    prof_end(ps__, (double)n * 3 + (double)nb * 6, st);
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
 }
 
 // ---- binary labelling on blocks -----------------------------------------------

@@ -17,12 +17,6 @@
 
 namespace pmg {
 
-struct Boxes {
-    int64_t own[6];
-    int64_t inlet[6], outlet[6];
-    int32_t rpad[6];
-};
-
 // Bytes equal to 1 in both words -> 1, else 0 (four voxels per 32-bit word).
 __device__ __forceinline__ uint32_t both_one(uint32_t a, uint32_t b)
 {
@@ -50,68 +44,6 @@ __global__ void k_constrain(uint8_t *res, const uint8_t *__restrict__ nconn, lon
     for (long long i = (nw << 4) + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
         res[i] = (res[i] == 1 && nconn[i] == 1) ? 1 : 0;
-}
-
-// mp = (morph == 1 && w == 2) ? 1 : mp, reservoir slabs -> 1
-// (equilibrium_distribution.py:133-179, subdomain_padded.py:285-307), fused
-// with the saturation count: the updated value is counted when it equals 2
-// inside the own box (count(own == 2), multiphase.py:56-96).  One warp per
-// (i, j) row.  Lanes take two voxels per load when rows start on
-// even addresses.
-__global__ void k_drain_update_count(uint8_t *mp, const uint8_t *__restrict__ morph, const uint8_t *__restrict__ w,
-                                     long long s0, long long s1, long long s2, Boxes B, unsigned long long *cnt,
-                                     unsigned long long *ones)
-{
-    const long long rows = s0 * s1;
-    const int lane = threadIdx.x & 31;
-    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    unsigned int c = 0, c1 = 0; // value 2 in the own box; value 1 anywhere
-    const bool pairs = (s2 & 1) == 0;
-    for (long long r = warp; r < rows; r += nwarps) {
-        const long long i = r / s1, j = r - (r / s1) * s1;
-        const bool row_res = (i < B.rpad[0]) || (i >= s0 - B.rpad[1]) || (j < B.rpad[2]) || (j >= s1 - B.rpad[3]);
-        const bool row_own = i >= B.own[0] && i < B.own[1] && j >= B.own[2] && j < B.own[3];
-        const long long base = r * s2;
-        if (pairs) {
-            const uint16_t *m2 = (const uint16_t *)(morph + base), *w2 = (const uint16_t *)(w + base);
-            uint16_t *p2 = (uint16_t *)(mp + base);
-            for (long long h = lane; h < (s2 >> 1); h += 32) {
-                const uint16_t mv = m2[h], wv = w2[h], pv = p2[h];
-                uint16_t o = 0;
-#pragma unroll
-                for (int b = 0; b < 2; b++) {
-                    const long long k = 2 * h + b;
-                    const uint8_t mb = (uint8_t)(mv >> (8 * b)), wb = (uint8_t)(wv >> (8 * b));
-                    uint8_t v = (mb == 1 && wb == 2) ? (uint8_t)1 : (uint8_t)(pv >> (8 * b));
-                    if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
-                        v = 1;
-                    c += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
-                    c1 += v == 1;
-                    o |= (uint16_t)v << (8 * b);
-                }
-                p2[h] = o;
-            }
-        } else {
-            for (long long k = lane; k < s2; k += 32) {
-                const long long idx = base + k;
-                uint8_t v = (morph[idx] == 1 && w[idx] == 2) ? (uint8_t)1 : mp[idx];
-                if (row_res || k < B.rpad[4] || k >= s2 - B.rpad[5])
-                    v = 1;
-                c += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
-                c1 += v == 1;
-                mp[idx] = v;
-            }
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        c += __shfl_down_sync(0xffffffffu, c, o);
-        c1 += __shfl_down_sync(0xffffffffu, c1, o);
-    }
-    if (lane == 0 && c)
-        atomicAdd(cnt, (unsigned long long)c);
-    if (lane == 0 && c1)
-        atomicAdd(ones, (unsigned long long)c1);
 }
 
 // Erosion by thresholding a precomputed squared EDT (subtraction's
@@ -425,7 +357,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
     Work w{};
     PMG_TRY(work_alloc(w, shape, mb, st));
     PMG_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), st));
-    uint8_t *morph = nullptr, *wet = nullptr;
+    uint8_t *morph = nullptr;
     unsigned long long *d_counts = nullptr;
     // Without periodic axes the erosion's extended image is the same for every
     // radius (no wrap extension), so its EDT is computed once and thresholded
@@ -517,8 +449,6 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
     if (s == PMG_OK)
         s = scratch_alloc((void **)&morph, (size_t)n, st);
     if (s == PMG_OK)
-        s = scratch_alloc((void **)&wet, (size_t)n, st);
-    if (s == PMG_OK)
         s = scratch_alloc((void **)&d_counts, sizeof(unsigned long long) * (size_t)(n_radii + 1), st);
     if (s == PMG_OK)
         s = cudaMemsetAsync(d_counts, 0, sizeof(unsigned long long) * (size_t)(n_radii + 1), st) == cudaSuccess
@@ -545,18 +475,29 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
         }
         if (s != PMG_OK)
             break;
-        s = select_run_binary(mp_img, wet, 1, shape, bc, pad, nullptr, Bx.outlet, PMG_SEL_OUTLET, 2, w.P, w.M,
-                              w.mark, w.err, st);
+        // wetting phase connected to the outlet (its union-find and marks
+        // only), then the update on blocks, which also brings the
+        // non-wetting phase's growing selection up to date
+        s = bcc_marks_binary(mp_img, 2, shape, bc, pad, nullptr, Bx.outlet, w.P, w.M, w.mark, w.err, st);
         if (s != PMG_OK)
             break;
-        {
-            PMG_CUDA(cudaMemsetAsync(w.cnt + 1, 0, sizeof(unsigned long long), st));
-            const int ps__ = prof_begin("k_drain_update_count", st);
-            k_drain_update_count<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
-                mp_img, morph, wet, shape[0], shape[1], shape[2], Bx, d_counts + k, w.cnt + 1);
-            prof_end(ps__, (double)n * 4, st);
+        GrowSel *gn = nullptr;
+        if (g_nw.built) {
+            if (g_nw.pending) {
+                // the last update's list was never consumed: rebuild instead
+                g_nw.built = false;
+                g_nw.pending = false;
+            } else {
+                PMG_CUDA(cudaMemsetAsync(g_nw.count, 0, sizeof(int), st));
+                gn = &g_nw;
+            }
         }
-        PMG_CHECK_LAUNCH();
+        PMG_CUDA(cudaMemsetAsync(w.cnt + 1, 0, sizeof(unsigned long long), st));
+        s = drain_update_blocks(mp_img, morph, shape, w.P, w.M, w.mark, Bx, gn, d_counts + k, w.cnt + 1, w.err, st);
+        if (s != PMG_OK)
+            break;
+        if (gn)
+            g_nw.pending = true;
     }
     // union-find iteration caps are checked once per curve: the status word
     // is only ever set, never cleared, during the sweep
@@ -574,7 +515,6 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
     scratch_free(De, st);
     scratch_free(KC, st);
     scratch_free(morph, st);
-    scratch_free(wet, st);
     scratch_free(d_counts, st);
     int s2 = scratch_free(w.base, st);
     return s != PMG_OK ? s : s2;

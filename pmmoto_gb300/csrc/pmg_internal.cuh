@@ -28,6 +28,14 @@ int select_run_erode(const uint16_t *E, int T, void *out, const int64_t *shape, 
                      const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int mode, int *P,
                      uint8_t *M, uint8_t *mark, int *err, cudaStream_t st, unsigned long long *kept = nullptr);
 
+// Boxes of a drainage run: own voxels, inlet / outlet faces (lo0, hi0, lo1,
+// hi1, lo2, hi2; lo0 < 0 for none), reservoir widths per face.
+struct Boxes {
+    int64_t own[6];
+    int64_t inlet[6], outlet[6];
+    int32_t rpad[6];
+};
+
 // Selection of a set that only grows from one call to the next (same shape,
 // boundaries and boxes): the block union-find is kept and only blocks whose
 // mask grew are united again.  Scratch of grow_sel_bytes(shape) bytes.
@@ -38,6 +46,9 @@ struct GrowSel {
     int *list = nullptr;
     int *count = nullptr;
     bool built = false;
+    // masks already brought up to date and grown blocks listed by the producer
+    // of the set (the drainage update); the next step skips its mask pass
+    bool pending = false;
 };
 size_t grow_sel_bytes(const int64_t *shape);
 void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape);
@@ -56,6 +67,17 @@ int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *
 // pass; kept counts a's inlet-connected voxels.
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
                      const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept);
+// Block union-find of the voxels equal to fgval with inlet / outlet marks,
+// without a selected image (parents left unflattened).
+int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc, const int32_t *pad,
+                     const int64_t *inlet_box, const int64_t *outlet_box, int *P, uint8_t *M, uint8_t *mark,
+                     int *err, cudaStream_t st);
+// The drainage update on blocks, reading the wetting phase's outlet
+// connection from its block union-find (P, M, mark from bcc_marks_binary with
+// the outlet box); maintains g_nw's masks when given.
+int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, const uint8_t *M,
+                        const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
+                        unsigned long long *cnt1, int *err, cudaStream_t st);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 
