@@ -1700,37 +1700,54 @@ __global__ void k_grow_masks(Src src, uint8_t *__restrict__ M, int *__restrict__
     }
 }
 
-// Each listed block unites with all touching neighbours (26 directions).  The
-// parents were flattened after the previous step, so a neighbour whose parent
-// equals the block's own starting parent is already in its component and is
-// skipped with one load; every other touching neighbour goes through unite.
+// Voxels of a block that touch its neighbour at offset (d0, d1, d2): bit
+// (x * 2 + y) * 2 + z, x on the d0 side and so on.
+__device__ __forceinline__ unsigned touch_bits(int d0, int d1, int d2)
+{
+    const unsigned X = d0 < 0 ? 0x0Fu : d0 > 0 ? 0xF0u : 0xFFu;
+    const unsigned Y = d1 < 0 ? 0x33u : d1 > 0 ? 0xCCu : 0xFFu;
+    const unsigned Z = d2 < 0 ? 0x55u : d2 > 0 ? 0xAAu : 0xFFu;
+    return X & Y & Z;
+}
+
+// One warp per listed block, one lane per neighbour (lanes 0-25): every lane
+// loads its neighbour's mask and parent at once.  The parents were flattened
+// after the previous step, so a touching neighbour whose parent equals the
+// block's starting parent is already in its component; of the others, one
+// lane per distinct parent unites (neighbours with one parent are in one
+// component already).
 __global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, const int *__restrict__ list,
                              const int *__restrict__ count, int *err)
 {
     const int cnt = *count;
-    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int q = lane < 13 ? lane : lane + 1; // offset code (d0 + 1) * 9 + (d1 + 1) * 3 + d2 + 1, 13 skipped
+    const int d0 = q / 9 - 1, d1 = (q / 3) % 3 - 1, d2 = q % 3 - 1;
+    const unsigned tself = lane < 26 ? touch_bits(d0, d1, d2) : 0u, tnb = touch_bits(-d0, -d1, -d2);
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long it = warp; it < cnt; it += nwarps) {
         const int b = list[it];
         const int r = b / G.b2;
         const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
         const unsigned m = M[b];
         const int pb = ld(P + b);
-        unsigned todo = 0; // touching neighbours in another component at the start of the step
-#pragma unroll
-        for (int q = 0; q < 26; q++) {
-            if (!(m & c_g_self[q]))
-                continue;
-            const int a0 = c0 + c_g_d[q][0], a1 = c1 + c_g_d[q][1], a2 = c2 + c_g_d[q][2];
-            if (a0 < 0 || a1 < 0 || a2 < 0 || a0 >= G.b0 || a1 >= G.b1 || a2 >= G.b2)
-                continue;
-            const int o = (a0 * G.b1 + a1) * G.b2 + a2;
-            if ((M[o] & c_g_nb[q]) && ld(P + o) != pb)
-                todo |= 1u << q;
+        const int a0 = c0 + d0, a1 = c1 + d1, a2 = c2 + d2;
+        const bool valid = (m & tself) && a0 >= 0 && a1 >= 0 && a2 >= 0 && a0 < G.b0 && a1 < G.b1 && a2 < G.b2;
+        const int o = (a0 * G.b1 + a1) * G.b2 + a2;
+        unsigned mo = 0;
+        int po = -1;
+        if (valid) {
+            mo = M[o];
+            po = ld(P + o);
         }
-        while (todo) {
-            const int q = __ffs(todo) - 1;
-            todo &= todo - 1;
-            unite(P, b, ((c0 + c_g_d[q][0]) * G.b1 + c1 + c_g_d[q][1]) * G.b2 + c2 + c_g_d[q][2], err);
-        }
+        const bool need = (mo & tnb) && po != pb;
+        const unsigned needs = __ballot_sync(0xffffffffu, need);
+        if (!needs)
+            continue;
+        const unsigned same = __match_any_sync(0xffffffffu, need ? po : -2 - lane);
+        if (need && (__ffs(same & needs) - 1) == lane)
+            unite(P, b, o, err);
     }
 }
 
@@ -1788,7 +1805,7 @@ static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int
     }
     {
         const int ps__ = prof_begin("k_grow_unite", st);
-        k_grow_unite<<<152 * 16, 256, 0, st>>>(g.P, g.M, G, g.list, g.count, err);
+        k_grow_unite<<<152 * 32, 256, 0, st>>>(g.P, g.M, G, g.list, g.count, err);
         prof_end(ps__, 0.0, st);
     }
     PMG_CHECK_LAUNCH();
@@ -1956,6 +1973,23 @@ int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const 
 // union-find (outlet mark bit 1), so no selected image is written.  With Mn,
 // the block masks of the non-wetting phase (value 1) are brought up to date
 // and grown blocks are listed for its next growing-selection step.
+// two consecutive coordinates v0, v0 + 1 inside [lo, hi): bits 0, 1
+__device__ __forceinline__ unsigned in2(int v0, long long lo, long long hi)
+{
+    return (unsigned)(v0 >= lo && v0 < hi) | ((unsigned)(v0 + 1 >= lo && v0 + 1 < hi) << 1);
+}
+
+// per-axis 2-bit masks spread over the block's bit layout (x * 2 + y) * 2 + z
+__device__ __forceinline__ unsigned spread_x(unsigned a) { return (a & 1 ? 0x0Fu : 0u) | (a & 2 ? 0xF0u : 0u); }
+__device__ __forceinline__ unsigned spread_y(unsigned a) { return (a & 1 ? 0x33u : 0u) | (a & 2 ? 0xCCu : 0u); }
+__device__ __forceinline__ unsigned spread_z(unsigned a) { return (a & 1 ? 0x55u : 0u) | (a & 2 ? 0xAAu : 0u); }
+
+// bytes 0 and 1 of a 16-bit pair equal to v: bits 0, 1
+__device__ __forceinline__ unsigned eq2(unsigned pair, unsigned v)
+{
+    return (unsigned)((pair & 0xffu) == v) | ((unsigned)((pair >> 8) == v) << 1);
+}
+
 __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ morph, int *Pw,
                                       const uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
                                       Boxes B, uint8_t *Mn, int *Pn, int *list, int *count,
@@ -1965,68 +1999,78 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
     const int lane = threadIdx.x & 31;
     unsigned int c2 = 0, c1 = 0;
     const bool pairs = !(G.s2 & 1);
+    const long long sx = (long long)G.s1 * G.s2, sy = G.s2;
     for (int base = blockIdx.x * blockDim.x; base < nb; base += gridDim.x * blockDim.x) {
         const int b = base + threadIdx.x;
         bool changed = false;
         if (b < nb) {
             const int r = b / G.b2;
             const int c2b = b - r * G.b2, c0 = r / G.b1, c1b = r - (r / G.b1) * G.b1;
+            const int i0 = 2 * c0, j0 = 2 * c1b, k0 = 2 * c2b;
+            // voxels inside the volume, the own box and the reservoir slabs
+            const unsigned vK = in2(k0, 0, G.s2);
+            const unsigned vol = spread_x(in2(i0, 0, G.s0)) & spread_y(in2(j0, 0, G.s1)) & spread_z(vK);
+            const unsigned own = spread_x(in2(i0, B.own[0], B.own[1])) & spread_y(in2(j0, B.own[2], B.own[3])) &
+                                 spread_z(in2(k0, B.own[4], B.own[5]));
+            const unsigned res = (spread_x(~in2(i0, B.rpad[0], (long long)G.s0 - B.rpad[1]) & 3u) |
+                                  spread_y(~in2(j0, B.rpad[2], (long long)G.s1 - B.rpad[3]) & 3u) |
+                                  spread_z(~in2(k0, B.rpad[4], (long long)G.s2 - B.rpad[5]) & 3u)) &
+                                 vol;
             unsigned wet = Mw[b];
             if (wet) {
                 const int rw = root_flatten(Pw, b, err);
                 if (rw < 0 || !(markw[rw] & 2))
                     wet = 0;
             }
-            unsigned nwm = 0;
+            // the four rows of the block: old values and the morph == 1 bits
+            const long long base0 = (long long)i0 * sx + (long long)j0 * sy + k0;
+            unsigned pv[4], m1 = 0, is1 = 0;
 #pragma unroll
-            for (int x = 0; x < 2; x++)
-#pragma unroll
-                for (int y = 0; y < 2; y++) {
-                    const int i = 2 * c0 + x, j = 2 * c1b + y;
-                    if (i >= G.s0 || j >= G.s1)
-                        continue;
-                    const long long row = ((long long)i * G.s1 + j) * G.s2;
-                    const bool row_res = i < B.rpad[0] || i >= G.s0 - B.rpad[1] || j < B.rpad[2] ||
-                                         j >= G.s1 - B.rpad[3];
-                    const bool row_own = i >= B.own[0] && i < B.own[1] && j >= B.own[2] && j < B.own[3];
-                    const int k0 = 2 * c2b;
-                    unsigned pv, mv;
+            for (int t = 0; t < 4; t++) {
+                const int x = t >> 1, y = t & 1;
+                pv[t] = 0;
+                unsigned mv = 0;
+                if ((vol >> (2 * t)) & 3u) {
+                    const long long a = base0 + x * sx + y * sy;
                     if (pairs) {
-                        pv = *(const uint16_t *)(mp + row + k0);
-                        mv = *(const uint16_t *)(morph + row + k0);
+                        pv[t] = *(const uint16_t *)(mp + a);
+                        mv = *(const uint16_t *)(morph + a);
                     } else {
-                        pv = mp[row + k0];
-                        mv = morph[row + k0];
-                        if (k0 + 1 < G.s2) {
-                            pv |= (unsigned)mp[row + k0 + 1] << 8;
-                            mv |= (unsigned)morph[row + k0 + 1] << 8;
+                        pv[t] = mp[a];
+                        mv = morph[a];
+                        if (vK & 2u) {
+                            pv[t] |= (unsigned)mp[a + 1] << 8;
+                            mv |= (unsigned)morph[a + 1] << 8;
                         }
-                    }
-                    unsigned o = 0;
-#pragma unroll
-                    for (int z = 0; z < 2; z++) {
-                        const int k = k0 + z;
-                        const int bit = (x * 2 + y) * 2 + z;
-                        uint8_t v = (uint8_t)(pv >> (8 * z));
-                        if (((mv >> (8 * z)) & 0xffu) == 1 && ((wet >> bit) & 1))
-                            v = 1;
-                        if (row_res || k < B.rpad[4] || k >= G.s2 - B.rpad[5])
-                            v = 1;
-                        if (k < G.s2) {
-                            c2 += (v == 2 && row_own && k >= B.own[4] && k < B.own[5]);
-                            c1 += v == 1;
-                            nwm |= (unsigned)(v == 1) << bit;
-                        }
-                        o |= (unsigned)v << (8 * z);
-                    }
-                    if (pairs) {
-                        *(uint16_t *)(mp + row + k0) = (uint16_t)o;
-                    } else {
-                        mp[row + k0] = (uint8_t)o;
-                        if (k0 + 1 < G.s2)
-                            mp[row + k0 + 1] = (uint8_t)(o >> 8);
                     }
                 }
+                m1 |= eq2(mv, 1) << (2 * t);
+                is1 |= eq2(pv[t], 1) << (2 * t);
+            }
+            // voxels set to 1: invaded wetting voxels and reservoir slabs
+            const unsigned set1 = ((m1 & wet) | res) & vol;
+            unsigned is2 = 0;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const unsigned bits = (set1 >> (2 * t)) & 3u;
+                if (bits) {
+                    const unsigned bm = (bits & 1u ? 0x00ffu : 0u) | (bits & 2u ? 0xff00u : 0u);
+                    pv[t] = (pv[t] & ~bm) | (0x0101u & bm);
+                    const long long a = base0 + (t >> 1) * sx + (t & 1) * sy;
+                    if (pairs) {
+                        *(uint16_t *)(mp + a) = (uint16_t)pv[t];
+                    } else {
+                        if (bits & 1u)
+                            mp[a] = 1;
+                        if (bits & 2u)
+                            mp[a + 1] = 1;
+                    }
+                }
+                is2 |= eq2(pv[t], 2) << (2 * t);
+            }
+            const unsigned nwm = (is1 | set1) & vol;
+            c2 += __popc(is2 & own & vol);
+            c1 += __popc(nwm);
             if (Mn) {
                 const unsigned old = Mn[b];
                 if (nwm != old) {
