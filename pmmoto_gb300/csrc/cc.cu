@@ -1095,6 +1095,19 @@ struct SrcErode {
     }
 };
 
+// ... or the voxels whose step (the first step at which they belong to a
+// growing set, 255 for never) is at most k.
+struct SrcStep {
+    const uint8_t *S;
+    int k;
+    __device__ __forceinline__ bool fg(long long idx, int, int, int) const { return (int)S[idx] <= k; }
+    __device__ __forceinline__ unsigned fg2(long long idx, int, int, int) const
+    {
+        const unsigned v = *(const uint16_t *)(S + idx);
+        return (unsigned)((int)(v & 0xffu) <= k) | ((unsigned)((int)(v >> 8) <= k) << 1);
+    }
+};
+
 // Mask of block (c0, c1, c2): bit (x * 2 + y) * 2 + z for a foreground voxel
 // (2 c0 + x, 2 c1 + y, 2 c2 + z) inside the volume.
 template <class Src>
@@ -1477,6 +1490,7 @@ __global__ void k_bcc_select(const uint8_t *__restrict__ M, int *P, const uint8_
 
 __host__ __device__ inline const uint8_t *src_elem(const SrcImg &s) { return s.img; }
 __host__ __device__ inline const uint16_t *src_elem(const SrcErode &s) { return s.E; }
+__host__ __device__ inline const uint8_t *src_elem(const SrcStep &s) { return s.S; }
 
 static BGrid bgrid_of(const int64_t *shape)
 {
@@ -1717,9 +1731,15 @@ __device__ __forceinline__ unsigned touch_bits(int d0, int d1, int d2)
 // lane per distinct parent unites (neighbours with one parent are in one
 // component already).
 __global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, const int *__restrict__ list,
-                             const int *__restrict__ count, int *err)
+                             const int *__restrict__ count, const int *__restrict__ off, int *err)
 {
-    const int cnt = *count;
+    int cnt;
+    if (off) {
+        list += off[0];
+        cnt = off[1] - off[0];
+    } else {
+        cnt = *count;
+    }
     const int lane = threadIdx.x & 31;
     const int q = lane < 13 ? lane : lane + 1; // offset code (d0 + 1) * 9 + (d1 + 1) * 3 + d2 + 1, 13 skipped
     const int d0 = q / 9 - 1, d1 = (q / 3) % 3 - 1, d2 = q % 3 - 1;
@@ -1779,9 +1799,30 @@ void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape)
 
 // One step of a growing selection up to the marks: the full block union-find
 // the first time, afterwards the grown blocks only.
+// Listed blocks take their masks from the source (steps known in advance).
+template <class Src>
+__global__ void k_grow_apply(Src src, uint8_t *__restrict__ M, int *__restrict__ P, BGrid G,
+                             const int *__restrict__ list, const int *__restrict__ off, int *err)
+{
+    const int a = off[0], cnt = off[1] - a;
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
+        const int b = list[a + it];
+        const int r = b / G.b2;
+        const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+        const unsigned old = M[b];
+        const unsigned m = block_mask(src, G, c0, c1, c2);
+        if (old & ~m)
+            atomicExch(err, 3);
+        M[b] = (uint8_t)m;
+        if (!old)
+            P[b] = b;
+    }
+}
+
 template <class Src>
 static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int32_t *bc, const int32_t *pad,
-                     const int64_t *inlet_box, const int64_t *outlet_box, int *err, cudaStream_t st)
+                     const int64_t *inlet_box, const int64_t *outlet_box, int *err, cudaStream_t st,
+                     const int *off = nullptr)
 {
     PMG_TRY(check_boxes(shape, inlet_box, outlet_box));
     if (!g.built) {
@@ -1794,7 +1835,12 @@ static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
     const long long n = shape[0] * shape[1] * shape[2];
-    if (g.pending) {
+    if (off) {
+        const int ps__ = prof_begin("k_grow_apply", st);
+        k_grow_apply<Src><<<152 * 8, 256, 0, st>>>(src, g.M, g.P, G, g.ev, off, err);
+        prof_end(ps__, 0.0, st);
+        PMG_CHECK_LAUNCH();
+    } else if (g.pending) {
         g.pending = false;
     } else {
         PMG_CUDA(cudaMemsetAsync(g.count, 0, sizeof(int), st));
@@ -1805,7 +1851,7 @@ static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int
     }
     {
         const int ps__ = prof_begin("k_grow_unite", st);
-        k_grow_unite<<<152 * 32, 256, 0, st>>>(g.P, g.M, G, g.list, g.count, err);
+        k_grow_unite<<<152 * 32, 256, 0, st>>>(g.P, g.M, G, off ? g.ev : g.list, g.count, off, err);
         prof_end(ps__, 0.0, st);
     }
     PMG_CHECK_LAUNCH();
@@ -1914,6 +1960,192 @@ int grow_marks_erode(GrowSel &g, const uint16_t *E, int T, const int64_t *shape,
                      const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st)
 {
     return grow_step(g, erode_src(E, T, shape, bc), shape, bc, pad, inlet_box, nullptr, err, st);
+}
+
+int grow_marks_step(GrowSel &g, const uint8_t *S, int k, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st)
+{
+    SrcStep src{S, k};
+    return grow_step(g, src, shape, bc, pad, inlet_box, nullptr, err, st, g.ev ? g.off + k : nullptr);
+}
+
+// Step values (255 outside the volume) of the eight voxels of a block, byte
+// (x * 2 + y) * 2 + z of the result.
+__device__ __forceinline__ unsigned long long block_steps(const uint8_t *S, const BGrid &G, int c0, int c1, int c2)
+{
+    unsigned long long v = ~0ull;
+#pragma unroll
+    for (int x = 0; x < 2; x++)
+#pragma unroll
+        for (int y = 0; y < 2; y++) {
+            const int i = 2 * c0 + x, j = 2 * c1 + y, k = 2 * c2;
+            if (i >= G.s0 || j >= G.s1)
+                continue;
+            const long long a = ((long long)i * G.s1 + j) * G.s2 + k;
+            unsigned pair;
+            if (!(G.s2 & 1))
+                pair = *(const uint16_t *)(S + a);
+            else
+                pair = S[a] | (k + 1 < G.s2 ? (unsigned)S[a + 1] << 8 : 0xff00u);
+            const int sh = 8 * ((x * 2 + y) * 2);
+            v = (v & ~(0xffffull << sh)) | ((unsigned long long)pair << sh);
+        }
+    return v;
+}
+
+// Distinct steps < nsteps among a block's eight voxels, packed in the low
+// bytes of the result; their number in nd.
+__device__ __forceinline__ unsigned long long distinct_steps(unsigned long long v, int nsteps, int &nd)
+{
+    unsigned long long d = 0;
+    nd = 0;
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+        const int x = (int)((v >> (8 * e)) & 0xffu);
+        bool fresh = x < nsteps;
+#pragma unroll
+        for (int f = 0; f < e; f++)
+            fresh = fresh && x != (int)((v >> (8 * f)) & 0xffu);
+        if (fresh) {
+            d |= (unsigned long long)x << (8 * nd);
+            nd++;
+        }
+    }
+    return d;
+}
+
+// Per-step counters live 32 ints apart (separate cache lines, separate L2
+// slices).
+constexpr int kStepStride = 32;
+
+// Events (block, step) for every distinct step of a block: counted per step
+// in shared memory, then added to the global counters once per CTA.
+__global__ void k_step_count(const uint8_t *__restrict__ S, BGrid G, int nsteps, int *cnt)
+{
+    __shared__ int hist[256];
+    for (int v = threadIdx.x; v < 256; v += blockDim.x)
+        hist[v] = 0;
+    __syncthreads();
+    const int nb = G.b0 * G.b1 * G.b2;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int r = b / G.b2;
+        int nd;
+        const unsigned long long d =
+            distinct_steps(block_steps(S, G, r / G.b1, r - (r / G.b1) * G.b1, b - r * G.b2), nsteps, nd);
+        for (int e = 0; e < nd; e++)
+            atomicAdd(&hist[(d >> (8 * e)) & 0xffu], 1);
+    }
+    __syncthreads();
+    for (int v = threadIdx.x; v < nsteps; v += blockDim.x)
+        if (hist[v])
+            atomicAdd(cnt + v * kStepStride, hist[v]);
+}
+
+// The events written at per-step cursors: each round of blockDim.x blocks
+// counts its events per step in shared memory, reserves one range per step
+// with a single global atomic, then writes them.
+__global__ void k_step_scatter(const uint8_t *__restrict__ S, BGrid G, int nsteps, int *cursor, int *__restrict__ ev)
+{
+    __shared__ int hist[256];
+    __shared__ int sbase[256];
+    for (int v = threadIdx.x; v < 256; v += blockDim.x)
+        hist[v] = 0;
+    __syncthreads();
+    const int nb = G.b0 * G.b1 * G.b2;
+    for (int base = blockIdx.x * blockDim.x; base < nb; base += gridDim.x * blockDim.x) {
+        const int b = base + threadIdx.x;
+        int nd = 0;
+        unsigned long long d = 0;
+        int loc[8];
+        if (b < nb) {
+            const int r = b / G.b2;
+            d = distinct_steps(block_steps(S, G, r / G.b1, r - (r / G.b1) * G.b1, b - r * G.b2), nsteps, nd);
+        }
+#pragma unroll
+        for (int e = 0; e < 8; e++)
+            loc[e] = e < nd ? atomicAdd(&hist[(d >> (8 * e)) & 0xffu], 1) : 0;
+        __syncthreads();
+        for (int v = threadIdx.x; v < nsteps; v += blockDim.x) {
+            sbase[v] = hist[v] ? atomicAdd(cursor + v * kStepStride, hist[v]) : 0;
+            hist[v] = 0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < 8; e++)
+            if (e < nd)
+                ev[sbase[(d >> (8 * e)) & 0xffu] + loc[e]] = b;
+    }
+}
+
+int step_lists_build(GrowSel &g, const uint8_t *S, const int64_t *shape, int nsteps, void **mem, cudaStream_t st)
+{
+    *mem = nullptr;
+    if (nsteps <= 0 || nsteps > 255) {
+        set_error("step lists: %d steps outside [1, 255]", nsteps);
+        return PMG_EINVAL;
+    }
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    int *tmp = nullptr;
+    const size_t tmpb = sizeof(int) * (size_t)kStepStride * 256;
+    PMG_TRY(scratch_alloc((void **)&tmp, tmpb, st));
+    int s = cudaMemsetAsync(tmp, 0, tmpb, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    if (s == PMG_OK) {
+        const int ps__ = prof_begin("k_step_count", st);
+        k_step_count<<<grid_for(nb, 256, 152LL * 8), 256, 0, st>>>(S, G, nsteps, tmp);
+        prof_end(ps__, 0.0, st);
+        s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    }
+    std::vector<int> hs((size_t)kStepStride * 256, 0), h((size_t)nsteps + 1, 0);
+    if (s == PMG_OK)
+        s = cudaMemcpyAsync(hs.data(), tmp, tmpb, cudaMemcpyDeviceToHost, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    if (s == PMG_OK)
+        s = cudaStreamSynchronize(st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    for (int k = 0; k < nsteps; k++)
+        h[(size_t)k] = hs[(size_t)k * kStepStride];
+    long long total = 0;
+    for (int k = 0; k <= nsteps && s == PMG_OK; k++) {
+        const int c = k < nsteps ? h[(size_t)k] : 0;
+        h[(size_t)k] = (int)total;
+        total += c;
+    }
+    if (s == PMG_OK && total > 8LL * nb) {
+        set_error("step lists: %lld events for %d blocks", total, nb);
+        s = PMG_EINVAL;
+    }
+    char *m = nullptr;
+    const size_t offb = ((size_t)(nsteps + 1) * sizeof(int) + 255) & ~(size_t)255;
+    if (s == PMG_OK)
+        s = scratch_alloc((void **)&m, offb + sizeof(int) * (size_t)(total > 0 ? total : 1), st);
+    if (s == PMG_OK) {
+        g.off = (int *)m;
+        g.ev = (int *)(m + offb);
+        *mem = m;
+        s = cudaMemcpyAsync(g.off, h.data(), sizeof(int) * (size_t)(nsteps + 1), cudaMemcpyHostToDevice, st) ==
+                    cudaSuccess
+                ? PMG_OK
+                : PMG_ECUDA;
+    }
+    // cursors start at the offsets
+    for (int k = 0; k < nsteps; k++)
+        hs[(size_t)k * kStepStride] = h[(size_t)k];
+    if (s == PMG_OK)
+        s = cudaMemcpyAsync(tmp, hs.data(), tmpb, cudaMemcpyHostToDevice, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    if (s == PMG_OK) {
+        const int ps__ = prof_begin("k_step_scatter", st);
+        k_step_scatter<<<grid_for(nb, 256, 152LL * 8), 256, 0, st>>>(S, G, nsteps, tmp, g.ev);
+        prof_end(ps__, 0.0, st);
+        s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    }
+    // the host offsets must outlive the copies
+    if (s == PMG_OK)
+        s = cudaStreamSynchronize(st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    const int s2 = scratch_free(tmp, st);
+    if (s != PMG_OK) {
+        g.ev = nullptr;
+        g.off = nullptr;
+    }
+    return s != PMG_OK ? s : s2;
 }
 
 int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,

@@ -125,6 +125,35 @@ static int work_alloc(Work &w, const int64_t *shape, size_t morph_bytes, cudaStr
     return PMG_OK;
 }
 
+// Step of every voxel in a growing eroded space: the first radius index whose
+// threshold its capped squared distance exceeds (the thresholds never rise),
+// read from a table over the capped values; wall planes never enter (255).
+// One warp per (i, j) row.
+__global__ void k_step_volume(const uint16_t *__restrict__ KC, uint8_t *__restrict__ S,
+                              const uint8_t *__restrict__ tab, int tmax, long long s0, long long s1, long long s2,
+                              unsigned walls)
+{
+    __shared__ uint8_t s_tab[kCapMaxT + 2];
+    for (int v = threadIdx.x; v <= tmax; v += blockDim.x)
+        s_tab[v] = tab[v];
+    __syncthreads();
+    const long long rows = s0 * s1;
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = warp; r < rows; r += nwarps) {
+        const long long i = r / s1, j = r - (r / s1) * s1;
+        const bool wrow = ((walls & 1u) && i == 0) || ((walls & 2u) && i == s0 - 1) || ((walls & 4u) && j == 0) ||
+                          ((walls & 8u) && j == s1 - 1);
+        const long long base = r * s2;
+        for (long long k = lane; k < s2; k += 32) {
+            const int v = min((int)KC[base + k], tmax);
+            const bool wall = wrow || ((walls & 16u) && k == 0) || ((walls & 32u) && k == s2 - 1);
+            S[base + k] = wall ? (uint8_t)255 : s_tab[v];
+        }
+    }
+}
+
 static void morph_split(Work &w, const int64_t *shape, const int32_t *bc, const int32_t *ext,
                         uint8_t *&E, float *&A, float *&B)
 {
@@ -154,7 +183,8 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
                            double r_e, int cmp_e, double r_d, int cmp_d, int inlet, const uint8_t *mp,
                            const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d,
                            const float *De = nullptr, const uint16_t *KC = nullptr, int Te = -1,
-                           bool m1_counted = false, GrowSel *g_er = nullptr, GrowSel *g_nw = nullptr)
+                           bool m1_counted = false, GrowSel *g_er = nullptr, GrowSel *g_nw = nullptr,
+                           const uint8_t *Sv = nullptr, int step = -1)
 {
     // m1_counted: w.cnt[1] already holds count(mp == 1) (the drainage update
     // counts it); the inlet selection counts its kept voxels into w.cnt[0], and
@@ -166,11 +196,14 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
     morph_split(w, shape, bc, ext_e, E, A, B);
     uint8_t *cur = w.t1;
     PMG_CUDA(cudaMemsetAsync(w.cnt, 0, sizeof(unsigned long long), st));
-    if (g_er && g_nw && KC && inlet && mp && m1_counted) {
+    if (g_er && g_nw && (KC || Sv) && inlet && mp && m1_counted) {
         // both selections grow along the curve: one pass writes the eroded
         // inlet-connected space constrained by the inlet-connected
         // non-wetting phase (when that phase exists, counted in w.cnt[1])
-        PMG_TRY(grow_marks_erode(*g_er, KC, Te, shape, bc, pad, Bx.inlet, w.err, st));
+        if (Sv)
+            PMG_TRY(grow_marks_step(*g_er, Sv, step, shape, bc, pad, Bx.inlet, w.err, st));
+        else
+            PMG_TRY(grow_marks_erode(*g_er, KC, Te, shape, bc, pad, Bx.inlet, w.err, st));
         PMG_TRY(grow_marks_binary(*g_nw, mp, 1, shape, bc, pad, Bx.inlet, w.err, st));
         PMG_TRY(grow_pair_select(*g_er, *g_nw, w.cnt + 1, w.t2, shape, w.err, st, w.cnt));
         unsigned long long c1 = 0;
@@ -376,6 +409,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
     // and each radius's erosion "E > T" is read off it inside the inlet
     // selection -- no eroded image is written.
     uint16_t *KC = nullptr;
+    int Tcap = 0;
     std::vector<int> Te((size_t)n_radii, -1);
     if (reuse_erosion && unit_res >= 0) {
         const float unit[3] = {1.0f, 1.0f, 1.0f};
@@ -384,7 +418,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
         bool ok = r[0] == r[1] && r[1] == r[2];
         for (int d = 0; d < 3 && ok; d++)
             ok = exact_path_ok(r[d], plain, (int)shape[d]);
-        int Tcap = 0;
+        Tcap = 0;
         for (int k = 0; k < n_radii && ok; k++) {
             if (!active[k])
                 continue;
@@ -437,6 +471,43 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
                 last = Te[(size_t)k];
             }
     }
+    // the growing eroded space as one byte per voxel: the radius index at
+    // which the voxel enters (the capped distances are not needed after it)
+    uint8_t *Sv = nullptr;
+    if (s == PMG_OK && grow_er && n_radii <= 254) {
+        std::vector<uint8_t> tab((size_t)Tcap + 2, 255);
+        for (int v = 0; v <= Tcap + 1; v++)
+            for (int k = 0; k < n_radii; k++)
+                if (active[k] && Te[(size_t)k] < v) {
+                    tab[(size_t)v] = (uint8_t)k;
+                    break;
+                }
+        uint8_t *dtab = nullptr;
+        s = scratch_alloc((void **)&Sv, (size_t)n + 256 + tab.size(), st);
+        if (s == PMG_OK) {
+            dtab = Sv + (((size_t)n + 255) & ~(size_t)255);
+            s = cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, st) == cudaSuccess
+                    ? PMG_OK
+                    : PMG_ECUDA;
+        }
+        if (s == PMG_OK) {
+            unsigned walls = 0;
+            for (int q = 0; q < 6; q++)
+                walls |= (bc[q] == PMG_BC_WALL ? 1u : 0u) << q;
+            const int ps__ = prof_begin("k_step_volume", st);
+            k_step_volume<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
+                KC, Sv, dtab, Tcap + 1, shape[0], shape[1], shape[2], walls);
+            prof_end(ps__, (double)n * 3, st);
+            s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            // the host table must outlive the copy
+            if (s == PMG_OK)
+                s = cudaStreamSynchronize(st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        }
+        if (s == PMG_OK) {
+            s = scratch_free(KC, st);
+            KC = nullptr;
+        }
+    }
     void *grow_mem = nullptr;
     const size_t gb = grow_sel_bytes(shape);
     if (s == PMG_OK)
@@ -446,6 +517,10 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
         if (grow_er)
             grow_sel_init(g_er, (char *)grow_mem + gb, shape);
     }
+    // the blocks of the eroded space that grow at each radius, listed once
+    void *lists_mem = nullptr;
+    if (s == PMG_OK && Sv)
+        s = step_lists_build(g_er, Sv, shape, n_radii, &lists_mem, st);
     if (s == PMG_OK)
         s = scratch_alloc((void **)&morph, (size_t)n, st);
     if (s == PMG_OK)
@@ -469,7 +544,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext_d, res, radii[k], 1, radii_dilate[k], 1, 1,
                                 mp_img,
                                 Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
-                                De, KC, Te[(size_t)k], true, grow_er ? &g_er : nullptr, &g_nw);
+                                De, KC, Te[(size_t)k], true, grow_er ? &g_er : nullptr, &g_nw, Sv, k);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
@@ -511,7 +586,9 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
         for (int k = 0; k < n_radii; k++)
             counts[k] = (int64_t)h[(size_t)k];
     }
+    scratch_free(lists_mem, st);
     scratch_free(grow_mem, st);
+    scratch_free(Sv, st);
     scratch_free(De, st);
     scratch_free(KC, st);
     scratch_free(morph, st);

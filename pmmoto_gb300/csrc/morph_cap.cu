@@ -49,64 +49,66 @@ struct RowSrc {
     int wall[6];
 };
 
+// Only distances d <= W = floor(sqrt T) <= 31 give values below T + 1, so a
+// voxel needs the seeds within 31 positions on either side: the row's seeds
+// are first gathered as bit words (one ballot per 32 voxels, kept in shared
+// memory with an empty word on either side), then every lane finds its
+// voxel's nearest seed in the three words around it with one count of
+// leading / trailing zeros each way.
 __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E, uint16_t *__restrict__ KA,
-                                                  long long rows, int X2, int T, RowSrc rs)
+                                                  long long rows, int X2, int T, int W, RowSrc rs)
 {
-    extern __shared__ uint16_t s_dq[];
+    extern __shared__ uint32_t s_zw[];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    uint16_t *dq = s_dq + (threadIdx.x >> 5) * X2;
-    // the row's bytes, staged first with independent loads
-    uint8_t *sb = (uint8_t *)(s_dq + (blockDim.x >> 5) * X2) + (threadIdx.x >> 5) * X2;
+    const int nw = (X2 + 31) >> 5;
+    uint32_t *zw = s_zw + (threadIdx.x >> 5) * (nw + 2) + 1; // zw[-1] and zw[nw] stay 0
+    if (lane == 0) {
+        zw[-1] = 0u;
+        zw[nw] = 0u;
+    }
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const int big = T + 1;
-    const int nc = (X2 + 31) >> 5;
-    const int none = 1 << 20;
     for (long long r = warp; r < rows; r += nwarps) {
         const uint8_t *src = E + r * X2;
+        bool wrow = false;
         if (rs.raw) {
             const long long i = r / rs.X1, j = r - (r / rs.X1) * rs.X1;
-            const bool wrow = (rs.wall[0] && i == 0) || (rs.wall[1] && i == rows / rs.X1 - 1) ||
-                              (rs.wall[2] && j == 0) || (rs.wall[3] && j == rs.X1 - 1);
+            wrow = (rs.wall[0] && i == 0) || (rs.wall[1] && i == rows / rs.X1 - 1) || (rs.wall[2] && j == 0) ||
+                   (rs.wall[3] && j == rs.X1 - 1);
+        }
 #pragma unroll 4
-            for (int x = lane; x < X2; x += 32) {
-                const bool wall = wrow || (rs.wall[4] && x == 0) || (rs.wall[5] && x == X2 - 1);
-                sb[x] = (!wall && src[x] != 0) ? 0 : 1;
+        for (int c = 0; c < nw; c++) {
+            const int x = (c << 5) + lane;
+            bool seed = false;
+            if (x < X2) {
+                const uint8_t v = src[x];
+                if (rs.raw)
+                    seed = v != 0 && !wrow && !(rs.wall[4] && x == 0) && !(rs.wall[5] && x == X2 - 1);
+                else
+                    seed = v == 0;
             }
-        } else {
-#pragma unroll 4
-            for (int x = lane; x < X2; x += 32)
-                sb[x] = src[x];
+            const unsigned zm = __ballot_sync(FULL, seed);
+            if (lane == 0)
+                zw[c] = zm;
         }
         __syncwarp();
-        // backward: distance to the next zero at or after x (65535: none)
-        int nextz = none;
-        for (int c = nc - 1; c >= 0; c--) {
+        uint16_t *dst = KA + r * X2;
+        uint32_t wp = 0u, wc = zw[0];
+        for (int c = 0; c < nw; c++) {
+            const uint32_t wn = zw[c + 1];
             const int x = (c << 5) + lane;
-            const bool z = x < X2 && sb[x] == 0;
-            const unsigned zm = __ballot_sync(FULL, z);
-            const unsigned ge = zm & (FULL << lane);
-            const int q = ge ? (c << 5) + __ffs(ge) - 1 : nextz;
+            // bit t of R: position x + t; bit 31 - t of L: position x - t
+            const uint32_t R = lane ? (wc >> lane) | (wn << (32 - lane)) : wc;
+            const uint32_t L = lane < 31 ? (wc << (31 - lane)) | (wp >> (lane + 1)) : wc;
+            const int dr = R ? __ffs(R) - 1 : 32;
+            const int dl = L ? __clz(L) : 32;
+            const int d = min(dl, dr);
             if (x < X2)
-                dq[x] = (uint16_t)min(q - x, 65535);
-            if (zm)
-                nextz = (c << 5) + __ffs(zm) - 1;
-        }
-        __syncwarp();
-        // forward: distance to the previous zero, combined
-        int prevz = -none;
-        for (int c = 0; c < nc; c++) {
-            const int x = (c << 5) + lane;
-            const int dqx = x < X2 ? dq[x] : 65535;
-            const unsigned zm = __ballot_sync(FULL, x < X2 && dqx == 0);
-            const unsigned le = zm & (lane == 31 ? FULL : ((2u << lane) - 1u));
-            const int p = le ? (c << 5) + 31 - __clz(le) : prevz;
-            const int d = min(x - p, dqx);
-            if (x < X2)
-                KA[r * X2 + x] = (uint16_t)(d >= 32768 ? big : min(d * d, big));
-            if (zm)
-                prevz = (c << 5) + 31 - __clz(zm);
+                dst[x] = (uint16_t)(d <= W ? d * d : big);
+            wp = wc;
+            wc = wn;
         }
         __syncwarp();
     }
@@ -357,11 +359,9 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
     const long long vox = rows * G.X2;
     {
         const int block = 256;
-        const size_t smem = (size_t)(block / 32) * G.X2 * (sizeof(uint16_t) + 1);
-        if (smem > 48 * 1024)
-            PMG_CUDA(cudaFuncSetAttribute(k_cap_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
-        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, rs);
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W, rs);
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();
@@ -402,11 +402,10 @@ int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, cons
     const long long vox = rows * G.X2;
     {
         const int block = 256;
-        const size_t smem = (size_t)(block / 32) * G.X2 * (sizeof(uint16_t) + 1);
-        if (smem > 48 * 1024)
-            PMG_CUDA(cudaFuncSetAttribute(k_cap_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
-        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, RowSrc{});
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W,
+                                                                                RowSrc{});
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();

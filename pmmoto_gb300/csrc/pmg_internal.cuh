@@ -49,7 +49,14 @@ struct GrowSel {
     // masks already brought up to date and grown blocks listed by the producer
     // of the set (the drainage update); the next step skips its mask pass
     bool pending = false;
+    // blocks that grow at each step, known in advance (step_lists_build):
+    // step k's blocks are ev[off[k] .. off[k + 1])
+    int *ev = nullptr;
+    int *off = nullptr;
 };
+// Per-step lists of the blocks of a step volume S (steps < nsteps; 255:
+// never) that grow at that step, in one allocation *mem (freed by the caller).
+int step_lists_build(GrowSel &g, const uint8_t *S, const int64_t *shape, int nsteps, void **mem, cudaStream_t st);
 size_t grow_sel_bytes(const int64_t *shape);
 void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape);
 int select_grow_binary(GrowSel &g, const uint8_t *img, int fgval, void *out, const int64_t *shape,
@@ -63,6 +70,9 @@ int grow_marks_erode(GrowSel &g, const uint16_t *E, int T, const int64_t *shape,
                      const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
 int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,
                       const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
+// (the set: voxels with step S <= k)
+int grow_marks_step(GrowSel &g, const uint8_t *S, int k, const int64_t *shape, const int32_t *bc,
+                    const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
 // ... and the inlet selection of a constrained by b (when *b_count > 0) in one
 // pass; kept counts a's inlet-connected voxels.
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
