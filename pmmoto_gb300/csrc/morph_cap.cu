@@ -78,20 +78,27 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
             wrow = (rs.wall[0] && i == 0) || (rs.wall[1] && i == rows / rs.X1 - 1) || (rs.wall[2] && j == 0) ||
                    (rs.wall[3] && j == rs.X1 - 1);
         }
+        if (wrow) {
+            // a wall row holds no seeds
+            for (int c = lane; c < nw; c += 32)
+                zw[c] = 0u;
+        } else {
+            const uint8_t want = rs.raw ? 0 : 1; // a seed is a voxel != want (raw) or == 0
 #pragma unroll 4
-        for (int c = 0; c < nw; c++) {
-            const int x = (c << 5) + lane;
-            bool seed = false;
-            if (x < X2) {
-                const uint8_t v = src[x];
-                if (rs.raw)
-                    seed = v != 0 && !wrow && !(rs.wall[4] && x == 0) && !(rs.wall[5] && x == X2 - 1);
-                else
-                    seed = v == 0;
+            for (int c = 0; c < nw; c++) {
+                const int x = (c << 5) + lane;
+                const bool seed = x < X2 && ((src[x] == 0) != (want == 0));
+                const unsigned zm = __ballot_sync(FULL, seed);
+                if (lane == 0)
+                    zw[c] = zm;
             }
-            const unsigned zm = __ballot_sync(FULL, seed);
-            if (lane == 0)
-                zw[c] = zm;
+            if (rs.raw && lane == 0) {
+                // wall planes at the row ends hold no seeds
+                if (rs.wall[4])
+                    zw[0] &= ~1u;
+                if (rs.wall[5])
+                    zw[(X2 - 1) >> 5] &= ~(1u << ((X2 - 1) & 31));
+            }
         }
         __syncwarp();
         uint16_t *dst = KA + r * X2;
@@ -100,11 +107,9 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
             const uint32_t wn = zw[c + 1];
             const int x = (c << 5) + lane;
             // bit t of R: position x + t; bit 31 - t of L: position x - t
-            const uint32_t R = lane ? (wc >> lane) | (wn << (32 - lane)) : wc;
-            const uint32_t L = lane < 31 ? (wc << (31 - lane)) | (wp >> (lane + 1)) : wc;
-            const int dr = R ? __ffs(R) - 1 : 32;
-            const int dl = L ? __clz(L) : 32;
-            const int d = min(dl, dr);
+            const uint32_t R = __funnelshift_r(wc, wn, lane);
+            const uint32_t L = __funnelshift_l(wp, wc, 31 - lane);
+            const int d = min(__clz(L), __clz(__brev(R)));
             if (x < X2)
                 dst[x] = (uint16_t)(d <= W ? d * d : big);
             wp = wc;
