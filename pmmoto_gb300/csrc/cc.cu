@@ -2249,11 +2249,6 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                                   spread_z(~in2(k0, B.rpad[4], (long long)G.s2 - B.rpad[5]) & 3u)) &
                                  vol;
             unsigned wet = Mw[b];
-            if (wet) {
-                const int rw = root_flatten(Pw, b, err);
-                if (rw < 0 || !(markw[rw] & 2))
-                    wet = 0;
-            }
             // the four rows of the block: old values and the morph == 1 bits
             const long long base0 = (long long)i0 * sx + (long long)j0 * sy + k0;
             unsigned pv[4], m1 = 0, is1 = 0;
@@ -2278,6 +2273,13 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                 }
                 m1 |= eq2(mv, 1) << (2 * t);
                 is1 |= eq2(pv[t], 1) << (2 * t);
+            }
+            // the wetting phase's outlet connection matters only where the
+            // dilation meets it
+            if (m1 & wet) {
+                const int rw = find_root(Pw, ld(Pw + b), err);
+                if (rw < 0 || !(markw[rw] & 2))
+                    wet = 0;
             }
             // voxels set to 1: invaded wetting voxels and reservoir slabs
             const unsigned set1 = ((m1 & wet) | res) & vol;
