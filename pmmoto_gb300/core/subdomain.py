@@ -84,6 +84,8 @@ class Domain:
 
     def __init__(self, box, boundary_types, inlet, outlet, voxels):
         self.box = tuple(tuple(float(x) for x in b) for b in box)
+        # the box as given (the image writer prints it the way it came)
+        self.box_input = tuple(tuple(b) for b in box)
         self.boundary_types = tuple(tuple(BoundaryType(bt_value(b)) for b in bt) for bt in boundary_types)
         self.inlet = inlet
         self.outlet = outlet

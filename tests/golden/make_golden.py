@@ -264,11 +264,30 @@ def main():
     put("pack_read_domain", np.asarray(dom_r))
     meta["pack_text"] = text
 
+    write_vti(pm)
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **out)
     with open(os.path.join(HERE, "golden_meta.json"), "w") as f:
         json.dump(meta, f, indent=1)
     print("wrote", len(out), "arrays")
 
 
-if __name__ == "__main__":
+def write_vti(pm):
+    """Image-writer fixtures: the reference's save_img output for the seeded
+    cases of vti_cases.py, one .vti file per case under vti/."""
+    import vti_cases
+
+    BT = pm.BoundaryType
+    for name, kw, imgs in vti_cases.cases():
+        kw = dict(kw)
+        if kw.pop("boundary_types", None) == "periodic":
+            kw["boundary_types"] = ((BT.PERIODIC,) * 2,) * 3
+        sd = pm.initialize(**kw)
+        extra = {k: v for k, v in imgs.items() if k != "img"}
+        pm.io.output.save_img(os.path.join(HERE, "vti", name), sd, imgs["img"],
+                              additional_img=extra or None)
+
+
+if __name__ == "__main__" and "--vti-only" in sys.argv:
+    write_vti(refshim.load())
+elif __name__ == "__main__":
     main()
