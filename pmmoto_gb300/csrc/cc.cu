@@ -1144,14 +1144,17 @@ __device__ __forceinline__ unsigned block_mask(const Src &src, const BGrid &G, i
 // block: block masks from the source, then a shared-memory union-find of the
 // tile whose roots are the smallest block index of each tile-local part.
 // Every later step reads the block masks M, never the source again.
+//
+// With Pl, the tile-local parents are also kept in Pl; with dirty (per tile),
+// a tile whose flag is clear has not changed since Pl was written and only
+// copies Pl to P, and every recomputed tile clears its flag.
 template <class Src>
 __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict__ P, uint8_t *__restrict__ M,
-                                                   BGrid G)
+                                                   BGrid G, int *__restrict__ Pl, int *__restrict__ dirty)
 {
     __shared__ uint8_t sm[kTile];
     __shared__ int L[kTile];
     __shared__ BTabs tb;
-    load_btabs(tb);
     const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
     const int tile = blockIdx.x;
     const int ti = tile / (nt1 * nt2), tj = (tile / nt2) % nt1, tk = tile % nt2;
@@ -1159,6 +1162,14 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
     const int a = t / (kT1 * kT2), b = (t / kT2) % kT1, c = t % kT2;
     const int c0 = ti * kT0 + a, c1 = tj * kT1 + b, c2 = tk * kT2 + c;
     const bool inside = c0 < G.b0 && c1 < G.b1 && c2 < G.b2;
+    if (dirty && !dirty[tile]) {
+        if (inside) {
+            const int bidx = (c0 * G.b1 + c1) * G.b2 + c2;
+            P[bidx] = Pl[bidx];
+        }
+        return;
+    }
+    load_btabs(tb);
     const unsigned m = inside ? block_mask(src, G, c0, c1, c2) : 0u;
     sm[t] = (uint8_t)m;
     L[t] = m ? t : -1;
@@ -1208,7 +1219,11 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
             out = ((ti * kT0 + ra) * G.b1 + tj * kT1 + rb) * G.b2 + tk * kT2 + rc;
         }
         P[bidx] = out;
+        if (Pl)
+            Pl[bidx] = out;
     }
+    if (dirty && t == 0)
+        dirty[tile] = 0;
 }
 
 // Phase 2: blocks on a tile border unite with touching earlier neighbours in
@@ -1509,7 +1524,8 @@ static BGrid bgrid_of(const int64_t *shape)
 // component), -1 for empty blocks; M[b] = block mask.
 template <class Src>
 static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, const int32_t *pad, bool twins,
-                     int *P, uint8_t *M, int *err, cudaStream_t st, bool flatten = true)
+                     int *P, uint8_t *M, int *err, cudaStream_t st, bool flatten = true, int *Pl = nullptr,
+                     int *dirty = nullptr)
 {
     PMG_TRY(ensure_tables());
     PMG_TRY(ensure_block_tables());
@@ -1519,7 +1535,7 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
     {
         const int nt = ((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
         const int ps__ = prof_begin("k_bcc_tile", st);
-        k_bcc_tile<Src><<<nt, kTile, 0, st>>>(src, P, M, G);
+        k_bcc_tile<Src><<<nt, kTile, 0, st>>>(src, P, M, G, Pl, dirty);
         prof_end(ps__, (double)n * sizeof(*src_elem(src)) + (double)nb * 5, st);
     }
     PMG_CHECK_LAUNCH();
@@ -2196,6 +2212,57 @@ int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const 
     return bcc_marks(shape, inlet_box, outlet_box, P, M, mark, err, st);
 }
 
+// ---- selection of a shrinking set, tile by tile ---------------------------------
+// The wetting phase of a drainage curve only loses voxels; components can
+// split, so its union-find is rebuilt every step, but the tile phase is local:
+// a tile none of whose voxels changed gives the same tile-local parents as
+// before, kept in Pl.  The producer of the changes (the drainage update)
+// flags the tiles it touched and writes their new block masks.
+
+size_t shrink_sel_bytes(const int64_t *shape)
+{
+    const BGrid G = bgrid_of(shape);
+    const size_t nb = (size_t)G.b0 * G.b1 * G.b2;
+    const size_t a = (nb + 255) & ~(size_t)255;
+    const size_t nt = (size_t)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
+    return a * 4 * 2 + a * 2 + ((nt * 4 + 255) & ~(size_t)255) + 256;
+}
+
+void shrink_sel_init(ShrinkSel &g, void *mem, const int64_t *shape)
+{
+    const BGrid G = bgrid_of(shape);
+    const size_t nb = (size_t)G.b0 * G.b1 * G.b2;
+    const size_t a = (nb + 255) & ~(size_t)255;
+    const size_t nt = (size_t)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
+    char *p = (char *)mem;
+    g.P = (int *)p;
+    p += a * 4;
+    g.Pl = (int *)p;
+    p += a * 4;
+    g.M = (uint8_t *)p;
+    p += a;
+    g.mark = (uint8_t *)p;
+    p += a;
+    g.dirty = (int *)p;
+    g.ntiles = (int)nt;
+    g.built = false;
+}
+
+int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,
+                        const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, bool unchanged,
+                        int *err, cudaStream_t st)
+{
+    PMG_TRY(check_boxes(shape, inlet_box, outlet_box));
+    if (g.built && unchanged)
+        return PMG_OK; // parents, masks and marks of the last step still hold
+    if (!g.built)
+        PMG_CUDA(cudaMemsetAsync(g.dirty, 0, sizeof(int) * (size_t)g.ntiles, st));
+    SrcImg src{img, fgval};
+    PMG_TRY(bcc_build(src, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, g.built ? g.dirty : nullptr));
+    g.built = true;
+    return bcc_marks(shape, inlet_box, outlet_box, g.P, g.M, g.mark, err, st);
+}
+
 // ---- drainage update on blocks -------------------------------------------------
 // mp = 1 where morph == 1 on a wetting voxel (2) connected to the outlet,
 // reservoir slabs -> 1 (equilibrium_distribution.py:133-179,
@@ -2223,9 +2290,10 @@ __device__ __forceinline__ unsigned eq2(unsigned pair, unsigned v)
 }
 
 __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ morph, int *Pw,
-                                      const uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
+                                      uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
                                       Boxes B, uint8_t *Mn, int *Pn, int *list, int *count,
-                                      unsigned long long *cnt2, unsigned long long *cnt1, int *err)
+                                      unsigned long long *cnt2, unsigned long long *cnt1, int *err,
+                                      int *wdirty, unsigned long long *nwdirty)
 {
     const int nb = G.b0 * G.b1 * G.b2;
     const int lane = threadIdx.x & 31;
@@ -2248,7 +2316,8 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                                   spread_y(~in2(j0, B.rpad[2], (long long)G.s1 - B.rpad[3]) & 3u) |
                                   spread_z(~in2(k0, B.rpad[4], (long long)G.s2 - B.rpad[5]) & 3u)) &
                                  vol;
-            unsigned wet = Mw[b];
+            const unsigned wold = Mw[b];
+            unsigned wet = wold;
             // the four rows of the block: old values and the morph == 1 bits
             const long long base0 = (long long)i0 * sx + (long long)j0 * sy + k0;
             unsigned pv[4], m1 = 0, is1 = 0;
@@ -2303,6 +2372,14 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                 is2 |= eq2(pv[t], 2) << (2 * t);
             }
             const unsigned nwm = (is1 | set1) & vol;
+            if (wdirty && (is2 & vol) != wold) {
+                // the wetting phase changed here: its tile is recomputed next step
+                Mw[b] = (uint8_t)(is2 & vol);
+                const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
+                const int tl = ((c0 / kT0) * nt1 + c1b / kT1) * nt2 + c2b / kT2;
+                if (!wdirty[tl] && atomicExch(wdirty + tl, 1) == 0)
+                    atomicAdd(nwdirty, 1ull);
+            }
             c2 += __popc(is2 & own & vol);
             c1 += __popc(nwm);
             if (Mn) {
@@ -2339,9 +2416,10 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
         atomicAdd(cnt1, (unsigned long long)c1);
 }
 
-int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, const uint8_t *M,
+int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, uint8_t *M,
                         const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
-                        unsigned long long *cnt1, int *err, cudaStream_t st)
+                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty,
+                        unsigned long long *nwdirty)
 {
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
@@ -2349,7 +2427,7 @@ int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape,
     const int ps__ = prof_begin("k_drain_update_blocks", st);
     k_drain_update_blocks<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
         mp, morph, P, M, mark, G, B, g_nw ? g_nw->M : nullptr, g_nw ? g_nw->P : nullptr,
-        g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err);
+        g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err, wdirty, nwdirty);
     prof_end(ps__, (double)n * 3 + (double)nb * 6, st);
     PMG_CHECK_LAUNCH();
     return PMG_OK;

@@ -77,6 +77,24 @@ int grow_marks_step(GrowSel &g, const uint8_t *S, int k, const int64_t *shape, c
 // pass; kept counts a's inlet-connected voxels.
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
                      const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept);
+// Selection of a set that only shrinks (the drainage's wetting phase): full
+// block union-find every step, but tiles the producer did not flag reuse
+// their tile-local parents Pl.  Scratch of shrink_sel_bytes(shape) bytes.
+struct ShrinkSel {
+    int *P = nullptr;
+    int *Pl = nullptr;
+    uint8_t *M = nullptr;
+    uint8_t *mark = nullptr;
+    int *dirty = nullptr; // per tile: changed since the last step
+    int ntiles = 0;
+    bool built = false;
+};
+size_t shrink_sel_bytes(const int64_t *shape);
+void shrink_sel_init(ShrinkSel &g, void *mem, const int64_t *shape);
+// unchanged: no tile was flagged since the last step (the result is reused)
+int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,
+                        const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, bool unchanged,
+                        int *err, cudaStream_t st);
 // Block union-find of the voxels equal to fgval with inlet / outlet marks,
 // without a selected image (parents left unflattened).
 int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc, const int32_t *pad,
@@ -85,9 +103,12 @@ int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const 
 // The drainage update on blocks, reading the wetting phase's outlet
 // connection from its block union-find (P, M, mark from bcc_marks_binary with
 // the outlet box); maintains g_nw's masks when given.
-int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, const uint8_t *M,
+// With wdirty, M (the wetting phase's masks) is brought up to date and the
+// tiles whose masks changed are flagged and counted in nwdirty.
+int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, uint8_t *M,
                         const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
-                        unsigned long long *cnt1, int *err, cudaStream_t st);
+                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty = nullptr,
+                        unsigned long long *nwdirty = nullptr);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 
