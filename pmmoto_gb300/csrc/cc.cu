@@ -1544,7 +1544,9 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
         const long long border = (long long)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) *
                                  ((G.b2 + kT2 - 1) / kT2) * kBorder;
         k_bcc_cross<<<grid_for(border, 256, 152LL * 64), 256, 0, st>>>(P, M, G, err);
-        prof_end(ps__, 0.0, st);
+        // per border block: its mask, the mask facing it across the tile
+        // border, its parent
+        prof_end(ps__, (double)border * 6, st);
     }
     PMG_CHECK_LAUNCH();
     if (twins && any_periodic(bc)) {
@@ -2249,12 +2251,10 @@ void shrink_sel_init(ShrinkSel &g, void *mem, const int64_t *shape)
 }
 
 int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,
-                        const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, bool unchanged,
-                        int *err, cudaStream_t st)
+                        const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int *err,
+                        cudaStream_t st)
 {
     PMG_TRY(check_boxes(shape, inlet_box, outlet_box));
-    if (g.built && unchanged)
-        return PMG_OK; // parents, masks and marks of the last step still hold
     if (!g.built)
         PMG_CUDA(cudaMemsetAsync(g.dirty, 0, sizeof(int) * (size_t)g.ntiles, st));
     SrcImg src{img, fgval};
@@ -2293,7 +2293,7 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                                       uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
                                       Boxes B, uint8_t *Mn, int *Pn, int *list, int *count,
                                       unsigned long long *cnt2, unsigned long long *cnt1, int *err,
-                                      int *wdirty, unsigned long long *nwdirty)
+                                      int *wdirty)
 {
     const int nb = G.b0 * G.b1 * G.b2;
     const int lane = threadIdx.x & 31;
@@ -2377,8 +2377,8 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                 Mw[b] = (uint8_t)(is2 & vol);
                 const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
                 const int tl = ((c0 / kT0) * nt1 + c1b / kT1) * nt2 + c2b / kT2;
-                if (!wdirty[tl] && atomicExch(wdirty + tl, 1) == 0)
-                    atomicAdd(nwdirty, 1ull);
+                if (!wdirty[tl])
+                    wdirty[tl] = 1;
             }
             c2 += __popc(is2 & own & vol);
             c1 += __popc(nwm);
@@ -2418,8 +2418,7 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
 
 int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, uint8_t *M,
                         const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
-                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty,
-                        unsigned long long *nwdirty)
+                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty)
 {
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
@@ -2427,7 +2426,7 @@ int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape,
     const int ps__ = prof_begin("k_drain_update_blocks", st);
     k_drain_update_blocks<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
         mp, morph, P, M, mark, G, B, g_nw ? g_nw->M : nullptr, g_nw ? g_nw->P : nullptr,
-        g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err, wdirty, nwdirty);
+        g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err, wdirty);
     prof_end(ps__, (double)n * 3 + (double)nb * 6, st);
     PMG_CHECK_LAUNCH();
     return PMG_OK;

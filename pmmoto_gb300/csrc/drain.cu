@@ -184,7 +184,7 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
                            const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d,
                            const float *De = nullptr, const uint16_t *KC = nullptr, int Te = -1,
                            bool m1_counted = false, GrowSel *g_er = nullptr, GrowSel *g_nw = nullptr,
-                           const uint8_t *Sv = nullptr, int step = -1, unsigned long long *wdirty_out = nullptr)
+                           const uint8_t *Sv = nullptr, int step = -1)
 {
     // m1_counted: w.cnt[1] already holds count(mp == 1) (the drainage update
     // counts it); the inlet selection counts its kept voxels into w.cnt[0], and
@@ -206,20 +206,10 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
             PMG_TRY(grow_marks_erode(*g_er, KC, Te, shape, bc, pad, Bx.inlet, w.err, st));
         PMG_TRY(grow_marks_binary(*g_nw, mp, 1, shape, bc, pad, Bx.inlet, w.err, st));
         PMG_TRY(grow_pair_select(*g_er, *g_nw, w.cnt + 1, w.t2, shape, w.err, st, w.cnt));
-        // the kept count, and (w.cnt[2]) how many wetting-phase tiles the last
-        // update changed
-        unsigned long long h[3] = {0, 0, 0};
-        PMG_CUDA(cudaMemcpyAsync(h, w.cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
-        PMG_CUDA(cudaStreamSynchronize(st));
-        const unsigned long long c1 = h[0];
-        if (wdirty_out)
-            *wdirty_out = h[2];
-        if (c1 == 0) {
-            PMG_CUDA(cudaMemsetAsync(out, 0, (size_t)n, st));
-            return PMG_OK;
-        }
+        // the dilation reads the kept count (w.cnt[0]) on the device: no
+        // dilation of an empty selection, and no host round trip per radius
         morph_split(w, shape, bc, ext_d, E, A, B);
-        return morph_run(w.t2, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st, ball_d);
+        return morph_run(w.t2, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st, ball_d, w.cnt);
     }
     if (KC && inlet) {
         if (g_er)
@@ -520,8 +510,6 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
     ShrinkSel g_w;
     if (s == PMG_OK)
         shrink_sel_init(g_w, (char *)grow_mem + gb * (grow_er ? 2 : 1), shape);
-    if (s == PMG_OK)
-        s = cudaMemsetAsync(w.cnt + 2, 0, sizeof(unsigned long long), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
     if (s == PMG_OK) {
         grow_sel_init(g_nw, grow_mem, shape);
         if (grow_er)
@@ -546,7 +534,6 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
     if (s == PMG_OK)
         s = count_eq_async(mp_img, shape, whole, 1, w.cnt + 1, st);
     for (int k = 0; k < n_radii && s == PMG_OK; k++) {
-        unsigned long long wdirty = ~0ull; // tiles of the wetting phase the last update changed (unknown)
         if (active[k]) {
             int32_t ext[6], ext_d[6];
             ext_of(bc, pad, ratios + 3 * k, ext);
@@ -555,7 +542,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext_d, res, radii[k], 1, radii_dilate[k], 1, 1,
                                 mp_img,
                                 Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
-                                De, KC, Te[(size_t)k], true, grow_er ? &g_er : nullptr, &g_nw, Sv, k, &wdirty);
+                                De, KC, Te[(size_t)k], true, grow_er ? &g_er : nullptr, &g_nw, Sv, k);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
@@ -563,10 +550,10 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
             break;
         // wetting phase connected to the outlet (its union-find and marks
         // only; tiles the last update left alone keep their tile-local
-        // parents, and nothing is redone when it changed no tile), then the
+        // parents), then the
         // update on blocks, which also brings the non-wetting phase's growing
         // selection and the wetting phase's masks and tile flags up to date
-        s = shrink_marks_binary(g_w, mp_img, 2, shape, bc, pad, nullptr, Bx.outlet, wdirty == 0, w.err, st);
+        s = shrink_marks_binary(g_w, mp_img, 2, shape, bc, pad, nullptr, Bx.outlet, w.err, st);
         if (s != PMG_OK)
             break;
         GrowSel *gn = nullptr;
@@ -580,9 +567,9 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
                 gn = &g_nw;
             }
         }
-        PMG_CUDA(cudaMemsetAsync(w.cnt + 1, 0, 2 * sizeof(unsigned long long), st));
+        PMG_CUDA(cudaMemsetAsync(w.cnt + 1, 0, sizeof(unsigned long long), st));
         s = drain_update_blocks(mp_img, morph, shape, g_w.P, g_w.M, g_w.mark, Bx, gn, d_counts + k, w.cnt + 1, w.err,
-                                st, g_w.dirty, w.cnt + 2);
+                                st, g_w.dirty);
         if (s != PMG_OK)
             break;
         if (gn)

@@ -92,7 +92,8 @@ __global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ 
 
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
-              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq)
+              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq,
+              const unsigned long long *gate)
 {
     ExtGeo G;
     int64_t X[3];
@@ -155,7 +156,18 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
     const bool cap = T != INT_MIN && cap_path_ok(res, X, T);
     const bool any_per = G.ax[0].periodic || G.ax[1].periodic || G.ax[2].periodic;
     if (cap && dilate && !any_per) // the row pass reads the image itself
-        return morph_cap_run(img, (uint16_t *)A, (uint16_t *)B, X, T, me, st, 1);
+        return morph_cap_run(img, (uint16_t *)A, (uint16_t *)B, X, T, me, st, 1, gate);
+    if (gate) {
+        // the other paths read the seed count on the host: an empty dilation
+        // source gives zeros
+        unsigned long long h = 0;
+        PMG_CUDA(cudaMemcpyAsync(&h, gate, sizeof(h), cudaMemcpyDeviceToHost, st));
+        PMG_CUDA(cudaStreamSynchronize(st));
+        if (h == 0) {
+            PMG_CUDA(cudaMemsetAsync(out, 0, (size_t)shape[0] * shape[1] * shape[2], st));
+            return PMG_OK;
+        }
+    }
 
     // last int of B: "the image holds a value above 1" (erosion only; the
     // capped pipeline needs a binary image)
@@ -319,7 +331,7 @@ extern "C" int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3
     uint8_t *E = (uint8_t *)buf;
     float *A = (float *)((char *)buf + (((size_t)nvox + 255) & ~(size_t)255));
     float *B = A + nvox;
-    int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st, ball_sq);
+    int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st, ball_sq, nullptr);
     int s2 = scratch_free(buf, st);
     return s != PMG_OK ? s : s2;
 }

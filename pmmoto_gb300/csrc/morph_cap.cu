@@ -56,8 +56,11 @@ struct RowSrc {
 // voxel's nearest seed in the three words around it with one count of
 // leading / trailing zeros each way.
 __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E, uint16_t *__restrict__ KA,
-                                                  long long rows, int X2, int T, int W, RowSrc rs)
+                                                  long long rows, int X2, int T, int W, RowSrc rs,
+                                                  const unsigned long long *__restrict__ gate)
 {
+    if (gate && *gate == 0)
+        return; // empty seed set: the last pass writes the result alone
     extern __shared__ uint32_t s_zw[];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -186,8 +189,10 @@ constexpr int kCapChunk = 8; // heights loaded ahead per line (memory-level para
 // it processes the current ones, so a thread keeps several loads in flight.
 template <int AX, int RING>
 __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA, uint16_t *__restrict__ KB,
-                                                 CapGeo G, int T, int W)
+                                                 CapGeo G, int T, int W, const unsigned long long *__restrict__ gate)
 {
+    if (gate && *gate == 0)
+        return;
     __shared__ int ring[RING * 128];
     const long long nlines = (long long)(AX == 1 ? G.X0 : G.nj) * G.nk;
     const long long st = AX == 1 ? (long long)G.X2 : (long long)G.X1 * G.X2;
@@ -244,9 +249,18 @@ __device__ __forceinline__ int isqrt_small(int m)
     return r;
 }
 
+// gate: a count of the seeds held in device memory (null: always seeds); when
+// it is zero the dilation is empty and only zeros are written.
 __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ KB, CapGeo G, int T, int W,
-                                                  MorphEpi me)
+                                                  MorphEpi me, const unsigned long long *__restrict__ gate)
 {
+    if (gate && *gate == 0) {
+        const long long nl = (long long)me.o1 * me.o2, no = me.o0 * nl;
+        for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < no;
+             q += (long long)gridDim.x * blockDim.x)
+            me.out[q] = 0;
+        return;
+    }
     // half-width of the interval of every height K <= T: floor(sqrt(T - K))
     __shared__ uint8_t s_w[kCapMaxT + 1];
     for (int q = threadIdx.x; q <= T; q += blockDim.x)
@@ -318,15 +332,15 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
 // the ring holds the live parabolas, at most 2W + 2
 template <int AX>
 static int launch_cap_mid(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, int W, long long lines,
-                          cudaStream_t st)
+                          cudaStream_t st, const unsigned long long *gate = nullptr)
 {
     const unsigned grid = grid_for(lines, 128, 1LL << 30);
     if (2 * W + 2 <= 16)
-        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W);
+        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate);
     else if (2 * W + 2 <= 32)
-        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W);
+        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W, gate);
     else
-        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W);
+        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W, gate);
     return PMG_OK;
 }
 
@@ -342,7 +356,7 @@ bool cap_path_ok(const float *res, const int64_t *X, int T)
 }
 
 int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
-                  cudaStream_t st, int raw_dilate)
+                  cudaStream_t st, int raw_dilate, const unsigned long long *gate)
 {
     RowSrc rs{};
     rs.raw = raw_dilate;
@@ -366,21 +380,22 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
         const int block = 256;
         const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
-        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W, rs);
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W, rs,
+                                                                                gate);
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();
     {
         const long long lines = (long long)G.X0 * G.nk;
         const int ps__ = prof_begin("k_cap_mid", st);
-        PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st));
+        PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st, gate));
         prof_end(ps__, (double)lines * G.X1 * 4, st);
     }
     PMG_CHECK_LAUNCH();
     {
         const long long lines = (long long)G.nj * G.nk;
         const int ps__ = prof_begin("k_cap_last", st);
-        k_cap_last<<<grid_for(lines, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me);
+        k_cap_last<<<grid_for(lines, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate);
         prof_end(ps__, (double)lines * G.X0 * 2 + (double)me.o0 * me.o1 * me.o2, st);
     }
     PMG_CHECK_LAUNCH();
@@ -410,7 +425,7 @@ int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, cons
         const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
         k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W,
-                                                                                RowSrc{});
+                                                                                RowSrc{}, nullptr);
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();

@@ -7,7 +7,8 @@ namespace pmg {
 
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
-              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq = -1.0);
+              int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq = -1.0,
+              const unsigned long long *gate = nullptr);
 size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext);
 int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const int32_t *bc,
                     const int32_t *pad, const float *res, int unit_res, uint8_t *E, float *A,
@@ -91,10 +92,9 @@ struct ShrinkSel {
 };
 size_t shrink_sel_bytes(const int64_t *shape);
 void shrink_sel_init(ShrinkSel &g, void *mem, const int64_t *shape);
-// unchanged: no tile was flagged since the last step (the result is reused)
 int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,
-                        const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, bool unchanged,
-                        int *err, cudaStream_t st);
+                        const int32_t *pad, const int64_t *inlet_box, const int64_t *outlet_box, int *err,
+                        cudaStream_t st);
 // Block union-find of the voxels equal to fgval with inlet / outlet marks,
 // without a selected image (parents left unflattened).
 int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc, const int32_t *pad,
@@ -104,11 +104,10 @@ int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const 
 // connection from its block union-find (P, M, mark from bcc_marks_binary with
 // the outlet box); maintains g_nw's masks when given.
 // With wdirty, M (the wetting phase's masks) is brought up to date and the
-// tiles whose masks changed are flagged and counted in nwdirty.
+// tiles whose masks changed are flagged.
 int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, uint8_t *M,
                         const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
-                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty = nullptr,
-                        unsigned long long *nwdirty = nullptr);
+                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty = nullptr);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 
