@@ -2095,6 +2095,22 @@ __global__ void k_step_scatter(const uint8_t *__restrict__ S, BGrid G, int nstep
     }
 }
 
+// Exclusive prefix of the per-step counts into the offsets (off[nsteps] =
+// total), the cursors reset to the offsets; one thread block.
+__global__ void k_step_offsets(int *cnt_cursor, int nsteps, int *off)
+{
+    if (threadIdx.x == 0) {
+        int total = 0;
+        for (int k = 0; k < nsteps; k++) {
+            const int c = cnt_cursor[k * kStepStride];
+            off[k] = total;
+            cnt_cursor[k * kStepStride] = total;
+            total += c;
+        }
+        off[nsteps] = total;
+    }
+}
+
 int step_lists_build(GrowSel &g, const uint8_t *S, const int64_t *shape, int nsteps, void **mem, cudaStream_t st)
 {
     *mem = nullptr;
@@ -2104,66 +2120,33 @@ int step_lists_build(GrowSel &g, const uint8_t *S, const int64_t *shape, int nst
     }
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
-    int *tmp = nullptr;
+    // a block has at most min(8, nsteps) distinct steps: the list is sized for
+    // that, so nothing has to be read back before the scatter
+    const size_t cap = (size_t)nb * (size_t)(nsteps < 8 ? nsteps : 8);
     const size_t tmpb = sizeof(int) * (size_t)kStepStride * 256;
-    PMG_TRY(scratch_alloc((void **)&tmp, tmpb, st));
-    int s = cudaMemsetAsync(tmp, 0, tmpb, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-    if (s == PMG_OK) {
+    const size_t offb = ((size_t)(nsteps + 1) * sizeof(int) + 255) & ~(size_t)255;
+    char *m = nullptr;
+    PMG_TRY(scratch_alloc((void **)&m, tmpb + offb + sizeof(int) * cap, st));
+    int *tmp = (int *)m;
+    g.off = (int *)(m + tmpb);
+    g.ev = (int *)(m + tmpb + offb);
+    *mem = m;
+    PMG_CUDA(cudaMemsetAsync(tmp, 0, tmpb, st));
+    {
         const int ps__ = prof_begin("k_step_count", st);
         k_step_count<<<grid_for(nb, 256, 152LL * 8), 256, 0, st>>>(S, G, nsteps, tmp);
-        prof_end(ps__, 0.0, st);
-        s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        prof_end(ps__, (double)nb * 8, st);
     }
-    std::vector<int> hs((size_t)kStepStride * 256, 0), h((size_t)nsteps + 1, 0);
-    if (s == PMG_OK)
-        s = cudaMemcpyAsync(hs.data(), tmp, tmpb, cudaMemcpyDeviceToHost, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-    if (s == PMG_OK)
-        s = cudaStreamSynchronize(st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-    for (int k = 0; k < nsteps; k++)
-        h[(size_t)k] = hs[(size_t)k * kStepStride];
-    long long total = 0;
-    for (int k = 0; k <= nsteps && s == PMG_OK; k++) {
-        const int c = k < nsteps ? h[(size_t)k] : 0;
-        h[(size_t)k] = (int)total;
-        total += c;
-    }
-    if (s == PMG_OK && total > 8LL * nb) {
-        set_error("step lists: %lld events for %d blocks", total, nb);
-        s = PMG_EINVAL;
-    }
-    char *m = nullptr;
-    const size_t offb = ((size_t)(nsteps + 1) * sizeof(int) + 255) & ~(size_t)255;
-    if (s == PMG_OK)
-        s = scratch_alloc((void **)&m, offb + sizeof(int) * (size_t)(total > 0 ? total : 1), st);
-    if (s == PMG_OK) {
-        g.off = (int *)m;
-        g.ev = (int *)(m + offb);
-        *mem = m;
-        s = cudaMemcpyAsync(g.off, h.data(), sizeof(int) * (size_t)(nsteps + 1), cudaMemcpyHostToDevice, st) ==
-                    cudaSuccess
-                ? PMG_OK
-                : PMG_ECUDA;
-    }
-    // cursors start at the offsets
-    for (int k = 0; k < nsteps; k++)
-        hs[(size_t)k * kStepStride] = h[(size_t)k];
-    if (s == PMG_OK)
-        s = cudaMemcpyAsync(tmp, hs.data(), tmpb, cudaMemcpyHostToDevice, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-    if (s == PMG_OK) {
+    PMG_CHECK_LAUNCH();
+    k_step_offsets<<<1, 32, 0, st>>>(tmp, nsteps, g.off);
+    PMG_CHECK_LAUNCH();
+    {
         const int ps__ = prof_begin("k_step_scatter", st);
         k_step_scatter<<<grid_for(nb, 256, 152LL * 8), 256, 0, st>>>(S, G, nsteps, tmp, g.ev);
-        prof_end(ps__, 0.0, st);
-        s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        prof_end(ps__, (double)nb * 8, st);
     }
-    // the host offsets must outlive the copies
-    if (s == PMG_OK)
-        s = cudaStreamSynchronize(st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-    const int s2 = scratch_free(tmp, st);
-    if (s != PMG_OK) {
-        g.ev = nullptr;
-        g.off = nullptr;
-    }
-    return s != PMG_OK ? s : s2;
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
 }
 
 int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *shape, const int32_t *bc,

@@ -493,10 +493,8 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
             k_step_volume<<<grid_for(shape[0] * shape[1] * 32, 256, 152LL * 64), 256, 0, st>>>(
                 KC, Sv, dtab, Tcap + 1, shape[0], shape[1], shape[2], walls);
             prof_end(ps__, (double)n * 3, st);
+            // (a copy from pageable memory has read the table when it returns)
             s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
-            // the host table must outlive the copy
-            if (s == PMG_OK)
-                s = cudaStreamSynchronize(st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
         if (s == PMG_OK) {
             s = scratch_free(KC, st);
