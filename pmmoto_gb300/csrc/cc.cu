@@ -1817,23 +1817,50 @@ void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape)
 
 // One step of a growing selection up to the marks: the full block union-find
 // the first time, afterwards the grown blocks only.
+// Parent of a block that has just become non-empty (fresh): the first block
+// of its run of fresh blocks in the warp, where each lane's block follows the
+// previous lane's in the same row (prev_adj) and the two touch across their
+// common z face; a run's first block is its own root.  The run is connected,
+// and its first block has the smallest index.  Every lane of the warp calls it.
+__device__ __forceinline__ int fresh_run_parent(int b, bool fresh, unsigned m, bool prev_adj)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned pm = __shfl_up_sync(FULL, m, 1);
+    const int pf = __shfl_up_sync(FULL, (int)fresh, 1);
+    const bool link = fresh && lane > 0 && pf && prev_adj && (m & 0x55u) && (pm & 0xAAu);
+    const unsigned lm = __ballot_sync(FULL, link);
+    const unsigned upto = lane == 31 ? FULL : ((2u << lane) - 1u);
+    const int head = 31 - __clz(~lm & upto);
+    return b - (lane - head);
+}
+
 // Listed blocks take their masks from the source (steps known in advance).
 template <class Src>
 __global__ void k_grow_apply(Src src, uint8_t *__restrict__ M, int *__restrict__ P, BGrid G,
                              const int *__restrict__ list, const int *__restrict__ off, int *err)
 {
     const int a = off[0], cnt = off[1] - a;
-    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
-        const int b = list[a + it];
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < cnt; base += gridDim.x * blockDim.x) {
+        const int it = base + lane;
+        const bool has = it < cnt;
+        const int b = has ? list[a + it] : -2;
         const int r = b / G.b2;
         const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
-        const unsigned old = M[b];
-        const unsigned m = block_mask(src, G, c0, c1, c2);
-        if (old & ~m)
-            atomicExch(err, 3);
-        M[b] = (uint8_t)m;
-        if (!old)
-            P[b] = b;
+        unsigned old = 0, m = 0;
+        if (has) {
+            old = M[b];
+            m = block_mask(src, G, c0, c1, c2);
+            if (old & ~m)
+                atomicExch(err, 3);
+            M[b] = (uint8_t)m;
+        }
+        const bool fresh = has && !old && m;
+        const int pb = __shfl_up_sync(0xffffffffu, b, 1);
+        const int parent = fresh_run_parent(b, fresh, m, has && c2 > 0 && pb == b - 1);
+        if (fresh)
+            P[b] = parent;
     }
 }
 
@@ -1868,7 +1895,7 @@ static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int
         PMG_CHECK_LAUNCH();
     }
     {
-        const int ps__ = prof_begin("k_grow_unite", st);
+        const int ps__ = prof_begin(g.unite_label, st);
         k_grow_unite<<<152 * 32, 256, 0, st>>>(g.P, g.M, G, off ? g.ev : g.list, g.count, off, err);
         prof_end(ps__, 0.0, st);
     }
@@ -1926,11 +1953,12 @@ __device__ __forceinline__ int root_flatten(int *P, int b, int *err)
 __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, const uint8_t *__restrict__ markA,
                                    const uint8_t *__restrict__ MB, int *PB, const uint8_t *__restrict__ markB,
                                    const unsigned long long *__restrict__ b_count, BGrid G,
-                                   uint8_t *__restrict__ out, unsigned long long *kept, int *err)
+                                   uint8_t *__restrict__ out, unsigned long long *kept, int *err, int *xr)
 {
     const int nb = G.b0 * G.b1 * G.b2;
     const bool constrain = *b_count > 0;
     unsigned int cnt = 0;
+    int xmax = 0, xmin = 0; // block-plane range of the output's voxels, encoded as in XRange
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         const int r = b / G.b2;
         const int c2 = b - r * G.b2;
@@ -1952,6 +1980,10 @@ __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, cons
         cnt += __popc(m);
         if (constrain)
             m &= keepB;
+        if (m) {
+            xmax = max(xmax, c0 + 1);
+            xmin = max(xmin, kRangeBig - c0);
+        }
 #pragma unroll
         for (int x = 0; x < 2; x++)
 #pragma unroll
@@ -1968,10 +2000,19 @@ __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, cons
                 }
             }
     }
-    for (int o = 16; o > 0; o >>= 1)
+    for (int o = 16; o > 0; o >>= 1) {
         cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if ((threadIdx.x & 31) == 0 && cnt)
-        atomicAdd(kept, (unsigned long long)cnt);
+        xmax = max(xmax, __shfl_down_sync(0xffffffffu, xmax, o));
+        xmin = max(xmin, __shfl_down_sync(0xffffffffu, xmin, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (cnt)
+            atomicAdd(kept, (unsigned long long)cnt);
+        if (xr && xmax) {
+            atomicMax(xr, xmax);
+            atomicMax(xr + 1, xmin);
+        }
+    }
 }
 
 int grow_marks_erode(GrowSel &g, const uint16_t *E, int T, const int64_t *shape, const int32_t *bc,
@@ -2157,14 +2198,16 @@ int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *
 }
 
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
-                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept)
+                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept, int *xr)
 {
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
     const long long n = shape[0] * shape[1] * shape[2];
     const int ps__ = prof_begin("k_grow_pair_select", st);
+    if (xr)
+        PMG_CUDA(cudaMemsetAsync(xr, 0, 2 * sizeof(int), st));
     k_grow_pair_select<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(a.M, a.P, a.mark, b.M, b.P, b.mark, b_count,
-                                                                      G, out, kept, err);
+                                                                      G, out, kept, err, xr);
     prof_end(ps__, (double)n + (double)nb * 10, st);
     PMG_CHECK_LAUNCH();
     return PMG_OK;
@@ -2276,8 +2319,15 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                                       uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
                                       Boxes B, uint8_t *Mn, int *Pn, int *list, int *count,
                                       unsigned long long *cnt2, unsigned long long *cnt1, int *err,
-                                      int *wdirty)
+                                      int *wdirty, const int *__restrict__ orange, int ranged)
 {
+    // orange: the x range [olo, ohi] (whole blocks) where the dilation result
+    // is defined; outside it the dilation is empty.  ranged: only blocks that
+    // can change are visited (the dilation range: the reservoir slabs were
+    // refilled by an earlier update), and cnt2 / cnt1 receive the changes
+    // (voxels leaving value 2 inside the own box, voxels newly 1) instead of
+    // the totals.
+    const int bxlo = orange ? orange[0] >> 1 : 0, bxhi = orange ? orange[1] >> 1 : G.b0 - 1;
     const int nb = G.b0 * G.b1 * G.b2;
     const int lane = threadIdx.x & 31;
     unsigned int c2 = 0, c1 = 0;
@@ -2285,8 +2335,11 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
     const long long sx = (long long)G.s1 * G.s2, sy = G.s2;
     for (int base = blockIdx.x * blockDim.x; base < nb; base += gridDim.x * blockDim.x) {
         const int b = base + threadIdx.x;
-        bool changed = false;
-        if (b < nb) {
+        bool changed = false, fresh = false, zrow = false;
+        unsigned mfresh = 0;
+        const int rr = b / G.b2, cc0 = rr / G.b1;
+        const bool in_dil = cc0 >= bxlo && cc0 <= bxhi;
+        if (b < nb && (in_dil || !ranged)) {
             const int r = b / G.b2;
             const int c2b = b - r * G.b2, c0 = r / G.b1, c1b = r - (r / G.b1) * G.b1;
             const int i0 = 2 * c0, j0 = 2 * c1b, k0 = 2 * c2b;
@@ -2303,7 +2356,7 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
             unsigned wet = wold;
             // the four rows of the block: old values and the morph == 1 bits
             const long long base0 = (long long)i0 * sx + (long long)j0 * sy + k0;
-            unsigned pv[4], m1 = 0, is1 = 0;
+            unsigned pv[4], m1 = 0, is1 = 0, is2o = 0;
 #pragma unroll
             for (int t = 0; t < 4; t++) {
                 const int x = t >> 1, y = t & 1;
@@ -2313,18 +2366,22 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                     const long long a = base0 + x * sx + y * sy;
                     if (pairs) {
                         pv[t] = *(const uint16_t *)(mp + a);
-                        mv = *(const uint16_t *)(morph + a);
+                        if (in_dil)
+                            mv = *(const uint16_t *)(morph + a);
                     } else {
                         pv[t] = mp[a];
-                        mv = morph[a];
+                        if (in_dil)
+                            mv = morph[a];
                         if (vK & 2u) {
                             pv[t] |= (unsigned)mp[a + 1] << 8;
-                            mv |= (unsigned)morph[a + 1] << 8;
+                            if (in_dil)
+                                mv |= (unsigned)morph[a + 1] << 8;
                         }
                     }
                 }
                 m1 |= eq2(mv, 1) << (2 * t);
                 is1 |= eq2(pv[t], 1) << (2 * t);
+                is2o |= eq2(pv[t], 2) << (2 * t);
             }
             // the wetting phase's outlet connection matters only where the
             // dilation meets it
@@ -2363,21 +2420,31 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                 if (!wdirty[tl])
                     wdirty[tl] = 1;
             }
-            c2 += __popc(is2 & own & vol);
-            c1 += __popc(nwm);
+            if (ranged) {
+                c2 += __popc(set1 & is2o & own & vol);
+                c1 += __popc(set1 & ~is1 & vol);
+            } else {
+                c2 += __popc(is2 & own & vol);
+                c1 += __popc(nwm);
+            }
             if (Mn) {
                 const unsigned old = Mn[b];
                 if (nwm != old) {
                     if (old & ~nwm)
                         atomicExch(err, 3);
                     Mn[b] = (uint8_t)nwm;
-                    if (!old)
-                        Pn[b] = b;
+                    fresh = !old;
                     changed = true;
                 }
+                mfresh = nwm;
+                zrow = c2b > 0;
             }
         }
         if (Mn) {
+            // consecutive lanes hold consecutive blocks
+            const int parent = fresh_run_parent(b, fresh, mfresh, zrow);
+            if (fresh)
+                Pn[b] = parent;
             const unsigned bal = __ballot_sync(0xffffffffu, changed);
             if (bal) {
                 int pos = 0;
@@ -2399,9 +2466,36 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
         atomicAdd(cnt1, (unsigned long long)c1);
 }
 
+// Running totals (count(own == 2), count(== 1)) from the update's full counts
+// or changes; the saturation numerator and the phase-1 count out.
+__global__ void k_drain_totals(int ranged, const unsigned long long *cnt2, const unsigned long long *cnt1,
+                               unsigned long long *tot, unsigned long long *sat_out, unsigned long long *ones_out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (ranged) {
+            tot[0] -= *cnt2;
+            tot[1] += *cnt1;
+        } else {
+            tot[0] = *cnt2;
+            tot[1] = *cnt1;
+        }
+        *sat_out = tot[0];
+        *ones_out = tot[1];
+    }
+}
+
+int drain_totals(bool ranged, const unsigned long long *cnt2, const unsigned long long *cnt1, unsigned long long *tot,
+                 unsigned long long *sat_out, unsigned long long *ones_out, cudaStream_t st)
+{
+    k_drain_totals<<<1, 32, 0, st>>>(ranged ? 1 : 0, cnt2, cnt1, tot, sat_out, ones_out);
+    PMG_CHECK_LAUNCH();
+    return PMG_OK;
+}
+
 int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, uint8_t *M,
                         const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
-                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty)
+                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty, const int *orange,
+                        bool ranged)
 {
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
@@ -2409,7 +2503,8 @@ int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape,
     const int ps__ = prof_begin("k_drain_update_blocks", st);
     k_drain_update_blocks<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
         mp, morph, P, M, mark, G, B, g_nw ? g_nw->M : nullptr, g_nw ? g_nw->P : nullptr,
-        g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err, wdirty);
+        g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err, wdirty, orange,
+        ranged ? 1 : 0);
     prof_end(ps__, (double)n * 3 + (double)nb * 6, st);
     PMG_CHECK_LAUNCH();
     return PMG_OK;

@@ -184,7 +184,7 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
                            const Boxes &Bx, Work &w, cudaStream_t st, double ball_e, double ball_d,
                            const float *De = nullptr, const uint16_t *KC = nullptr, int Te = -1,
                            bool m1_counted = false, GrowSel *g_er = nullptr, GrowSel *g_nw = nullptr,
-                           const uint8_t *Sv = nullptr, int step = -1)
+                           const uint8_t *Sv = nullptr, int step = -1, int *orange = nullptr)
 {
     // m1_counted: w.cnt[1] already holds count(mp == 1) (the drainage update
     // counts it); the inlet selection counts its kept voxels into w.cnt[0], and
@@ -205,11 +205,20 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
         else
             PMG_TRY(grow_marks_erode(*g_er, KC, Te, shape, bc, pad, Bx.inlet, w.err, st));
         PMG_TRY(grow_marks_binary(*g_nw, mp, 1, shape, bc, pad, Bx.inlet, w.err, st));
-        PMG_TRY(grow_pair_select(*g_er, *g_nw, w.cnt + 1, w.t2, shape, w.err, st, w.cnt));
+        // the selection's x range (w.cnt[4]) limits the dilation to the planes
+        // it can reach; the dilation's result range goes to orange
+        int *xr = orange ? (int *)(w.cnt + 4) : nullptr;
+        PMG_TRY(grow_pair_select(*g_er, *g_nw, w.cnt + 1, w.t2, shape, w.err, st, w.cnt, xr));
         // the dilation reads the kept count (w.cnt[0]) on the device: no
         // dilation of an empty selection, and no host round trip per radius
         morph_split(w, shape, bc, ext_d, E, A, B);
-        return morph_run(w.t2, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st, ball_d, w.cnt);
+        return morph_run(w.t2, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st, ball_d, w.cnt, xr,
+                         orange);
+    }
+    if (orange) {
+        // the paths below write the whole result
+        const int full[2] = {0, (int)shape[0] - 1};
+        PMG_CUDA(cudaMemcpyAsync(orange, full, sizeof(full), cudaMemcpyHostToDevice, st));
     }
     if (KC && inlet) {
         if (g_er)
@@ -510,8 +519,11 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
         shrink_sel_init(g_w, (char *)grow_mem + gb * (grow_er ? 2 : 1), shape);
     if (s == PMG_OK) {
         grow_sel_init(g_nw, grow_mem, shape);
-        if (grow_er)
+        g_nw.unite_label = "k_grow_unite[nonwetting]";
+        if (grow_er) {
             grow_sel_init(g_er, (char *)grow_mem + gb, shape);
+            g_er.unite_label = "k_grow_unite[eroded]";
+        }
     }
     // the blocks of the eroded space that grow at each radius, listed once
     void *lists_mem = nullptr;
@@ -531,7 +543,19 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
         s = cudaMemsetAsync(w.cnt + 1, 0, sizeof(unsigned long long), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
     if (s == PMG_OK)
         s = count_eq_async(mp_img, shape, whole, 1, w.cnt + 1, st);
+    // After the first update (which refills the reservoir slabs), a radius can
+    // change only voxels within the dilation's x range: the update visits that
+    // range alone and keeps the saturation counts as running totals
+    // (w.cnt[10], w.cnt[11]) from the changes it counts (w.cnt[8], w.cnt[9]).
+    int *orange = (int *)(w.cnt + 5);
+    bool full_done = false;
     for (int k = 0; k < n_radii && s == PMG_OK; k++) {
+        if (!active[k] && full_done) {
+            // no dilation: nothing changes, the totals stand
+            PMG_CUDA(cudaMemsetAsync(w.cnt + 8, 0, 2 * sizeof(unsigned long long), st));
+            s = drain_totals(true, w.cnt + 8, w.cnt + 9, w.cnt + 10, d_counts + k, w.cnt + 1, st);
+            continue;
+        }
         if (active[k]) {
             int32_t ext[6], ext_d[6];
             ext_of(bc, pad, ratios + 3 * k, ext);
@@ -540,7 +564,7 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
             s = porosimetry_run(pm_img, morph, shape, bc, pad, ext, ext_d, res, radii[k], 1, radii_dilate[k], 1, 1,
                                 mp_img,
                                 Bx, w, st, ball_erode ? ball_erode[k] : -1.0, ball_dilate ? ball_dilate[k] : -1.0,
-                                De, KC, Te[(size_t)k], true, grow_er ? &g_er : nullptr, &g_nw, Sv, k);
+                                De, KC, Te[(size_t)k], true, grow_er ? &g_er : nullptr, &g_nw, Sv, k, orange);
         } else {
             s = cudaMemsetAsync(morph, 0, (size_t)n, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
@@ -565,11 +589,14 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
                 gn = &g_nw;
             }
         }
-        PMG_CUDA(cudaMemsetAsync(w.cnt + 1, 0, sizeof(unsigned long long), st));
-        s = drain_update_blocks(mp_img, morph, shape, g_w.P, g_w.M, g_w.mark, Bx, gn, d_counts + k, w.cnt + 1, w.err,
-                                st, g_w.dirty);
+        PMG_CUDA(cudaMemsetAsync(w.cnt + 8, 0, 2 * sizeof(unsigned long long), st));
+        s = drain_update_blocks(mp_img, morph, shape, g_w.P, g_w.M, g_w.mark, Bx, gn, w.cnt + 8, w.cnt + 9, w.err,
+                                st, g_w.dirty, active[k] ? orange : nullptr, full_done);
+        if (s == PMG_OK)
+            s = drain_totals(full_done, w.cnt + 8, w.cnt + 9, w.cnt + 10, d_counts + k, w.cnt + 1, st);
         if (s != PMG_OK)
             break;
+        full_done = true;
         if (gn)
             g_nw.pending = true;
     }

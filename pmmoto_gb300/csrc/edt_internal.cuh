@@ -143,9 +143,13 @@ constexpr int kCapMaxT = 1023;
 bool cap_path_ok(const float *res, const int64_t *X, int T);
 // raw_dilate: E is the unextended image of a dilation without periodic axes
 // (no k_extend copy); gate: a device count of the seeds (null: not known to
-// be empty), zero making the result all zeros without the envelope passes
+// be empty), zero making the result all zeros without the envelope passes;
+// xr: a device x range of the seed blocks (kRangeBig encoding) -- the
+// result is then written only on the x range orange receives ([lo, hi] in
+// whole blocks, lo > hi for none) and is undefined elsewhere
 int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
-                  cudaStream_t st, int raw_dilate = 0, const unsigned long long *gate = nullptr);
+                  cudaStream_t st, int raw_dilate = 0, const unsigned long long *gate = nullptr,
+                  const int *xr = nullptr, int *orange = nullptr);
 int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, const int64_t *X, int T,
                 cudaStream_t st);
 

@@ -93,8 +93,13 @@ __global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ 
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
               int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq,
-              const unsigned long long *gate)
+              const unsigned long long *gate, const int *xr, int *orange)
 {
+    // orange: on the paths below that ignore xr the whole result is written
+    if (orange) {
+        const int full[2] = {0, (int)shape[0] - 1};
+        PMG_CUDA(cudaMemcpyAsync(orange, full, sizeof(full), cudaMemcpyHostToDevice, st));
+    }
     ExtGeo G;
     int64_t X[3];
     for (int d = 0; d < 3; d++) {
@@ -156,7 +161,7 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
     const bool cap = T != INT_MIN && cap_path_ok(res, X, T);
     const bool any_per = G.ax[0].periodic || G.ax[1].periodic || G.ax[2].periodic;
     if (cap && dilate && !any_per) // the row pass reads the image itself
-        return morph_cap_run(img, (uint16_t *)A, (uint16_t *)B, X, T, me, st, 1, gate);
+        return morph_cap_run(img, (uint16_t *)A, (uint16_t *)B, X, T, me, st, 1, gate, xr, orange);
     if (gate) {
         // the other paths read the seed count on the host: an empty dilation
         // source gives zeros
@@ -331,7 +336,8 @@ extern "C" int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3
     uint8_t *E = (uint8_t *)buf;
     float *A = (float *)((char *)buf + (((size_t)nvox + 255) & ~(size_t)255));
     float *B = A + nvox;
-    int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st, ball_sq, nullptr);
+    int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st, ball_sq, nullptr,
+                      nullptr, nullptr);
     int s2 = scratch_free(buf, st);
     return s != PMG_OK ? s : s2;
 }

@@ -38,6 +38,28 @@ struct CapGeo {
     int j0, nj, k0, nk;   // unextended ranges of axes 1 and 2
 };
 
+// ---- x range of the seeds -------------------------------------------------------
+// An optional block-plane range of the seeds (kRangeBig encoding, device
+// memory): planes outside [hlo, hhi] hold no seed, so the row and envelope
+// passes skip them, and the last pass produces only the outputs within W of
+// the seeds, [olo, ohi] widened to whole 2x2x2 blocks.
+struct SeedRange {
+    int hlo, hhi, olo, ohi; // hlo > hhi: no seeds
+    __device__ __forceinline__ void load(const int *xr, int n, int W)
+    {
+        const int a = xr[0], b = xr[1];
+        if (a == 0) {
+            hlo = olo = 2;
+            hhi = ohi = -1;
+            return;
+        }
+        hlo = 2 * (kRangeBig - b);
+        hhi = min(2 * (a - 1) + 1, n - 1);
+        olo = max(0, hlo - W) & ~1;
+        ohi = min(n - 1, (hhi + W) | 1);
+    }
+};
+
 // ---- pass A: rows -------------------------------------------------------------
 // raw == 0: E is the (extended) image whose zeros are the seeds.  raw == 1:
 // E is the unextended image of a dilation without periodic axes, read
@@ -57,10 +79,14 @@ struct RowSrc {
 // leading / trailing zeros each way.
 __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E, uint16_t *__restrict__ KA,
                                                   long long rows, int X2, int T, int W, RowSrc rs,
-                                                  const unsigned long long *__restrict__ gate)
+                                                  const unsigned long long *__restrict__ gate,
+                                                  const int *__restrict__ xr)
 {
     if (gate && *gate == 0)
         return; // empty seed set: the last pass writes the result alone
+    SeedRange sr{0, 0x7fffffff, 0, 0};
+    if (xr)
+        sr.load(xr, (int)(rows / rs.X1), W);
     extern __shared__ uint32_t s_zw[];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -74,6 +100,11 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const int big = T + 1;
     for (long long r = warp; r < rows; r += nwarps) {
+        if (xr) {
+            const int x0 = (int)(r / rs.X1);
+            if (x0 < sr.hlo || x0 > sr.hhi)
+                continue;
+        }
         const uint8_t *src = E + r * X2;
         bool wrow = false;
         if (rs.raw) {
@@ -189,10 +220,14 @@ constexpr int kCapChunk = 8; // heights loaded ahead per line (memory-level para
 // it processes the current ones, so a thread keeps several loads in flight.
 template <int AX, int RING>
 __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA, uint16_t *__restrict__ KB,
-                                                 CapGeo G, int T, int W, const unsigned long long *__restrict__ gate)
+                                                 CapGeo G, int T, int W, const unsigned long long *__restrict__ gate,
+                                                 const int *__restrict__ xr)
 {
     if (gate && *gate == 0)
         return;
+    SeedRange sr{0, 0x7fffffff, 0, 0};
+    if (xr)
+        sr.load(xr, G.X0, W);
     __shared__ int ring[RING * 128];
     const long long nlines = (long long)(AX == 1 ? G.X0 : G.nj) * G.nk;
     const long long st = AX == 1 ? (long long)G.X2 : (long long)G.X1 * G.X2;
@@ -201,6 +236,8 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
     for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
          li += (long long)gridDim.x * blockDim.x) {
         const long long q = li / G.nk;
+        if (AX == 1 && xr && (q < sr.hlo || q > sr.hhi))
+            continue;
         const int x2 = G.k0 + (int)(li - q * G.nk);
         const long long base = AX == 1 ? q * G.X1 * G.X2 + x2 : (G.j0 + q) * G.X2 + x2;
         const uint16_t *in = KA + base;
@@ -252,8 +289,22 @@ __device__ __forceinline__ int isqrt_small(int m)
 // gate: a count of the seeds held in device memory (null: always seeds); when
 // it is zero the dilation is empty and only zeros are written.
 __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ KB, CapGeo G, int T, int W,
-                                                  MorphEpi me, const unsigned long long *__restrict__ gate)
+                                                  MorphEpi me, const unsigned long long *__restrict__ gate,
+                                                  const int *__restrict__ xr, int *__restrict__ orange)
 {
+    SeedRange sr{0, G.X0 - 1, 0, G.X0 - 1};
+    if (xr)
+        sr.load(xr, G.X0, W);
+    if (gate && *gate == 0) {
+        sr.olo = 2;
+        sr.ohi = -1;
+    }
+    if (orange && blockIdx.x == 0 && threadIdx.x == 0) {
+        orange[0] = sr.olo;
+        orange[1] = sr.ohi;
+    }
+    if (xr && sr.olo > sr.ohi)
+        return; // nothing within reach of a seed: the caller reads no output
     if (gate && *gate == 0) {
         const long long nl = (long long)me.o1 * me.o2, no = me.o0 * nl;
         for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < no;
@@ -269,8 +320,13 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
     const long long nlines = (long long)G.nj * G.nk;
     const long long st = (long long)G.X1 * G.X2;
     const int n = G.X0;
-    // positions x of the line that lie in the unextended volume
-    const int xlo = max(0, me.e0), xhi = min(n, me.e0 + (int)me.o0);
+    // positions x of the line that lie in the unextended volume (and in the
+    // output range of the seeds)
+    const int xlo = max(max(0, me.e0), sr.olo), xhi = min(min(n, me.e0 + (int)me.o0), sr.ohi + 1);
+    // heights exist on [sr.hlo, sr.hhi] only; the sweep starts where either the
+    // first height or the first output is due
+    const int istart = min(sr.hlo, xlo + W) < 0 ? 0 : min(sr.hlo, xlo + W);
+    const int iend = xhi - 1 + W; // last step that emits an output
     for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
          li += (long long)gridDim.x * blockDim.x) {
         const int x1 = G.j0 + (int)(li / G.nk);
@@ -287,18 +343,21 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
         uint64_t pend = 0; // bit b: position i - b is covered
         int reach = -1;
         const int big = T + 1;
+        const int hend = min(n, sr.hhi + 1); // heights are read on [hlo, hend)
         int cur[kCapChunk];
-        const uint16_t *pin = in;
+        const uint16_t *pin = in + (long long)istart * st;
 #pragma unroll
         for (int u = 0; u < kCapChunk; u++) {
-            cur[u] = u < n ? (int)*pin : big;
+            const int i = istart + u;
+            cur[u] = i >= sr.hlo && i < hend ? (int)*pin : big;
             pin += st;
         }
-        for (int i0 = 0; i0 < n + W; i0 += kCapChunk) {
+        for (int i0 = istart; i0 <= iend; i0 += kCapChunk) {
             int nxt[kCapChunk];
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++) {
-                nxt[u] = i0 + kCapChunk + u < n ? (int)*pin : big;
+                const int i = i0 + kCapChunk + u;
+                nxt[u] = i >= sr.hlo && i < hend ? (int)*pin : big;
                 pin += st;
             }
 #pragma unroll
@@ -332,15 +391,15 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
 // the ring holds the live parabolas, at most 2W + 2
 template <int AX>
 static int launch_cap_mid(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, int W, long long lines,
-                          cudaStream_t st, const unsigned long long *gate = nullptr)
+                          cudaStream_t st, const unsigned long long *gate = nullptr, const int *xr = nullptr)
 {
     const unsigned grid = grid_for(lines, 128, 1LL << 30);
     if (2 * W + 2 <= 16)
-        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate);
+        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr);
     else if (2 * W + 2 <= 32)
-        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W, gate);
+        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr);
     else
-        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W, gate);
+        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr);
     return PMG_OK;
 }
 
@@ -356,7 +415,7 @@ bool cap_path_ok(const float *res, const int64_t *X, int T)
 }
 
 int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
-                  cudaStream_t st, int raw_dilate, const unsigned long long *gate)
+                  cudaStream_t st, int raw_dilate, const unsigned long long *gate, const int *xr, int *orange)
 {
     RowSrc rs{};
     rs.raw = raw_dilate;
@@ -381,21 +440,21 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
         const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
         k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W, rs,
-                                                                                gate);
+                                                                                gate, xr);
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();
     {
         const long long lines = (long long)G.X0 * G.nk;
         const int ps__ = prof_begin("k_cap_mid", st);
-        PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st, gate));
+        PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st, gate, xr));
         prof_end(ps__, (double)lines * G.X1 * 4, st);
     }
     PMG_CHECK_LAUNCH();
     {
         const long long lines = (long long)G.nj * G.nk;
         const int ps__ = prof_begin("k_cap_last", st);
-        k_cap_last<<<grid_for(lines, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate);
+        k_cap_last<<<grid_for(lines, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate, xr, orange);
         prof_end(ps__, (double)lines * G.X0 * 2 + (double)me.o0 * me.o1 * me.o2, st);
     }
     PMG_CHECK_LAUNCH();
@@ -425,7 +484,7 @@ int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, cons
         const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
         k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W,
-                                                                                RowSrc{}, nullptr);
+                                                                                RowSrc{}, nullptr, nullptr);
         prof_end(ps__, (double)vox * 3, st);
     }
     PMG_CHECK_LAUNCH();

@@ -129,4 +129,9 @@ __device__ __forceinline__ float isect(float f_r, float r, float f_q, float q, f
     return __fdiv_rn(num, fmul(2.0f, factor1));
 }
 
+// x range of a set of 2x2x2 blocks kept in device memory as two ints, both
+// raised with atomicMax from zero: [0] = 1 + the largest block plane,
+// [1] = kRangeBig - the smallest (so a zeroed pair is the empty range).
+constexpr int kRangeBig = 1 << 30;
+
 } // namespace pmg

@@ -8,7 +8,7 @@ namespace pmg {
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
               int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq = -1.0,
-              const unsigned long long *gate = nullptr);
+              const unsigned long long *gate = nullptr, const int *xr = nullptr, int *orange = nullptr);
 size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext);
 int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const int32_t *bc,
                     const int32_t *pad, const float *res, int unit_res, uint8_t *E, float *A,
@@ -54,6 +54,8 @@ struct GrowSel {
     // step k's blocks are ev[off[k] .. off[k + 1])
     int *ev = nullptr;
     int *off = nullptr;
+    // profiler label of the union step
+    const char *unite_label = "k_grow_unite";
 };
 // Per-step lists of the blocks of a step volume S (steps < nsteps; 255:
 // never) that grow at that step, in one allocation *mem (freed by the caller).
@@ -76,8 +78,9 @@ int grow_marks_step(GrowSel &g, const uint8_t *S, int k, const int64_t *shape, c
                     const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
 // ... and the inlet selection of a constrained by b (when *b_count > 0) in one
 // pass; kept counts a's inlet-connected voxels.
+// xr (optional): the x range of the output's set (kRangeBig encoding)
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
-                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept);
+                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept, int *xr = nullptr);
 // Selection of a set that only shrinks (the drainage's wetting phase): full
 // block union-find every step, but tiles the producer did not flag reuse
 // their tile-local parents Pl.  Scratch of shrink_sel_bytes(shape) bytes.
@@ -104,10 +107,16 @@ int bcc_marks_binary(const uint8_t *img, int fgval, const int64_t *shape, const 
 // connection from its block union-find (P, M, mark from bcc_marks_binary with
 // the outlet box); maintains g_nw's masks when given.
 // With wdirty, M (the wetting phase's masks) is brought up to date and the
-// tiles whose masks changed are flagged.
+// tiles whose masks changed are flagged.  orange (device, voxel x range
+// [lo, hi] in whole blocks, null: everything): the only blocks that can
+// change; ranged: the counts are changes since the last update rather than
+// totals (drain_totals keeps the running totals).
 int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape, int *P, uint8_t *M,
                         const uint8_t *mark, const Boxes &B, GrowSel *g_nw, unsigned long long *cnt2_own,
-                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty = nullptr);
+                        unsigned long long *cnt1, int *err, cudaStream_t st, int *wdirty = nullptr,
+                        const int *orange = nullptr, bool ranged = false);
+int drain_totals(bool ranged, const unsigned long long *cnt2, const unsigned long long *cnt1, unsigned long long *tot,
+                 unsigned long long *sat_out, unsigned long long *ones_out, cudaStream_t st);
 int check_err(int *err, cudaStream_t st);
 int check_volume(const int64_t *shape);
 
