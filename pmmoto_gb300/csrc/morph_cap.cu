@@ -218,10 +218,13 @@ constexpr int kCapChunk = 8; // heights loaded ahead per line (memory-level para
 // AX = 0: lines over (x1 in [j0, j0 + nj), x2 in [k0, k0 + nk)) along axis 0.
 // One thread per line; each loop trip loads the next kCapChunk heights before
 // it processes the current ones, so a thread keeps several loads in flight.
+// Lines are cut into nseg segments: an output at x depends only on the
+// heights within W of it, so a segment [a, b) is exact when its sweep starts
+// at a - W (2W extra steps per segment buy nseg times the threads).
 template <int AX, int RING>
 __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA, uint16_t *__restrict__ KB,
                                                  CapGeo G, int T, int W, const unsigned long long *__restrict__ gate,
-                                                 const int *__restrict__ xr)
+                                                 const int *__restrict__ xr, int nseg)
 {
     if (gate && *gate == 0)
         return;
@@ -232,26 +235,33 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
     const long long nlines = (long long)(AX == 1 ? G.X0 : G.nj) * G.nk;
     const long long st = AX == 1 ? (long long)G.X2 : (long long)G.X1 * G.X2;
     const int n = AX == 1 ? G.X1 : G.X0;
+    const int seglen = (n + nseg - 1) / nseg;
     const int big = T + 1;
-    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
-         li += (long long)gridDim.x * blockDim.x) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nlines * nseg;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int seg = (int)(g / nlines);
+        const long long li = g - (long long)seg * nlines;
         const long long q = li / G.nk;
         if (AX == 1 && xr && (q < sr.hlo || q > sr.hhi))
+            continue;
+        const int a = seg * seglen, b = min(n, a + seglen);
+        if (a >= b)
             continue;
         const int x2 = G.k0 + (int)(li - q * G.nk);
         const long long base = AX == 1 ? q * G.X1 * G.X2 + x2 : (G.j0 + q) * G.X2 + x2;
         const uint16_t *in = KA + base;
         uint16_t *out = KB + base;
         CapLine<RING> L{ring + threadIdx.x, 0, -1, 0};
+        const int i_first = max(0, a - W), i_last = b - 1 + W; // steps; step i emits x = i - W
         int cur[kCapChunk];
-        const uint16_t *pin = in; // next height to prefetch
+        const uint16_t *pin = in + (long long)i_first * st; // next height to prefetch
 #pragma unroll
         for (int u = 0; u < kCapChunk; u++) {
-            cur[u] = u < n ? (int)*pin : big;
+            cur[u] = i_first + u < n ? (int)*pin : big;
             pin += st;
         }
-        uint16_t *po = out; // output position x = i - W
-        for (int i0 = 0; i0 < n + W; i0 += kCapChunk) {
+        uint16_t *po = out + (long long)a * st; // output position x = i - W
+        for (int i0 = i_first; i0 <= i_last; i0 += kCapChunk) {
             int nxt[kCapChunk];
 #pragma unroll
             for (int u = 0; u < kCapChunk; u++) {
@@ -263,7 +273,7 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
                 const int i = i0 + u;
                 const int v = L.step(i, cur[u], T, W, big);
                 const int x = i - W;
-                if (x >= 0 && x < n) {
+                if (x >= a && x < b) {
                     *po = (uint16_t)v;
                     po += st;
                 }
@@ -393,13 +403,17 @@ template <int AX>
 static int launch_cap_mid(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, int W, long long lines,
                           cudaStream_t st, const unsigned long long *gate = nullptr, const int *xr = nullptr)
 {
-    const unsigned grid = grid_for(lines, 128, 1LL << 30);
+    // segments of at least 4 W + 32 positions, at most 4 per line
+    const int n = AX == 1 ? G.X1 : G.X0;
+    int nseg = n / (4 * W + 32);
+    nseg = nseg < 1 ? 1 : nseg > 4 ? 4 : nseg;
+    const unsigned grid = grid_for(lines * nseg, 128, 1LL << 30);
     if (2 * W + 2 <= 16)
-        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr);
+        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg);
     else if (2 * W + 2 <= 32)
-        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr);
+        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg);
     else
-        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr);
+        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg);
     return PMG_OK;
 }
 
