@@ -1817,50 +1817,23 @@ void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape)
 
 // One step of a growing selection up to the marks: the full block union-find
 // the first time, afterwards the grown blocks only.
-// Parent of a block that has just become non-empty (fresh): the first block
-// of its run of fresh blocks in the warp, where each lane's block follows the
-// previous lane's in the same row (prev_adj) and the two touch across their
-// common z face; a run's first block is its own root.  The run is connected,
-// and its first block has the smallest index.  Every lane of the warp calls it.
-__device__ __forceinline__ int fresh_run_parent(int b, bool fresh, unsigned m, bool prev_adj)
-{
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const unsigned pm = __shfl_up_sync(FULL, m, 1);
-    const int pf = __shfl_up_sync(FULL, (int)fresh, 1);
-    const bool link = fresh && lane > 0 && pf && prev_adj && (m & 0x55u) && (pm & 0xAAu);
-    const unsigned lm = __ballot_sync(FULL, link);
-    const unsigned upto = lane == 31 ? FULL : ((2u << lane) - 1u);
-    const int head = 31 - __clz(~lm & upto);
-    return b - (lane - head);
-}
-
 // Listed blocks take their masks from the source (steps known in advance).
 template <class Src>
 __global__ void k_grow_apply(Src src, uint8_t *__restrict__ M, int *__restrict__ P, BGrid G,
                              const int *__restrict__ list, const int *__restrict__ off, int *err)
 {
     const int a = off[0], cnt = off[1] - a;
-    const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < cnt; base += gridDim.x * blockDim.x) {
-        const int it = base + lane;
-        const bool has = it < cnt;
-        const int b = has ? list[a + it] : -2;
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
+        const int b = list[a + it];
         const int r = b / G.b2;
         const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
-        unsigned old = 0, m = 0;
-        if (has) {
-            old = M[b];
-            m = block_mask(src, G, c0, c1, c2);
-            if (old & ~m)
-                atomicExch(err, 3);
-            M[b] = (uint8_t)m;
-        }
-        const bool fresh = has && !old && m;
-        const int pb = __shfl_up_sync(0xffffffffu, b, 1);
-        const int parent = fresh_run_parent(b, fresh, m, has && c2 > 0 && pb == b - 1);
-        if (fresh)
-            P[b] = parent;
+        const unsigned old = M[b];
+        const unsigned m = block_mask(src, G, c0, c1, c2);
+        if (old & ~m)
+            atomicExch(err, 3);
+        M[b] = (uint8_t)m;
+        if (!old)
+            P[b] = b;
     }
 }
 
@@ -2335,8 +2308,7 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
     const long long sx = (long long)G.s1 * G.s2, sy = G.s2;
     for (int base = blockIdx.x * blockDim.x; base < nb; base += gridDim.x * blockDim.x) {
         const int b = base + threadIdx.x;
-        bool changed = false, fresh = false, zrow = false;
-        unsigned mfresh = 0;
+        bool changed = false;
         const int rr = b / G.b2, cc0 = rr / G.b1;
         const bool in_dil = cc0 >= bxlo && cc0 <= bxhi;
         if (b < nb && (in_dil || !ranged)) {
@@ -2433,18 +2405,13 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                     if (old & ~nwm)
                         atomicExch(err, 3);
                     Mn[b] = (uint8_t)nwm;
-                    fresh = !old;
+                    if (!old)
+                        Pn[b] = b;
                     changed = true;
                 }
-                mfresh = nwm;
-                zrow = c2b > 0;
             }
         }
         if (Mn) {
-            // consecutive lanes hold consecutive blocks
-            const int parent = fresh_run_parent(b, fresh, mfresh, zrow);
-            if (fresh)
-                Pn[b] = parent;
             const unsigned bal = __ballot_sync(0xffffffffu, changed);
             if (bal) {
                 int pos = 0;

@@ -298,9 +298,11 @@ __device__ __forceinline__ int isqrt_small(int m)
 
 // gate: a count of the seeds held in device memory (null: always seeds); when
 // it is zero the dilation is empty and only zeros are written.
+// Lines are cut into nseg segments of outputs, each swept from W positions
+// before its first output (heights farther away cannot reach it).
 __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ KB, CapGeo G, int T, int W,
                                                   MorphEpi me, const unsigned long long *__restrict__ gate,
-                                                  const int *__restrict__ xr, int *__restrict__ orange)
+                                                  const int *__restrict__ xr, int *__restrict__ orange, int nseg)
 {
     SeedRange sr{0, G.X0 - 1, 0, G.X0 - 1};
     if (xr)
@@ -333,12 +335,17 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
     // positions x of the line that lie in the unextended volume (and in the
     // output range of the seeds)
     const int xlo = max(max(0, me.e0), sr.olo), xhi = min(min(n, me.e0 + (int)me.o0), sr.ohi + 1);
-    // heights exist on [sr.hlo, sr.hhi] only; the sweep starts where either the
-    // first height or the first output is due
-    const int istart = min(sr.hlo, xlo + W) < 0 ? 0 : min(sr.hlo, xlo + W);
-    const int iend = xhi - 1 + W; // last step that emits an output
-    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
-         li += (long long)gridDim.x * blockDim.x) {
+    const int seglen = (n + nseg - 1) / nseg;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nlines * nseg;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int seg = (int)(g / nlines);
+        const long long li = g - (long long)seg * nlines;
+        // this segment's outputs [ax, bx); heights exist on [sr.hlo, sr.hhi]
+        // only, and the sweep starts W steps before the first output
+        const int ax = max(xlo, seg * seglen), bx = min(xhi, (seg + 1) * seglen);
+        if (ax >= bx)
+            continue;
+        const int istart = max(0, ax - W), iend = bx - 1 + W;
         const int x1 = G.j0 + (int)(li / G.nk);
         const int x2 = G.k0 + (int)(li - (li / G.nk) * G.nk);
         const uint16_t *in = KB + (long long)x1 * G.X2 + x2;
@@ -346,7 +353,7 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
         const bool wall_jk = (me.wall[2] && jo == 0) || (me.wall[3] && jo == me.o1 - 1) ||
                              (me.wall[4] && ko == 0) || (me.wall[5] && ko == me.o2 - 1);
         const long long ost = me.o1 * me.o2;
-        uint8_t *dst = me.out + jo * me.o2 + ko + (long long)(xlo - me.e0) * ost; // output of x = xlo
+        uint8_t *dst = me.out + jo * me.o2 + ko + (long long)(ax - me.e0) * ost; // output of x = ax
         // wall planes of axis 0 (unextended coordinates 0 and o0 - 1)
         const int xw0 = me.wall[0] ? me.e0 : -1, xw1 = me.wall[1] ? me.e0 + (int)me.o0 - 1 : -1;
         const uint8_t in_v = me.dilate ? 1 : 0, out_v = me.dilate ? 0 : 1;
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
                 if (reach >= i && i < n)
                     pend |= 1ull;
                 const int x = i - W;
-                if (x < xlo || x >= xhi)
+                if (x < ax || x >= bx)
                     continue;
                 uint8_t v = ((pend >> W) & 1ull) ? in_v : out_v;
                 if (wall_jk || x == xw0 || x == xw1)
@@ -468,7 +475,11 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
     {
         const long long lines = (long long)G.nj * G.nk;
         const int ps__ = prof_begin("k_cap_last", st);
-        k_cap_last<<<grid_for(lines, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate, xr, orange);
+        // one segment per line: this pass is short per voxel, the extra sweep
+        // of a cut costs more than the threads it adds
+        const int nseg = 1;
+        k_cap_last<<<grid_for(lines * nseg, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate, xr, orange,
+                                                                           nseg);
         prof_end(ps__, (double)lines * G.X0 * 2 + (double)me.o0 * me.o1 * me.o2, st);
     }
     PMG_CHECK_LAUNCH();
