@@ -2301,17 +2301,21 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
     // (voxels leaving value 2 inside the own box, voxels newly 1) instead of
     // the totals.
     const int bxlo = orange ? orange[0] >> 1 : 0, bxhi = orange ? orange[1] >> 1 : G.b0 - 1;
+    // a ranged update walks the dilation's block planes only
+    const int plane = G.b1 * G.b2;
+    const int bstart = ranged ? max(0, bxlo) * plane : 0;
     const int nb = G.b0 * G.b1 * G.b2;
+    const int bend = ranged ? min(nb, max(0, bxhi + 1) * plane) : nb;
     const int lane = threadIdx.x & 31;
     unsigned int c2 = 0, c1 = 0;
     const bool pairs = !(G.s2 & 1);
     const long long sx = (long long)G.s1 * G.s2, sy = G.s2;
-    for (int base = blockIdx.x * blockDim.x; base < nb; base += gridDim.x * blockDim.x) {
+    for (int base = bstart + blockIdx.x * blockDim.x; base < bend; base += gridDim.x * blockDim.x) {
         const int b = base + threadIdx.x;
         bool changed = false;
         const int rr = b / G.b2, cc0 = rr / G.b1;
         const bool in_dil = cc0 >= bxlo && cc0 <= bxhi;
-        if (b < nb && (in_dil || !ranged)) {
+        if (b < bend && (in_dil || !ranged)) {
             const int r = b / G.b2;
             const int c2b = b - r * G.b2, c0 = r / G.b1, c1b = r - (r / G.b1) * G.b1;
             const int i0 = 2 * c0, j0 = 2 * c1b, k0 = 2 * c2b;

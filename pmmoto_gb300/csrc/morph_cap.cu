@@ -99,12 +99,10 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const int big = T + 1;
-    for (long long r = warp; r < rows; r += nwarps) {
-        if (xr) {
-            const int x0 = (int)(r / rs.X1);
-            if (x0 < sr.hlo || x0 > sr.hhi)
-                continue;
-        }
+    // with a seed range, only the rows of its planes
+    const long long r0 = xr ? (long long)max(sr.hlo, 0) * rs.X1 : 0;
+    const long long r1 = xr ? min(rows, (long long)(sr.hhi + 1) * rs.X1) : rows;
+    for (long long r = r0 + warp; r < r1; r += nwarps) {
         const uint8_t *src = E + r * X2;
         bool wrow = false;
         if (rs.raw) {
@@ -237,13 +235,15 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
     const int n = AX == 1 ? G.X1 : G.X0;
     const int seglen = (n + nseg - 1) / nseg;
     const int big = T + 1;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nlines * nseg;
+    // with a seed range (axis-1 lines), only the lines of its planes
+    const long long l0 = AX == 1 && xr ? (long long)max(sr.hlo, 0) * G.nk : 0;
+    const long long l1 = AX == 1 && xr ? min(nlines, (long long)(sr.hhi + 1) * G.nk) : nlines;
+    const long long span = l1 > l0 ? l1 - l0 : 0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < span * nseg;
          g += (long long)gridDim.x * blockDim.x) {
-        const int seg = (int)(g / nlines);
-        const long long li = g - (long long)seg * nlines;
+        const int seg = (int)(g / span);
+        const long long li = l0 + (g - (long long)seg * span);
         const long long q = li / G.nk;
-        if (AX == 1 && xr && (q < sr.hlo || q > sr.hhi))
-            continue;
         const int a = seg * seglen, b = min(n, a + seglen);
         if (a >= b)
             continue;
