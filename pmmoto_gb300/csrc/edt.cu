@@ -385,9 +385,95 @@ __device__ int boundary_hull(Stack &S, const float *line, long long st, int star
 // ---------------------------------------------------------------------------
 // envelope pass along axis `ax`: fin -> fout (out of place)
 // ---------------------------------------------------------------------------
-__global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
-                           float res, pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me,
-                           int redo)
+
+// The imported boundary hulls of a periodic line (return_boundary_hull on the
+// segment before the first zero and after the last zero, the far end's hull
+// becoming the lower imports): lower imports into S, upper ones into up_*.
+__device__ __forceinline__ void load_imports(Stack &S, const float *line, long long st, int n, float aniso,
+                                             const pmg_axis_cfg &cfg, int num_hull, int *up_v, float *up_h,
+                                             float *up_r, int &n_up)
+{
+    // first / last zero (a zero height is exactly a zero voxel of the
+    // original image: pass 0 gives 0 only there and every later pass keeps
+    // it, all other values being >= res^2 > 0)
+    int bf = -1, bb = -1;
+    for (int i = cfg.hf_lo; i < n; i++)
+        if (line[i * st] == 0.0f) {
+            bf = i;
+            break;
+        }
+    for (int i = n - cfg.hb_hi - 1; i >= 0; i--)
+        if (line[i * st] == 0.0f) {
+            bb = i;
+            break;
+        }
+    // near end (forward) -> upper imports
+    int start, nv, corr;
+    if (bf == -1) {
+        start = cfg.hf_lo;
+        nv = n - cfg.hf_lo;
+    } else {
+        start = cfg.hf_lo;
+        nv = bf - cfg.hf_lo + 1;
+    }
+    corr = 0;
+    n_up = boundary_hull(S, line, st, start, nv, aniso, num_hull, corr, true, up_v, up_h, up_r);
+    // far end (backward) -> lower imports, given in top-down order
+    int lo_v[kMaxHull];
+    float lo_h[kMaxHull], lo_r[kMaxHull];
+    if (bb == -1) {
+        start = 0;
+        nv = n - cfg.hb_hi;
+    } else {
+        start = bb;
+        nv = n - bb - cfg.hb_hi;
+    }
+    corr = -nv;
+    const int n_lo = boundary_hull(S, line, st, start, nv, aniso, num_hull, corr, false, lo_v, lo_h, lo_r);
+    // the reference pushes the lower list in reverse (rbegin..rend)
+    for (int j = 0; j < n_lo; j++) {
+        S.lv[j] = lo_v[n_lo - 1 - j];
+        S.lh[j] = lo_h[n_lo - 1 - j];
+        S.lr[j] = lo_r[n_lo - 1 - j];
+    }
+    S.nl = n_lo;
+}
+
+// Evaluation sweep over the final stack (bottom to top), written for
+// positions [i_lo, i_hi) of the line.
+__device__ __forceinline__ void evaluate(Stack &S, const float *line, long long st, int nwords, float aniso,
+                                         int form, const MorphEpi &me, const LineGeo &g, float *o, int i_lo,
+                                         int i_hi)
+{
+    Iter it{0, 0};
+    Entry cur, nxt;
+    int is_lower;
+    float given_r;
+    iter_next(S, it, line, st, nwords, cur, is_lower, given_r);
+    bool has_next = iter_next(S, it, line, st, nwords, nxt, is_lower, given_r);
+    float nr = has_next ? (is_lower ? given_r : isect(nxt.h, (float)nxt.v, cur.h, (float)cur.v, aniso)) : INFINITY;
+    for (int i = i_lo; i < i_hi; i++) {
+        const float fi = (float)i;
+        while (nr < fi) {
+            cur = nxt;
+            has_next = iter_next(S, it, line, st, nwords, nxt, is_lower, given_r);
+            nr = has_next ? (is_lower ? given_r : isect(nxt.h, (float)nxt.v, cur.h, (float)cur.v, aniso))
+                          : INFINITY;
+        }
+        const float dx = (float)(i - cur.v);
+        float val = fadd(fmul(aniso, fmul(dx, dx)), cur.h);
+        if (form == PMG_EDT_MORPH) {
+            morph_store(me, g, i, val);
+            continue;
+        }
+        if (form == PMG_EDT_DIST)
+            val = __fsqrt_rn(val);
+        o[i * st] = val;
+    }
+}
+
+__global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
+                           pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me, int redo)
 {
     const long long nlines = Ls.count();
     extern __shared__ uint32_t smem_bm[];
@@ -411,54 +497,8 @@ __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fo
         int up_v[kMaxHull];
         float up_h[kMaxHull], up_r[kMaxHull];
         int n_up = 0;
-        if (cfg.periodic) {
-            // first / last zero (a zero height is exactly a zero voxel of the
-            // original image: pass 0 gives 0 only there and every later pass
-            // keeps it, all other values being >= res^2 > 0)
-            int bf = -1, bb = -1;
-            for (int i = cfg.hf_lo; i < n; i++)
-                if (line[i * st] == 0.0f) {
-                    bf = i;
-                    break;
-                }
-            for (int i = n - cfg.hb_hi - 1; i >= 0; i--)
-                if (line[i * st] == 0.0f) {
-                    bb = i;
-                    break;
-                }
-            // near end (forward) -> upper imports
-            int start, nv, corr;
-            if (bf == -1) {
-                start = cfg.hf_lo;
-                nv = n - cfg.hf_lo;
-            } else {
-                start = cfg.hf_lo;
-                nv = bf - cfg.hf_lo + 1;
-            }
-            corr = 0;
-            n_up = boundary_hull(S, line, st, start, nv, aniso, num_hull, corr, true, up_v, up_h,
-                                 up_r);
-            // far end (backward) -> lower imports, given in top-down order
-            int lo_v[kMaxHull];
-            float lo_h[kMaxHull], lo_r[kMaxHull];
-            if (bb == -1) {
-                start = 0;
-                nv = n - cfg.hb_hi;
-            } else {
-                start = bb;
-                nv = n - bb - cfg.hb_hi;
-            }
-            corr = -nv;
-            const int n_lo = boundary_hull(S, line, st, start, nv, aniso, num_hull, corr, false,
-                                           lo_v, lo_h, lo_r);
-            // the reference pushes the lower list in reverse (rbegin..rend)
-            for (int j = 0; j < n_lo; j++) {
-                S.lv[j] = lo_v[n_lo - 1 - j];
-                S.lh[j] = lo_h[n_lo - 1 - j];
-                S.lr[j] = lo_r[n_lo - 1 - j];
-            }
-            S.nl = n_lo;
-        }
+        if (cfg.periodic)
+            load_imports(S, line, st, n, aniso, cfg, num_hull, up_v, up_h, up_r, n_up);
         // main build
         int loop_start;
         if (S.nl > 0) {
@@ -481,34 +521,223 @@ __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fo
             insert(S, line, st, i, vh(line, st, i), aniso, 0);
         for (int j = 0; j < n_up; j++)
             insert(S, line, st, up_v[j] + n, up_h[j], aniso, 1);
+        evaluate(S, line, st, nwords, aniso, form, me, g, fout + g.base, 0, n);
+    }
+}
 
-        // evaluation sweep
-        Iter it{0, 0};
-        Entry cur, nxt;
-        int is_lower;
-        float given_r;
-        iter_next(S, it, line, st, nwords, cur, is_lower, given_r);
-        bool has_next = iter_next(S, it, line, st, nwords, nxt, is_lower, given_r);
-        float nr = has_next ? (is_lower ? given_r : isect(nxt.h, (float)nxt.v, cur.h, (float)cur.v, aniso))
-                            : INFINITY;
-        float *o = fout + g.base;
-        for (int i = 0; i < n; i++) {
-            const float fi = (float)i;
-            while (nr < fi) {
-                cur = nxt;
-                has_next = iter_next(S, it, line, st, nwords, nxt, is_lower, given_r);
-                nr = has_next ? (is_lower ? given_r : isect(nxt.h, (float)nxt.v, cur.h, (float)cur.v, aniso))
-                              : INFINITY;
+// ---------------------------------------------------------------------------
+// periodic lines with power-of-two voxels: windowed exact minimum + end
+// segments
+// ---------------------------------------------------------------------------
+// Every height is an exact integer multiple K * res^2, and a zero height (a
+// solid voxel) shields everything beyond it: at x, a parabola beyond the
+// nearest zero on either side is above that zero's value.  So the result at x
+// is the exact minimum of K_v + (x - v)^2 over the voxels v that the scan
+// outward from x reaches before (x - v)^2 exceeds the best value, and the
+// reference's float32 envelope returns exactly that minimum there (the
+// rounding argument of edt_exact.cu) -- unless the scan runs off the end of
+// a periodic line, where the imported boundary hulls (a truncated set) come
+// into play.  k_env_window computes every voxel whose scan stays inside the
+// line and flags the lines with one that does not; k_envelope_ends then
+// replays the reference's float envelope on those lines' end segments only:
+// the lower imports with the voxels up to the first zero, and the voxels from
+// the last zero with the upper imports.  No parabola can pop a zero off the
+// stack, so these partial stacks and sweeps make the same float decisions as
+// the whole line's.  A line without a zero, with a height that is not an
+// exact integer, or with a scan longer than kWinMax is flagged for the whole
+// float envelope.
+
+constexpr int kWinMax = 64;
+
+__global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float a,
+                             float inv_a, int periodic, int form, int *__restrict__ flag)
+{
+    const long long nlines = Ls.count();
+    const LineGeo g0 = line_addr(Ls, 0);
+    const int n = g0.n;
+    const bool contiguous = g0.stride == 1;
+    const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
+    const long long total = nlines * n;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        // consecutive threads: along the line when it is contiguous, across
+        // neighbouring lines otherwise (coalesced either way)
+        long long li;
+        int x;
+        if (contiguous) {
+            li = q / n;
+            x = (int)(q - li * n);
+        } else {
+            x = (int)(q / nlines);
+            li = q - (long long)x * nlines;
+        }
+        const LineGeo g = line_addr(Ls, li);
+        const float *line = fin + g.base;
+        const long long st = g.stride;
+        const float f = line[x * st];
+        float *o = fout + g.base + x * st;
+        if (f == 0.0f) {
+            *o = 0.0f;
+            continue;
+        }
+        const float kf = fmul(f, inv_a);
+        int best = (int)kf;
+        if ((float)best != kf || kf >= kmax) {
+            atomicOr(flag + li, 2);
+            continue;
+        }
+        bool ldone = false, rdone = false, off_end = false, whole = false;
+        for (int t = 1; t * t < best; t++) {
+            if (t > kWinMax) {
+                whole = true;
+                break;
             }
-            const float dx = (float)(i - cur.v);
-            float val = fadd(fmul(aniso, fmul(dx, dx)), cur.h);
-            if (form == PMG_EDT_MORPH) {
-                morph_store(me, g, i, val);
+            if (!ldone) {
+                const int v = x - t;
+                if (v < 0) {
+                    if (periodic) {
+                        off_end = true;
+                        break;
+                    }
+                    ldone = true;
+                } else {
+                    const float fv = line[v * st];
+                    const float kv = fmul(fv, inv_a);
+                    const int Kv = (int)kv;
+                    if ((float)Kv != kv || kv >= kmax) {
+                        whole = true;
+                        break;
+                    }
+                    best = min(best, Kv + t * t);
+                    ldone = Kv == 0;
+                }
+            }
+            if (!rdone) {
+                const int v = x + t;
+                if (v >= n) {
+                    if (periodic) {
+                        off_end = true;
+                        break;
+                    }
+                    rdone = true;
+                } else {
+                    const float fv = line[v * st];
+                    const float kv = fmul(fv, inv_a);
+                    const int Kv = (int)kv;
+                    if ((float)Kv != kv || kv >= kmax) {
+                        whole = true;
+                        break;
+                    }
+                    best = min(best, Kv + t * t);
+                    rdone = Kv == 0;
+                }
+            }
+            if (ldone && rdone)
+                break;
+        }
+        if (whole || off_end) {
+            // bit 1: the whole line needs the float envelope; bit 0: its ends
+            const int want = whole ? 2 : 1;
+            if ((flag[li] & want) == 0)
+                atomicOr(flag + li, want);
+            continue;
+        }
+        float val = fmul((float)best, a);
+        if (form == PMG_EDT_DIST)
+            val = __fsqrt_rn(val);
+        *o = val;
+    }
+}
+
+__global__ void k_envelope_ends(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
+                                pmg_axis_cfg cfg, int num_hull, int form, const int *__restrict__ flag)
+{
+    const long long nlines = Ls.count();
+    extern __shared__ uint32_t smem_bm[];
+    const float aniso = fmul(res, res);
+    const MorphEpi none{};
+    Stack S;
+    S.bm = smem_bm + threadIdx.x;
+    S.nthr = blockDim.x;
+    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
+         li += (long long)gridDim.x * blockDim.x) {
+        const int fl = flag[li];
+        if (!fl)
+            continue;
+        const LineGeo g = line_addr(Ls, li);
+        const float *line = fin + g.base;
+        const long long st = g.stride;
+        const int n = g.n;
+        const int nwords = (n + 31) >> 5;
+        int z1 = -1, z2 = -1;
+        for (int i = 0; i < n; i++)
+            if (line[i * st] == 0.0f) {
+                z1 = i;
+                break;
+            }
+        for (int i = n - 1; i >= 0; i--)
+            if (line[i * st] == 0.0f) {
+                z2 = i;
+                break;
+            }
+        S.clear(nwords);
+        S.nl = 0;
+        S.nu = 0;
+        int up_v[kMaxHull];
+        float up_h[kMaxHull], up_r[kMaxHull];
+        int n_up = 0;
+        if (cfg.periodic)
+            load_imports(S, line, st, n, aniso, cfg, num_hull, up_v, up_h, up_r, n_up);
+        const bool whole = (fl & 2) || z1 < 0;
+        const int lo_end = whole ? n - 1 : z1; // last native of the lower stack
+        // lower part: the imports below, natives up to lo_end
+        if (whole || z1 > 0) {
+            int loop_start;
+            if (S.nl > 0) {
+                loop_start = 0;
+                S.nn = 0;
+                S.ntv = -1;
+                S.tv = S.lv[S.nl - 1];
+                S.th = S.lh[S.nl - 1];
+                S.tr = S.lr[S.nl - 1];
+            } else {
+                loop_start = 1;
+                S.setbit(0);
+                S.nn = 1;
+                S.ntv = 0;
+                S.tv = 0;
+                S.th = vh(line, st, 0);
+                S.tr = -INFINITY;
+            }
+            for (int i = loop_start; i <= lo_end; i++)
+                insert(S, line, st, i, vh(line, st, i), aniso, 0);
+            if (whole) {
+                for (int j = 0; j < n_up; j++)
+                    insert(S, line, st, up_v[j] + n, up_h[j], aniso, 1);
+                evaluate(S, line, st, nwords, aniso, form, none, g, fout + g.base, 0, n);
+                S.clear(nwords);
                 continue;
             }
-            if (form == PMG_EDT_DIST)
-                val = __fsqrt_rn(val);
-            o[i * st] = val;
+            evaluate(S, line, st, nwords, aniso, form, none, g, fout + g.base, 0, z1);
+            S.clear(nwords);
+        }
+        // upper part: the zero at z2 at the bottom, natives above it, the
+        // upper imports on top
+        if (z2 < n - 1) {
+            S.nl = 0;
+            S.nu = 0;
+            S.setbit(z2);
+            S.nn = 1;
+            S.ntv = z2;
+            S.tv = z2;
+            S.th = 0.0f;
+            S.tr = -INFINITY;
+            for (int i = z2 + 1; i < n; i++)
+                insert(S, line, st, i, vh(line, st, i), aniso, 0);
+            for (int j = 0; j < n_up; j++)
+                insert(S, line, st, up_v[j] + n, up_h[j], aniso, 1);
+            evaluate(S, line, st, nwords, aniso, form, none, g, fout + g.base, z2 + 1, n);
+            S.clear(nwords);
         }
     }
 }
@@ -539,6 +768,18 @@ static int envelope_block(int n)
     return block;
 }
 
+// power-of-two voxel size and lines of at most 1024 voxels (imported hull
+// vertices then stay within the exact float range of the reference's
+// intersection arithmetic)
+static bool window_path_ok(float res, int n)
+{
+    if (n > 1024 || !(res > 0.0f))
+        return false;
+    int ex = 0;
+    const float m = frexpf(res, &ex);
+    return m == 0.5f && ex > -40 && ex < 40;
+}
+
 int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                     const pmg_axis_cfg &cfg, int num_hull, int form, const MorphEpi &me,
                     cudaStream_t st, int cap)
@@ -549,6 +790,31 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     if (smem > 48 * 1024)
         PMG_CUDA(cudaFuncSetAttribute(k_envelope, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
+    if (cfg.periodic && form != PMG_EDT_MORPH && window_path_ok(res, n)) {
+        // windowed exact minimum everywhere, the float envelope on the end
+        // segments (or whole lines) the window kernel flags
+        const long long nl = Ls.count();
+        int *flag = nullptr;
+        PMG_TRY(scratch_alloc((void **)&flag, sizeof(int) * (size_t)nl, st));
+        int s = cudaMemsetAsync(flag, 0, sizeof(int) * (size_t)nl, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        if (s == PMG_OK) {
+            const float a = res * res;
+            const int ps__ = prof_begin("k_env_window", st);
+            k_env_window<<<grid_for(nl * n, 256, 152LL * 32), 256, 0, st>>>(fin, fout, Ls, a, 1.0f / a, 1, form,
+                                                                           flag);
+            prof_end(ps__, (double)nl * n * 8, st);
+            s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        }
+        if (s == PMG_OK) {
+            const int ps__ = prof_begin("k_envelope_ends", st);
+            k_envelope_ends<<<grid_for(nl, block, 1LL << 30), block, smem, st>>>(fin, fout, Ls, res, cfg, num_hull,
+                                                                                form, flag);
+            prof_end(ps__, 0.0, st);
+            s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        }
+        const int s2 = scratch_free(flag, st);
+        return s != PMG_OK ? s : s2;
+    }
     int redo = 0;
     if (exact_path_ok(res, cfg, n)) {
         // exact integer streaming pass; lines it cannot finish are redone below

@@ -56,6 +56,26 @@ def test_edt3d_random_vs_oracle(D, seed):
     np.testing.assert_array_equal(D.edt3d(img, periodic=per, resolution=res), np.sqrt(want))
 
 
+@pytest.mark.parametrize("seed", range(16))
+def test_edt3d_periodic_pow2_vs_oracle(D, seed):
+    """Periodic axes with power-of-two voxels: windowed exact minima in the
+    line interiors, the float envelope on the end segments and on lines
+    without a solid voxel."""
+    rng = np.random.default_rng(300 + seed)
+    shape = tuple(int(x) for x in rng.integers(1, 61, 3))
+    p0 = float([0.02, 0.1, 0.3, 0.5, 0.7, 0.9, 0.98, 0.999][seed % 8])
+    img = (rng.random(shape) >= p0).astype(np.uint8)
+    if seed % 5 == 4:
+        img = np.where(img > 0, rng.integers(1, 4, shape), 0).astype(np.uint8)
+    per = tuple(bool(x) for x in rng.integers(0, 2, 3))
+    if not any(per):
+        per = (True, True, True)
+    res = [(1.0, 1.0, 1.0), (0.5, 0.5, 0.5), (1 / 128, 1 / 128, 1 / 128), (0.25, 1.0, 2.0)][seed % 4]
+    got = D.edt3d(img, periodic=per, resolution=res, squared=True)
+    want = O.edt3d(img, periodic=per, resolution=res, squared=True)
+    np.testing.assert_array_equal(got, want)
+
+
 def test_edt_subdomain_golden(D, golden, golden_meta):
     from tests._helpers import geom_from_meta
     for ci, case in enumerate(golden_meta["sub_cases"]):
