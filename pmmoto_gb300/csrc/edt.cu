@@ -549,6 +549,75 @@ __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fo
 
 constexpr int kWinMax = 64;
 
+// One voxel: the exact windowed minimum (returns true and the value), or
+// false with the flag bits its line needs (2: the whole float envelope, 1: its
+// end segments).
+__device__ __forceinline__ bool window_voxel(const float *line, long long st, int n, int x, float inv_a, float kmax,
+                                             int periodic, int &best, int &need)
+{
+    const float f = line[x * st];
+    if (f == 0.0f) {
+        best = 0;
+        return true;
+    }
+    const float kf = fmul(f, inv_a);
+    best = (int)kf;
+    if ((float)best != kf || kf >= kmax) {
+        need = 2;
+        return false;
+    }
+    bool ldone = false, rdone = false;
+    for (int t = 1; t * t < best; t++) {
+        if (t > kWinMax) {
+            need = 2;
+            return false;
+        }
+        if (!ldone) {
+            const int v = x - t;
+            if (v < 0) {
+                if (periodic) {
+                    need = 1;
+                    return false;
+                }
+                ldone = true;
+            } else {
+                const float kv = fmul(line[v * st], inv_a);
+                const int Kv = (int)kv;
+                if ((float)Kv != kv || kv >= kmax) {
+                    need = 2;
+                    return false;
+                }
+                best = min(best, Kv + t * t);
+                ldone = Kv == 0;
+            }
+        }
+        if (!rdone) {
+            const int v = x + t;
+            if (v >= n) {
+                if (periodic) {
+                    need = 1;
+                    return false;
+                }
+                rdone = true;
+            } else {
+                const float kv = fmul(line[v * st], inv_a);
+                const int Kv = (int)kv;
+                if ((float)Kv != kv || kv >= kmax) {
+                    need = 2;
+                    return false;
+                }
+                best = min(best, Kv + t * t);
+                rdone = Kv == 0;
+            }
+        }
+        if (ldone && rdone)
+            break;
+    }
+    return true;
+}
+
+// Strided lines: one thread per line, neighbouring lines in neighbouring
+// lanes; contiguous lines: one warp per line, lanes 32 voxels apart.
 __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float a,
                              float inv_a, int periodic, int form, int *__restrict__ flag)
 {
@@ -557,95 +626,31 @@ __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ 
     const int n = g0.n;
     const bool contiguous = g0.stride == 1;
     const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
-    const long long total = nlines * n;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
-         q += (long long)gridDim.x * blockDim.x) {
-        // consecutive threads: along the line when it is contiguous, across
-        // neighbouring lines otherwise (coalesced either way)
-        long long li;
-        int x;
-        if (contiguous) {
-            li = q / n;
-            x = (int)(q - li * n);
-        } else {
-            x = (int)(q / nlines);
-            li = q - (long long)x * nlines;
-        }
+    const int lane = threadIdx.x & 31;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long first = contiguous ? tid >> 5 : tid, step = contiguous ? nthreads >> 5 : nthreads;
+    const int x0 = contiguous ? lane : 0, dx = contiguous ? 32 : 1;
+    for (long long li = first; li < nlines; li += step) {
         const LineGeo g = line_addr(Ls, li);
         const float *line = fin + g.base;
+        float *o = fout + g.base;
         const long long st = g.stride;
-        const float f = line[x * st];
-        float *o = fout + g.base + x * st;
-        if (f == 0.0f) {
-            *o = 0.0f;
-            continue;
-        }
-        const float kf = fmul(f, inv_a);
-        int best = (int)kf;
-        if ((float)best != kf || kf >= kmax) {
-            atomicOr(flag + li, 2);
-            continue;
-        }
-        bool ldone = false, rdone = false, off_end = false, whole = false;
-        for (int t = 1; t * t < best; t++) {
-            if (t > kWinMax) {
-                whole = true;
-                break;
+        int need = 0;
+        for (int x = x0; x < n; x += dx) {
+            int best = 0, nd = 0;
+            if (!window_voxel(line, st, n, x, inv_a, kmax, periodic, best, nd)) {
+                need |= nd;
+                continue;
             }
-            if (!ldone) {
-                const int v = x - t;
-                if (v < 0) {
-                    if (periodic) {
-                        off_end = true;
-                        break;
-                    }
-                    ldone = true;
-                } else {
-                    const float fv = line[v * st];
-                    const float kv = fmul(fv, inv_a);
-                    const int Kv = (int)kv;
-                    if ((float)Kv != kv || kv >= kmax) {
-                        whole = true;
-                        break;
-                    }
-                    best = min(best, Kv + t * t);
-                    ldone = Kv == 0;
-                }
-            }
-            if (!rdone) {
-                const int v = x + t;
-                if (v >= n) {
-                    if (periodic) {
-                        off_end = true;
-                        break;
-                    }
-                    rdone = true;
-                } else {
-                    const float fv = line[v * st];
-                    const float kv = fmul(fv, inv_a);
-                    const int Kv = (int)kv;
-                    if ((float)Kv != kv || kv >= kmax) {
-                        whole = true;
-                        break;
-                    }
-                    best = min(best, Kv + t * t);
-                    rdone = Kv == 0;
-                }
-            }
-            if (ldone && rdone)
-                break;
+            float val = fmul((float)best, a);
+            if (form == PMG_EDT_DIST)
+                val = __fsqrt_rn(val);
+            o[x * st] = val;
         }
-        if (whole || off_end) {
-            // bit 1: the whole line needs the float envelope; bit 0: its ends
-            const int want = whole ? 2 : 1;
-            if ((flag[li] & want) == 0)
-                atomicOr(flag + li, want);
-            continue;
-        }
-        float val = fmul((float)best, a);
-        if (form == PMG_EDT_DIST)
-            val = __fsqrt_rn(val);
-        *o = val;
+        // bit 1: the whole line needs the float envelope; bit 0: its ends
+        if (need)
+            atomicOr(flag + li, need);
     }
 }
 
@@ -800,8 +805,9 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
         if (s == PMG_OK) {
             const float a = res * res;
             const int ps__ = prof_begin("k_env_window", st);
-            k_env_window<<<grid_for(nl * n, 256, 152LL * 32), 256, 0, st>>>(fin, fout, Ls, a, 1.0f / a, 1, form,
-                                                                           flag);
+            const bool contiguous = Ls.ax == 2;
+            k_env_window<<<grid_for(contiguous ? nl * 32 : nl, 256, 152LL * 32), 256, 0, st>>>(
+                fin, fout, Ls, a, 1.0f / a, 1, form, flag);
             prof_end(ps__, (double)nl * n * 8, st);
             s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
