@@ -551,27 +551,29 @@ constexpr int kWinMax = 64;
 
 // One voxel: the exact windowed minimum (returns true and the value), or
 // false with the flag bits its line needs (2: the whole float envelope, 1: its
-// end segments).
+// end segments).  Heights are exact multiples of res^2 here (the passes
+// before only ever produce such values, or FLT_MAX for a line without a
+// solid voxel), so K = f / res^2 and every sum below are exact in float32.
 __device__ __forceinline__ bool window_voxel(const float *line, long long st, int n, int x, float inv_a, float kmax,
-                                             int periodic, int &best, int &need)
+                                             int periodic, float &best, int &need)
 {
     const float f = line[x * st];
     if (f == 0.0f) {
-        best = 0;
+        best = 0.0f;
         return true;
     }
-    const float kf = fmul(f, inv_a);
-    best = (int)kf;
-    if ((float)best != kf || kf >= kmax) {
+    best = fmul(f, inv_a);
+    if (best >= kmax) {
         need = 2;
         return false;
     }
     bool ldone = false, rdone = false;
-    for (int t = 1; t * t < best; t++) {
+    for (int t = 1; (float)(t * t) < best; t++) {
         if (t > kWinMax) {
             need = 2;
             return false;
         }
+        const float tt = (float)(t * t);
         if (!ldone) {
             const int v = x - t;
             if (v < 0) {
@@ -582,13 +584,12 @@ __device__ __forceinline__ bool window_voxel(const float *line, long long st, in
                 ldone = true;
             } else {
                 const float kv = fmul(line[v * st], inv_a);
-                const int Kv = (int)kv;
-                if ((float)Kv != kv || kv >= kmax) {
+                if (kv >= kmax) {
                     need = 2;
                     return false;
                 }
-                best = min(best, Kv + t * t);
-                ldone = Kv == 0;
+                best = fminf(best, fadd(kv, tt));
+                ldone = kv == 0.0f;
             }
         }
         if (!rdone) {
@@ -601,13 +602,12 @@ __device__ __forceinline__ bool window_voxel(const float *line, long long st, in
                 rdone = true;
             } else {
                 const float kv = fmul(line[v * st], inv_a);
-                const int Kv = (int)kv;
-                if ((float)Kv != kv || kv >= kmax) {
+                if (kv >= kmax) {
                     need = 2;
                     return false;
                 }
-                best = min(best, Kv + t * t);
-                rdone = Kv == 0;
+                best = fminf(best, fadd(kv, tt));
+                rdone = kv == 0.0f;
             }
         }
         if (ldone && rdone)
@@ -616,8 +616,11 @@ __device__ __forceinline__ bool window_voxel(const float *line, long long st, in
     return true;
 }
 
-// Strided lines: one thread per line, neighbouring lines in neighbouring
-// lanes; contiguous lines: one warp per line, lanes 32 voxels apart.
+// Strided lines: one thread per chunk of kWinChunk voxels of a line,
+// neighbouring lines in neighbouring lanes; contiguous lines: one warp per
+// line, lanes 32 voxels apart.
+constexpr int kWinChunk = 64;
+
 __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float a,
                              float inv_a, int periodic, int form, int *__restrict__ flag)
 {
@@ -625,25 +628,31 @@ __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ 
     const LineGeo g0 = line_addr(Ls, 0);
     const int n = g0.n;
     const bool contiguous = g0.stride == 1;
+    const int nchunk = contiguous ? 1 : (n + kWinChunk - 1) / kWinChunk;
     const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
     const int lane = threadIdx.x & 31;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long items = nlines * nchunk;
     const long long first = contiguous ? tid >> 5 : tid, step = contiguous ? nthreads >> 5 : nthreads;
-    const int x0 = contiguous ? lane : 0, dx = contiguous ? 32 : 1;
-    for (long long li = first; li < nlines; li += step) {
+    for (long long it = first; it < items; it += step) {
+        const int chunk = (int)(it / nlines);
+        const long long li = it - (long long)chunk * nlines;
         const LineGeo g = line_addr(Ls, li);
         const float *line = fin + g.base;
         float *o = fout + g.base;
         const long long st = g.stride;
         int need = 0;
-        for (int x = x0; x < n; x += dx) {
-            int best = 0, nd = 0;
+        const int x0 = contiguous ? lane : chunk * kWinChunk, dx = contiguous ? 32 : 1;
+        const int x1 = contiguous ? n : min(n, x0 + kWinChunk);
+        for (int x = x0; x < x1; x += dx) {
+            float best = 0.0f;
+            int nd = 0;
             if (!window_voxel(line, st, n, x, inv_a, kmax, periodic, best, nd)) {
                 need |= nd;
                 continue;
             }
-            float val = fmul((float)best, a);
+            float val = fmul(best, a);
             if (form == PMG_EDT_DIST)
                 val = __fsqrt_rn(val);
             o[x * st] = val;
@@ -806,7 +815,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
             const float a = res * res;
             const int ps__ = prof_begin("k_env_window", st);
             const bool contiguous = Ls.ax == 2;
-            k_env_window<<<grid_for(contiguous ? nl * 32 : nl, 256, 152LL * 32), 256, 0, st>>>(
+            k_env_window<<<grid_for(contiguous ? nl * 32 : nl * ((n + 63) / 64), 256, 152LL * 32), 256, 0, st>>>(
                 fin, fout, Ls, a, 1.0f / a, 1, form, flag);
             prof_end(ps__, (double)nl * n * 8, st);
             s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
