@@ -361,8 +361,19 @@ __global__ void k_label_out(const int *__restrict__ P, const int *__restrict__ R
 // keys[r] = label(own/neighbour voxel r) << 32 | label(twin), rows in the
 // reference's order: own slab then neighbour slab of the feature, each
 // flattened in C order, paired with the opposite feature's neighbour then own.
-__global__ void k_seam_pairs(const uint64_t *__restrict__ L, Vol3 V, Box a0, Box a1, Box b0, Box b1,
-                             uint64_t *__restrict__ keys, uint32_t *__restrict__ idx)
+// Labels read from a label volume ...
+struct LabImg {
+    const uint64_t *L;
+    Vol3 V;
+    __device__ __forceinline__ uint64_t at(long long i, long long j, long long k) const
+    {
+        return L[(i * V.s1 + j) * V.s2 + k];
+    }
+};
+
+template <class Src>
+__global__ void k_seam_pairs(Src src, Box a0, Box a1, Box b0, Box b1, uint64_t *__restrict__ keys,
+                             uint32_t *__restrict__ idx)
 {
     const long long n0 = a0.size(), n = n0 + a1.size();
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
@@ -374,8 +385,8 @@ __global__ void k_seam_pairs(const uint64_t *__restrict__ L, Vol3 V, Box a0, Box
         const long long wb = B.hi[2] - B.lo[2], hb = B.hi[1] - B.lo[1];
         const long long ak = q % wa, aj = (q / wa) % ha, ai = q / (wa * ha);
         const long long bk = q % wb, bj = (q / wb) % hb, bi = q / (wb * hb);
-        const uint64_t la = L[((A.lo[0] + ai) * V.s1 + A.lo[1] + aj) * V.s2 + A.lo[2] + ak];
-        const uint64_t lb = L[((B.lo[0] + bi) * V.s1 + B.lo[1] + bj) * V.s2 + B.lo[2] + bk];
+        const uint64_t la = src.at(A.lo[0] + ai, A.lo[1] + aj, A.lo[2] + ak);
+        const uint64_t lb = src.at(B.lo[0] + bi, B.lo[1] + bj, B.lo[2] + bk);
         keys[r] = (la << 32) | lb;
         idx[r] = (uint32_t)r;
     }
@@ -620,12 +631,14 @@ static std::vector<std::array<int, 3>> feature_order()
 // reference uses so its iteration order is reproduced, then the dict / stack
 // merge of merge_matched_voxels and local_to_global_labeling on the host
 // (boundary data only), and one relabel pass on the device.
-static int periodic_renumber(uint64_t *L, const int64_t *shape, const int32_t *bc,
-                             const int32_t *pad, int64_t count, int64_t *out_count,
-                             cudaStream_t st)
+// The labels come from src; with lut_out the relabelling table (indexed by
+// the local label) is handed back instead of being applied to L.
+template <class Src>
+static int periodic_renumber(const Src &src, uint64_t *L, const int64_t *shape, const int32_t *bc,
+                             const int32_t *pad, int64_t count, int64_t *out_count, cudaStream_t st,
+                             uint64_t **lut_out = nullptr)
 {
     const long long n = shape[0] * shape[1] * shape[2];
-    Vol3 V{shape[0], shape[1], shape[2]};
     auto feats = feature_order();
     // insertion-ordered map (key label -> neighbour list), as a Python dict
     std::vector<uint64_t> keys_order;
@@ -674,8 +687,7 @@ static int periodic_renumber(uint64_t *L, const int64_t *shape, const int32_t *b
         PMG_TRY(scratch_alloc((void **)&d_nsel, 2 * sizeof(int), st));
         {
             const int ps__ = prof_begin("k_seam_pairs", st);
-            k_seam_pairs<<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(L, V, own, nb, onb, oown, d_k,
-                                                                      d_i);
+            k_seam_pairs<Src><<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(src, own, nb, onb, oown, d_k, d_i);
             prof_end(ps__, (double)rows * 28, st);
         }
         PMG_CHECK_LAUNCH();
@@ -823,18 +835,21 @@ static int periodic_renumber(uint64_t *L, const int64_t *shape, const int32_t *b
         prof_end(ps__, (double)m * 13, st);
     }
     PMG_CHECK_LAUNCH();
-    {
+    if (!lut_out) {
         const int ps__ = prof_begin("k_apply_lut", st);
         k_apply_lut<<<grid_for(n, 256, 1LL << 30), 256, 0, st>>>(L, n, d_lut);
         prof_end(ps__, (double)n * 16, st);
+        PMG_CHECK_LAUNCH();
     }
-    PMG_CHECK_LAUNCH();
     const long long nloc = (long long)count - nbnd;
     int64_t max_label = (int64_t)(nloc + (long long)global_id);
     if (max_label < 1)
         max_label = (int64_t)global_id;
     PMG_TRY(scratch_free(d_t, st));
-    PMG_TRY(scratch_free(d_lut, st));
+    if (lut_out)
+        *lut_out = d_lut;
+    else
+        PMG_TRY(scratch_free(d_lut, st));
     PMG_TRY(scratch_free(d_flag, st));
     PMG_TRY(scratch_free(d_nf, st));
     PMG_TRY(scratch_free(d_rank, st));
@@ -895,7 +910,8 @@ static int cc_label_t(const T *img, uint64_t *labels, const int64_t *shape, cons
         return s;
     *count = total;
     if (any_periodic(bc))
-        return periodic_renumber(labels, shape, bc, pad, total, count, st);
+        return periodic_renumber(LabImg{labels, Vol3{shape[0], shape[1], shape[2]}}, labels, shape, bc, pad, total,
+                                 count, st);
     return PMG_OK;
 }
 
@@ -2588,7 +2604,7 @@ __global__ void k_root_label(const int *__restrict__ P, const uint8_t *__restric
 
 // labels of every voxel: a block's label on its foreground voxels, 0 elsewhere
 __global__ void k_blk_label_out(const int *__restrict__ P, const uint8_t *__restrict__ M, const int *__restrict__ F,
-                                BGrid G, uint64_t *__restrict__ labels)
+                                BGrid G, uint64_t *__restrict__ labels, const uint64_t *__restrict__ lut)
 {
     const int nb = G.b0 * G.b1 * G.b2;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
@@ -2597,7 +2613,9 @@ __global__ void k_blk_label_out(const int *__restrict__ P, const uint8_t *__rest
         const int c0 = r / G.b1;
         const int c1 = r - c0 * G.b1;
         const unsigned m = M[b];
-        const uint64_t lab = m ? (uint64_t)F[P[b]] : 0;
+        uint64_t lab = m ? (uint64_t)F[P[b]] : 0;
+        if (lut && lab)
+            lab = lut[lab];
 #pragma unroll
         for (int x = 0; x < 2; x++)
 #pragma unroll
@@ -2637,6 +2655,21 @@ static int single_value(const uint8_t *img, long long n, int *yes, cudaStream_t 
     return PMG_OK;
 }
 
+// ... or computed from the block union-find: a voxel's label is its block's
+// root's number when the voxel is foreground.
+struct LabBlk {
+    const int *P;
+    const uint8_t *M;
+    const int *F;
+    BGrid G;
+    __device__ __forceinline__ uint64_t at(long long i, long long j, long long k) const
+    {
+        const int b = (int)(((i >> 1) * G.b1 + (j >> 1)) * G.b2 + (k >> 1));
+        const int bit = (int)(((i & 1) * 2 + (j & 1)) * 2 + (k & 1));
+        return ((M[b] >> bit) & 1u) ? (uint64_t)F[P[b]] : 0;
+    }
+};
+
 int cc_label_blocks(const uint8_t *img, uint64_t *labels, const int64_t *shape, const int32_t *bc,
                     const int32_t *pad, int64_t *count, cudaStream_t st)
 {
@@ -2673,16 +2706,25 @@ int cc_label_blocks(const uint8_t *img, uint64_t *labels, const int64_t *shape, 
     PMG_TRY(scratch_alloc(&tmp, tb, st));
     PMG_CUDA(cudaMemsetAsync(cnt + ntiles, 0, 4, st));
     PMG_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, offs, (int)ntiles + 1, st));
-    {
-        const int ps__ = prof_begin("k_blk_label_out", st);
-        k_root_label<<<grid_for(nb, 256, 152LL * 32), 256, 0, st>>>(P, M, F, nb, bits, offs);
-        k_blk_label_out<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(P, M, F, G, labels);
-        prof_end(ps__, (double)n * 8 + (double)nb * 9, st);
-    }
+    k_root_label<<<grid_for(nb, 256, 152LL * 32), 256, 0, st>>>(P, M, F, nb, bits, offs);
     PMG_CHECK_LAUNCH();
     int total = 0;
     PMG_CUDA(cudaMemcpyAsync(&total, offs + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st));
     int s = read_err(err, st);
+    // periodic seams: the relabelling table is built from the blocks' labels
+    // on the seam slabs and folded into the one pass that writes the labels
+    uint64_t *lut = nullptr;
+    int64_t merged = total;
+    if (s == PMG_OK && any_periodic(bc))
+        s = periodic_renumber(LabBlk{P, M, F, G}, labels, shape, bc, pad, total, &merged, st, &lut);
+    if (s == PMG_OK) {
+        const int ps__ = prof_begin("k_blk_label_out", st);
+        k_blk_label_out<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(P, M, F, G, labels, lut);
+        prof_end(ps__, (double)n * 8 + (double)nb * 9, st);
+        s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+    }
+    if (lut)
+        PMG_TRY(scratch_free(lut, st));
     PMG_TRY(scratch_free(tmp, st));
     PMG_TRY(scratch_free(P, st));
     PMG_TRY(scratch_free(F, st));
@@ -2693,9 +2735,7 @@ int cc_label_blocks(const uint8_t *img, uint64_t *labels, const int64_t *shape, 
     PMG_TRY(scratch_free(offs, st));
     if (s != PMG_OK)
         return s;
-    *count = total;
-    if (any_periodic(bc))
-        return periodic_renumber(labels, shape, bc, pad, total, count, st);
+    *count = merged;
     return PMG_OK;
 }
 
