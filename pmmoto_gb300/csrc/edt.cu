@@ -804,9 +804,9 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     if (smem > 48 * 1024)
         PMG_CUDA(cudaFuncSetAttribute(k_envelope, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    if (cfg.periodic && form != PMG_EDT_MORPH && window_path_ok(res, n)) {
+    if (form != PMG_EDT_MORPH && window_path_ok(res, n)) {
         // windowed exact minimum everywhere, the float envelope on the end
-        // segments (or whole lines) the window kernel flags
+        // segments of periodic lines (or whole lines) the window kernel flags
         const long long nl = Ls.count();
         int *flag = nullptr;
         PMG_TRY(scratch_alloc((void **)&flag, sizeof(int) * (size_t)nl, st));
@@ -816,7 +816,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
             const int ps__ = prof_begin("k_env_window", st);
             const bool contiguous = Ls.ax == 2;
             k_env_window<<<grid_for(contiguous ? nl * 32 : nl * ((n + 63) / 64), 256, 152LL * 32), 256, 0, st>>>(
-                fin, fout, Ls, a, 1.0f / a, 1, form, flag);
+                fin, fout, Ls, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
             prof_end(ps__, (double)nl * n * 8, st);
             s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
         }
