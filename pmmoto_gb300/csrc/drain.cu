@@ -217,8 +217,8 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
     }
     if (orange) {
         // the paths below write the whole result
-        const int full[2] = {0, (int)shape[0] - 1};
-        PMG_CUDA(cudaMemcpyAsync(orange, full, sizeof(full), cudaMemcpyHostToDevice, st));
+        k_set_int2<<<1, 32, 0, st>>>(orange, 0, (int)shape[0] - 1);
+        PMG_CHECK_LAUNCH();
     }
     if (KC && inlet) {
         if (g_er)

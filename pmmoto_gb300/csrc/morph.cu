@@ -97,8 +97,8 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
 {
     // orange: on the paths below that ignore xr the whole result is written
     if (orange) {
-        const int full[2] = {0, (int)shape[0] - 1};
-        PMG_CUDA(cudaMemcpyAsync(orange, full, sizeof(full), cudaMemcpyHostToDevice, st));
+        k_set_int2<<<1, 32, 0, st>>>(orange, 0, (int)shape[0] - 1);
+        PMG_CHECK_LAUNCH();
     }
     ExtGeo G;
     int64_t X[3];

@@ -129,6 +129,10 @@ __device__ __forceinline__ float isect(float f_r, float r, float f_q, float q, f
     return __fdiv_rn(num, fmul(2.0f, factor1));
 }
 
+// Two ints set on the device in stream order (a host-to-device copy from
+// pageable memory would wait for the stream first).
+__global__ void k_set_int2(int *p, int a, int b);
+
 // x range of a set of 2x2x2 blocks kept in device memory as two ints, both
 // raised with atomicMax from zero: [0] = 1 + the largest block plane,
 // [1] = kRangeBig - the smallest (so a zeroed pair is the empty range).
