@@ -59,8 +59,8 @@ def drainage_counts(multiphase, radii, mode="distance", radii_dilate=None):
             continue
         morph.check_radii(sd, [r, rd])
         active[k] = 1
-        ratios[k] = morph.gen_struct_element(g.res, r)[0]
-        ratios_d[k] = morph.gen_struct_element(g.res, rd)[0]
+        ratios[k] = morph.element_ratio(g.res, r)
+        ratios_d[k] = morph.element_ratio(g.res, rd)
         if mode == "morph":
             be[k] = morph.ball_sq(g.res, r)
         if mode in ("morph", "hybrid"):

@@ -52,6 +52,16 @@ def gen_struct_element(resolution, radius):
     return ratio, np.array(s <= r * r, dtype=np.uint8)
 
 
+def element_ratio(resolution, radius):
+    """gen_struct_element's checks and ratio without building the element
+    (the device paths only need the ratio)."""
+    if len(resolution) not in {2, 3}:
+        raise ValueError("Resolution must be a list or tuple of length 2 or 3.")
+    if resolution[0] != resolution[1] != resolution[2]:
+        raise ValueError("Resolution must be isotropic for morphological methods.")
+    return gen_struct_ratio(resolution, radius)
+
+
 def compare_in_float64(radius) -> bool:
     """The dtype numpy uses for ``float32_array <= radius`` (NEP 50): Python
     scalars are weak (float32 compare); numpy scalars promote normally."""
@@ -103,7 +113,7 @@ def ball_sq(resolution, radius) -> float:
 
 def morph_device(g, t: torch.Tensor, radius, dilate: bool, out: torch.Tensor | None = None, fft: bool = False):
     """Addition/subtraction of a contiguous uint8 CUDA tensor of the padded shape."""
-    ratio = gen_struct_element(g.res, radius)[0]
+    ratio = element_ratio(g.res, radius)
     _check_buffer(g, ratio)
     if tuple(t.shape) != g.shape:
         raise ValueError(f"image shape {tuple(t.shape)} != subdomain voxels {g.shape}")
@@ -156,5 +166,5 @@ def check_radii(subdomain, radii):
     """morphological_operators.py:300-329."""
     g = geo_of(subdomain)
     for radius in radii:
-        ratio, _ = gen_struct_element(g.res, radius)
+        ratio = element_ratio(g.res, radius)
         _check_buffer(g, ratio)

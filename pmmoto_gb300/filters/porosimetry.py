@@ -46,8 +46,8 @@ def _balls(g, r_e, r_d, mode):
 
 
 def porosimetry_device(g, pm: torch.Tensor, r_e, r_d, inlet: bool, mp: torch.Tensor | None, mode: str):
-    ratio_e = np.ascontiguousarray(morph.gen_struct_element(g.res, r_e)[0], dtype=np.int32)
-    ratio_d = np.ascontiguousarray(morph.gen_struct_element(g.res, r_d)[0], dtype=np.int32)
+    ratio_e = np.ascontiguousarray(morph.element_ratio(g.res, r_e), dtype=np.int32)
+    ratio_d = np.ascontiguousarray(morph.element_ratio(g.res, r_d), dtype=np.int32)
     be, bd = _balls(g, r_e, r_d, mode)
     out = torch.empty_like(pm)
     from .connected_components import _box
