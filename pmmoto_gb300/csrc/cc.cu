@@ -1272,59 +1272,114 @@ __device__ __forceinline__ void border_block(int q, int &a, int &b, int &c)
     }
 }
 
-__global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int *err)
+// Touching earlier neighbours of border block (c0, c1, c2) at tile offset
+// (a, b, c): conn, those inside the tile (local), the dense flag and their
+// masks (mlo: neighbours 0-7, mhi: 8-12).
+__device__ __forceinline__ void border_conn(const uint8_t *__restrict__ M, const BGrid &G, int c0, int c1, int c2,
+                                            int a, int b, int c, unsigned m, unsigned &conn, unsigned &local,
+                                            bool &full, uint64_t &mlo, uint64_t &mhi)
+{
+    conn = 0;
+    local = 0;
+    mlo = 0;
+    mhi = 0;
+    full = m == 0xffu;
+#pragma unroll
+    for (int q = 0; q < 13; q++) {
+        const int a0 = c0 + c_nb[q][0], a1 = c1 + c_nb[q][1], a2 = c2 + c_nb[q][2];
+        if (a0 < 0 || a1 < 0 || a2 < 0 || a1 >= G.b1 || a2 >= G.b2)
+            continue;
+        if (!(m & c_bt_self[q]))
+            continue;
+        const unsigned mn = M[(a0 * G.b1 + a1) * G.b2 + a2];
+        if (!(mn & c_bt_nb[q]))
+            continue;
+        conn |= 1u << q;
+        full = full && mn == 0xffu;
+        if (q < 8)
+            mlo |= (uint64_t)mn << (8 * q);
+        else
+            mhi |= (uint64_t)mn << (8 * (q - 8));
+        const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
+        if (aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2)
+            local |= 1u << q;
+    }
+}
+
+__device__ __forceinline__ bool border_item(long long it, const BGrid &G, int nt1, int nt2, int &bi, int &c0, int &c1,
+                                            int &c2, int &a, int &b, int &c)
+{
+    const int tile = (int)(it / kBorder);
+    border_block((int)(it - (long long)tile * kBorder), a, b, c);
+    c0 = (tile / (nt1 * nt2)) * kT0 + a;
+    c1 = ((tile / nt2) % nt1) * kT1 + b;
+    c2 = (tile % nt2) * kT2 + c;
+    if (c0 >= G.b0 || c1 >= G.b1 || c2 >= G.b2)
+        return false;
+    bi = (c0 * G.b1 + c1) * G.b2 + c2;
+    return true;
+}
+
+// Phase 2a: border blocks whose cross-tile links need no union (empty, no
+// touching neighbour outside the tile, or dense with an in-tile neighbour
+// that links them all) stop here; the others are listed for phase 2b, so
+// that its warps run full.
+__global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int *err, int *hard, int *nhard)
+{
+    const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
+    const long long items = (long long)((G.b0 + kT0 - 1) / kT0) * nt1 * nt2 * kBorder;
+    const int lane = threadIdx.x & 31;
+    for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < items;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long it = base + lane;
+        bool need = false;
+        int bi, c0, c1, c2, a, b, c;
+        if (it < items && border_item(it, G, nt1, nt2, bi, c0, c1, c2, a, b, c)) {
+            const unsigned m = M[bi];
+            if (m) {
+                unsigned conn, local;
+                bool full;
+                uint64_t mlo, mhi;
+                border_conn(M, G, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+                // in-tile neighbours were united in phase 1, and so was
+                // everything touching them
+                need = (conn & ~local) != 0 && !(full && ((conn >> kCentre) & 1u) && local);
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, need);
+        if (bal) {
+            int pos = 0;
+            if (lane == 0)
+                pos = atomicAdd(nhard, __popc(bal));
+            pos = __shfl_sync(0xffffffffu, pos, 0);
+            if (need)
+                hard[pos + __popc(bal & ((1u << lane) - 1u))] = (int)it;
+        }
+    }
+}
+
+// Phase 2b: the listed border blocks unite with touching earlier neighbours in
+// other tiles; neighbours reached through an in-tile neighbour are skipped.
+__global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G, int *err, const int *hard,
+                                  const int *nhard)
 {
     __shared__ BTabs tb;
     load_btabs(tb);
     __syncthreads();
     const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
-    const long long items = (long long)((G.b0 + kT0 - 1) / kT0) * nt1 * nt2 * kBorder;
-    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items;
-         it += (long long)gridDim.x * blockDim.x) {
-        const int tile = (int)(it / kBorder);
-        int a, b, c;
-        border_block((int)(it - (long long)tile * kBorder), a, b, c);
-        const int c0 = (tile / (nt1 * nt2)) * kT0 + a, c1 = ((tile / nt2) % nt1) * kT1 + b,
-                  c2 = (tile % nt2) * kT2 + c;
-        if (c0 >= G.b0 || c1 >= G.b1 || c2 >= G.b2)
+    const int cnt = *nhard;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < cnt; h += gridDim.x * blockDim.x) {
+        int bi, c0, c1, c2, a, b, c;
+        if (!border_item(hard[h], G, nt1, nt2, bi, c0, c1, c2, a, b, c))
             continue;
-        const int bi = (c0 * G.b1 + c1) * G.b2 + c2;
         const unsigned m = M[bi];
-        if (!m)
-            continue;
-        unsigned conn = 0, local = 0;
-        uint64_t mlo = 0, mhi = 0;
-        bool full = m == 0xffu;
-#pragma unroll
-        for (int q = 0; q < 13; q++) {
-            const int a0 = c0 + c_nb[q][0], a1 = c1 + c_nb[q][1], a2 = c2 + c_nb[q][2];
-            if (a0 < 0 || a1 < 0 || a2 < 0 || a1 >= G.b1 || a2 >= G.b2)
-                continue;
-            if (!(m & c_bt_self[q]))
-                continue;
-            const unsigned mn = M[(a0 * G.b1 + a1) * G.b2 + a2];
-            if (!(mn & c_bt_nb[q]))
-                continue;
-            conn |= 1u << q;
-            full = full && mn == 0xffu;
-            if (q < 8)
-                mlo |= (uint64_t)mn << (8 * q);
-            else
-                mhi |= (uint64_t)mn << (8 * (q - 8));
-            const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
-            if (aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2)
-                local |= 1u << q;
-        }
-        // in-tile neighbours were united in phase 1, and so was everything
-        // touching them
+        unsigned conn, local;
+        bool full;
+        uint64_t mlo, mhi;
+        border_conn(M, G, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
         unsigned covered = 0;
-        if (full && ((conn >> kCentre) & 1u)) {
-            // dense fast path (see k_bcc_tile): any in-tile neighbour already
-            // links all of them; otherwise the centre does
-            if (local)
-                continue;
-            covered = conn & ~(1u << kCentre);
-        }
+        if (full && ((conn >> kCentre) & 1u))
+            covered = conn & ~(1u << kCentre); // the centre links all of them
         while (local & ~covered) {
             const int q = next_cover(local & ~covered);
             covered |= bcover(q, conn & ~covered, mlo, mhi, tb);
@@ -1556,15 +1611,29 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
     }
     PMG_CHECK_LAUNCH();
     {
-        const int ps__ = prof_begin("k_bcc_cross", st);
         const long long border = (long long)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) *
                                  ((G.b2 + kT2 - 1) / kT2) * kBorder;
-        k_bcc_cross<<<grid_for(border, 256, 152LL * 64), 256, 0, st>>>(P, M, G, err);
-        // per border block: its mask, the mask facing it across the tile
-        // border, its parent
-        prof_end(ps__, (double)border * 6, st);
+        // list of the border blocks that need unions, and its length
+        int *hard = nullptr;
+        PMG_TRY(scratch_alloc((void **)&hard, sizeof(int) * (size_t)(border + 64), st));
+        int *nhard = hard + border + 32;
+        PMG_CUDA(cudaMemsetAsync(nhard, 0, sizeof(int), st));
+        {
+            const int ps__ = prof_begin("k_bcc_cross", st);
+            k_bcc_cross<<<grid_for(border, 256, 152LL * 64), 256, 0, st>>>(P, M, G, err, hard, nhard);
+            // per border block: its mask, the mask facing it across the tile
+            // border
+            prof_end(ps__, (double)border * 2, st);
+        }
+        PMG_CHECK_LAUNCH();
+        {
+            const int ps__ = prof_begin("k_bcc_cross_unite", st);
+            k_bcc_cross_unite<<<152 * 16, 256, 0, st>>>(P, M, G, err, hard, nhard);
+            prof_end(ps__, 0.0, st);
+        }
+        PMG_CHECK_LAUNCH();
+        PMG_TRY(scratch_free(hard, st));
     }
-    PMG_CHECK_LAUNCH();
     if (twins && any_periodic(bc)) {
         const int ps__ = prof_begin("k_bcc_twins", st);
         k_bcc_twins<<<grid_for(n, 256, 152LL * 32), 256, 0, st>>>(M, P, G, make_twins(shape, bc, pad), err);
