@@ -2377,7 +2377,8 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
                                       uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
                                       Boxes B, uint8_t *Mn, int *Pn, int *list, int *count,
                                       unsigned long long *cnt2, unsigned long long *cnt1, int *err,
-                                      int *wdirty, const int *__restrict__ orange, int ranged)
+                                      int *wdirty, const int *__restrict__ orange, int ranged,
+                                      unsigned long long *units)
 {
     // orange: the x range [olo, ohi] (whole blocks) where the dilation result
     // is defined; outside it the dilation is empty.  ranged: only blocks that
@@ -2391,6 +2392,8 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
     const int bstart = ranged ? max(0, bxlo) * plane : 0;
     const int nb = G.b0 * G.b1 * G.b2;
     const int bend = ranged ? min(nb, max(0, bxhi + 1) * plane) : nb;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && bend > bstart)
+        atomicAdd(units, (unsigned long long)(bend - bstart) * 8ull);
     const int lane = threadIdx.x & 31;
     unsigned int c2 = 0, c1 = 0;
     const bool pairs = !(G.s2 & 1);
@@ -2560,8 +2563,10 @@ int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape,
     k_drain_update_blocks<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
         mp, morph, P, M, mark, G, B, g_nw ? g_nw->M : nullptr, g_nw ? g_nw->P : nullptr,
         g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err, wdirty, orange,
-        ranged ? 1 : 0);
-    prof_end(ps__, (double)n * 3 + (double)nb * 6, st);
+        ranged ? 1 : 0, prof_units(kUnitsDrainUpdate));
+    // per voxel visited: multiphase read and written, dilation read
+    prof_end_units(ps__, kUnitsDrainUpdate, 3.0, st);
+    (void)n;
     PMG_CHECK_LAUNCH();
     return PMG_OK;
 }

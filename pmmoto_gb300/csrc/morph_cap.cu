@@ -80,7 +80,7 @@ struct RowSrc {
 __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E, uint16_t *__restrict__ KA,
                                                   long long rows, int X2, int T, int W, RowSrc rs,
                                                   const unsigned long long *__restrict__ gate,
-                                                  const int *__restrict__ xr)
+                                                  const int *__restrict__ xr, unsigned long long *units)
 {
     if (gate && *gate == 0)
         return; // empty seed set: the last pass writes the result alone
@@ -102,6 +102,8 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
     // with a seed range, only the rows of its planes
     const long long r0 = xr ? (long long)max(sr.hlo, 0) * rs.X1 : 0;
     const long long r1 = xr ? min(rows, (long long)(sr.hhi + 1) * rs.X1) : rows;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && r1 > r0)
+        atomicAdd(units, (unsigned long long)((r1 - r0) * X2));
     for (long long r = r0 + warp; r < r1; r += nwarps) {
         const uint8_t *src = E + r * X2;
         bool wrow = false;
@@ -222,7 +224,7 @@ constexpr int kCapChunk = 8; // heights loaded ahead per line (memory-level para
 template <int AX, int RING>
 __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA, uint16_t *__restrict__ KB,
                                                  CapGeo G, int T, int W, const unsigned long long *__restrict__ gate,
-                                                 const int *__restrict__ xr, int nseg)
+                                                 const int *__restrict__ xr, int nseg, unsigned long long *units)
 {
     if (gate && *gate == 0)
         return;
@@ -239,6 +241,8 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
     const long long l0 = AX == 1 && xr ? (long long)max(sr.hlo, 0) * G.nk : 0;
     const long long l1 = AX == 1 && xr ? min(nlines, (long long)(sr.hhi + 1) * G.nk) : nlines;
     const long long span = l1 > l0 ? l1 - l0 : 0;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && span)
+        atomicAdd(units, (unsigned long long)(span * n));
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < span * nseg;
          g += (long long)gridDim.x * blockDim.x) {
         const int seg = (int)(g / span);
@@ -302,7 +306,8 @@ __device__ __forceinline__ int isqrt_small(int m)
 // before its first output (heights farther away cannot reach it).
 __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ KB, CapGeo G, int T, int W,
                                                   MorphEpi me, const unsigned long long *__restrict__ gate,
-                                                  const int *__restrict__ xr, int *__restrict__ orange, int nseg)
+                                                  const int *__restrict__ xr, int *__restrict__ orange, int nseg,
+                                                  unsigned long long *units)
 {
     SeedRange sr{0, G.X0 - 1, 0, G.X0 - 1};
     if (xr)
@@ -335,6 +340,8 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
     // positions x of the line that lie in the unextended volume (and in the
     // output range of the seeds)
     const int xlo = max(max(0, me.e0), sr.olo), xhi = min(min(n, me.e0 + (int)me.o0), sr.ohi + 1);
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && xhi > xlo)
+        atomicAdd(units, (unsigned long long)(nlines * (xhi - xlo)));
     const int seglen = (n + nseg - 1) / nseg;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nlines * nseg;
          g += (long long)gridDim.x * blockDim.x) {
@@ -415,12 +422,15 @@ static int launch_cap_mid(const uint16_t *in, uint16_t *out, const CapGeo &G, in
     int nseg = n / (4 * W + 32);
     nseg = nseg < 1 ? 1 : nseg > 4 ? 4 : nseg;
     const unsigned grid = grid_for(lines * nseg, 128, 1LL << 30);
+    // axis-1 passes count their voxels (k_cap_mid); the axis-0 pass of the
+    // erosion EDT (k_cap_mid0) is booked from the host
+    unsigned long long *units = AX == 1 ? prof_units(kUnitsCapMid) : nullptr;
     if (2 * W + 2 <= 16)
-        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg);
+        k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg, units);
     else if (2 * W + 2 <= 32)
-        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg);
+        k_cap_mid<AX, 32><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg, units);
     else
-        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg);
+        k_cap_mid<AX, 64><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg, units);
     return PMG_OK;
 }
 
@@ -461,15 +471,16 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
         const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
         k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W, rs,
-                                                                                gate, xr);
-        prof_end(ps__, (double)vox * 3, st);
+                                                                                gate, xr, prof_units(kUnitsCapRows));
+        prof_end_units(ps__, kUnitsCapRows, 3.0, st); // 1 B read + 2 B written per voxel
+        (void)vox;
     }
     PMG_CHECK_LAUNCH();
     {
         const long long lines = (long long)G.X0 * G.nk;
         const int ps__ = prof_begin("k_cap_mid", st);
         PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st, gate, xr));
-        prof_end(ps__, (double)lines * G.X1 * 4, st);
+        prof_end_units(ps__, kUnitsCapMid, 4.0, st); // 2 B read + 2 B written per voxel
     }
     PMG_CHECK_LAUNCH();
     {
@@ -479,8 +490,8 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
         // of a cut costs more than the threads it adds
         const int nseg = 1;
         k_cap_last<<<grid_for(lines * nseg, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate, xr, orange,
-                                                                           nseg);
-        prof_end(ps__, (double)lines * G.X0 * 2 + (double)me.o0 * me.o1 * me.o2, st);
+                                                                           nseg, prof_units(kUnitsCapLast));
+        prof_end_units(ps__, kUnitsCapLast, 3.0, st); // 2 B read + 1 B written per output
     }
     PMG_CHECK_LAUNCH();
     return PMG_OK;
@@ -509,15 +520,16 @@ int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, cons
         const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
         k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W,
-                                                                                RowSrc{}, nullptr, nullptr);
-        prof_end(ps__, (double)vox * 3, st);
+                                                                                RowSrc{}, nullptr, nullptr,
+                                                                                prof_units(kUnitsCapRows));
+        prof_end_units(ps__, kUnitsCapRows, 3.0, st);
     }
     PMG_CHECK_LAUNCH();
     {
         const long long lines = (long long)G.X0 * G.nk;
         const int ps__ = prof_begin("k_cap_mid", st);
         PMG_TRY(launch_cap_mid<1>(KA, KB, G, T, W, lines, st));
-        prof_end(ps__, (double)vox * 4, st);
+        prof_end_units(ps__, kUnitsCapMid, 4.0, st);
     }
     PMG_CHECK_LAUNCH();
     {

@@ -48,6 +48,13 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 // resolves the events into per-kernel totals.
 int prof_begin(const char *name, cudaStream_t st);
 void prof_end(int slot, double bytes, cudaStream_t st);
+// Kernels whose work is sized on the device add the units they process to
+// prof_units(id) (one counter per kind of kernel); prof_end_units records the
+// bytes per unit for the profile.
+constexpr int kUnitSlots = 8;
+constexpr int kUnitsCapRows = 0, kUnitsCapMid = 1, kUnitsCapLast = 2, kUnitsDrainUpdate = 3;
+unsigned long long *prof_units(int id);
+void prof_end_units(int slot, int id, double bytes_per_unit, cudaStream_t st);
 
 // Validate a padded single-rank geometry: positive shape, boundary codes in
 // range, non-negative pads that leave a non-empty own region on every axis.

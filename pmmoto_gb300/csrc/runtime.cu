@@ -75,6 +75,24 @@ struct ProfTot {
 };
 static std::map<std::string, ProfTot> g_prof_tot;
 
+// Units processed by kernels whose amount of work is decided on the device
+// (a range computed by an earlier kernel): each launch adds its count to a
+// device counter, and the profile converts the total to bytes.
+__device__ unsigned long long g_units[kUnitSlots];
+struct UnitInfo {
+    const char *name = nullptr;
+    double bytes_per_unit = 0.0;
+};
+static UnitInfo g_unit_info[kUnitSlots];
+
+unsigned long long *prof_units(int id)
+{
+    unsigned long long *p = nullptr;
+    if (id < 0 || id >= kUnitSlots || cudaGetSymbolAddress((void **)&p, g_units) != cudaSuccess)
+        return nullptr;
+    return p + id;
+}
+
 __global__ void k_set_int2(int *p, int a, int b)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -105,6 +123,21 @@ void prof_end(int slot, double bytes, cudaStream_t st)
     if (slot >= (int)g_prof.size())
         return;
     g_prof[(size_t)slot].bytes = bytes;
+    cudaEventRecord(g_prof[(size_t)slot].b, st);
+}
+
+void prof_end_units(int slot, int id, double bytes_per_unit, cudaStream_t st)
+{
+    if (slot < 0)
+        return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (slot >= (int)g_prof.size())
+        return;
+    if (id >= 0 && id < kUnitSlots) {
+        g_unit_info[id].name = g_prof[(size_t)slot].name;
+        g_unit_info[id].bytes_per_unit = bytes_per_unit;
+    }
+    g_prof[(size_t)slot].bytes = 0.0;
     cudaEventRecord(g_prof[(size_t)slot].b, st);
 }
 
@@ -141,6 +174,11 @@ extern "C" int pmg_prof_reset(void)
     pmg::prof_resolve();
     std::lock_guard<std::mutex> lk(pmg::g_prof_mu);
     pmg::g_prof_tot.clear();
+    unsigned long long *u = pmg::prof_units(0);
+    if (u && cudaMemset(u, 0, sizeof(unsigned long long) * pmg::kUnitSlots) != cudaSuccess) {
+        pmg::set_error("pmg_prof_reset: clearing the unit counters failed");
+        return PMG_ECUDA;
+    }
     return PMG_OK;
 }
 
@@ -153,6 +191,18 @@ extern "C" int pmg_prof_read(char *names, size_t names_len, double *ms, double *
     }
     pmg::prof_resolve();
     std::lock_guard<std::mutex> lk(pmg::g_prof_mu);
+    {
+        // bytes of the kernels that count their own units
+        unsigned long long units[pmg::kUnitSlots] = {};
+        unsigned long long *u = pmg::prof_units(0);
+        if (u && cudaMemcpy(units, u, sizeof(units), cudaMemcpyDeviceToHost) == cudaSuccess)
+            for (int i = 0; i < pmg::kUnitSlots; i++) {
+                const pmg::UnitInfo &ui = pmg::g_unit_info[i];
+                auto it = ui.name ? pmg::g_prof_tot.find(ui.name) : pmg::g_prof_tot.end();
+                if (it != pmg::g_prof_tot.end())
+                    it->second.bytes = (double)units[i] * ui.bytes_per_unit;
+            }
+    }
     std::string joined;
     int k = 0;
     for (auto &kv : pmg::g_prof_tot) {
