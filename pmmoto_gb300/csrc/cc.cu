@@ -2008,6 +2008,9 @@ __device__ __forceinline__ int root_flatten(int *P, int b, int *err)
 // (porosimetry.py:130-148: img_results kept where n_connected == 1 once the
 // phase exists); kept counts A's inlet-connected voxels before the
 // constraint.  Both parent arrays are flattened on the way.
+// BLK: out holds one mask per 2x2x2 block (bit (x * 2 + y) * 2 + z), else
+// one byte per voxel.
+template <bool BLK>
 __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, const uint8_t *__restrict__ markA,
                                    const uint8_t *__restrict__ MB, int *PB, const uint8_t *__restrict__ markB,
                                    const unsigned long long *__restrict__ b_count, BGrid G,
@@ -2041,6 +2044,10 @@ __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, cons
         if (m) {
             xmax = max(xmax, c0 + 1);
             xmin = max(xmin, kRangeBig - c0);
+        }
+        if (BLK) {
+            out[b] = (uint8_t)m;
+            continue;
         }
 #pragma unroll
         for (int x = 0; x < 2; x++)
@@ -2256,7 +2263,8 @@ int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *
 }
 
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
-                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept, int *xr)
+                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept, int *xr,
+                     bool blocks)
 {
     const BGrid G = bgrid_of(shape);
     const int nb = G.b0 * G.b1 * G.b2;
@@ -2264,9 +2272,15 @@ int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, 
     const int ps__ = prof_begin("k_grow_pair_select", st);
     if (xr)
         PMG_CUDA(cudaMemsetAsync(xr, 0, 2 * sizeof(int), st));
-    k_grow_pair_select<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(a.M, a.P, a.mark, b.M, b.P, b.mark, b_count,
-                                                                      G, out, kept, err, xr);
-    prof_end(ps__, (double)n + (double)nb * 10, st);
+    const unsigned grid = grid_for(nb, 256, 152LL * 64);
+    if (blocks)
+        k_grow_pair_select<true><<<grid, 256, 0, st>>>(a.M, a.P, a.mark, b.M, b.P, b.mark, b_count, G, out, kept,
+                                                        err, xr);
+    else
+        k_grow_pair_select<false><<<grid, 256, 0, st>>>(a.M, a.P, a.mark, b.M, b.P, b.mark, b_count, G, out, kept,
+                                                         err, xr);
+    // masks 2 B, parents and marks of the nonempty blocks about 8 B per block
+    prof_end(ps__, (blocks ? 0.0 : (double)n) + (double)nb * (blocks ? 11 : 10), st);
     PMG_CHECK_LAUNCH();
     return PMG_OK;
 }

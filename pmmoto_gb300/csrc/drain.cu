@@ -208,12 +208,14 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
         // the selection's x range (w.cnt[4]) limits the dilation to the planes
         // it can reach; the dilation's result range goes to orange
         int *xr = orange ? (int *)(w.cnt + 4) : nullptr;
-        PMG_TRY(grow_pair_select(*g_er, *g_nw, w.cnt + 1, w.t2, shape, w.err, st, w.cnt, xr));
+        // the selection is written as per-block masks (w.M): the dilation's
+        // row pass reads them directly (w.t2 receives bytes on other paths)
+        PMG_TRY(grow_pair_select(*g_er, *g_nw, w.cnt + 1, w.M, shape, w.err, st, w.cnt, xr, true));
         // the dilation reads the kept count (w.cnt[0]) on the device: no
         // dilation of an empty selection, and no host round trip per radius
         morph_split(w, shape, bc, ext_d, E, A, B);
         return morph_run(w.t2, out, shape, bc, pad, ext_d, res, r_d, cmp_d, 1, E, A, B, st, ball_d, w.cnt, xr,
-                         orange);
+                         orange, w.M);
     }
     if (orange) {
         // the paths below write the whole result

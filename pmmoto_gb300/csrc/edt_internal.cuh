@@ -146,10 +146,12 @@ bool cap_path_ok(const float *res, const int64_t *X, int T);
 // be empty), zero making the result all zeros without the envelope passes;
 // xr: a device x range of the seed blocks (kRangeBig encoding) -- the
 // result is then written only on the x range orange receives ([lo, hi] in
-// whole blocks, lo > hi for none) and is undefined elsewhere
+// whole blocks, lo > hi for none) and is undefined elsewhere; blk (with
+// raw_dilate): the seeds as one mask per 2x2x2 block (bit (x * 2 + y) * 2 +
+// z, blocks in C order over the ceil-halved shape) instead of E
 int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
                   cudaStream_t st, int raw_dilate = 0, const unsigned long long *gate = nullptr,
-                  const int *xr = nullptr, int *orange = nullptr);
+                  const int *xr = nullptr, int *orange = nullptr, const uint8_t *blk = nullptr);
 int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, const int64_t *X, int T,
                 cudaStream_t st);
 

@@ -90,10 +90,33 @@ __global__ void k_extend(const uint8_t *__restrict__ img, uint8_t *__restrict__ 
     }
 }
 
+// One byte per voxel from per-block masks (bit (x * 2 + y) * 2 + z of the
+// block over the ceil-halved shape), one thread per block.
+__global__ void k_blocks_to_bytes(const uint8_t *__restrict__ blk, uint8_t *__restrict__ out, long long s0,
+                                  long long s1, long long s2)
+{
+    const long long b1 = (s1 + 1) / 2, b2 = (s2 + 1) / 2, nb = (s0 + 1) / 2 * b1 * b2;
+    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nb;
+         b += (long long)gridDim.x * blockDim.x) {
+        const long long r = b / b2, c2 = b - r * b2, c0 = r / b1, c1 = r - c0 * b1;
+        const unsigned m = blk[b];
+        for (int x = 0; x < 2; x++)
+            for (int y = 0; y < 2; y++) {
+                const long long i = 2 * c0 + x, j = 2 * c1 + y;
+                if (i >= s0 || j >= s1)
+                    continue;
+                uint8_t *row = out + (i * s1 + j) * s2;
+                for (int z = 0; z < 2; z++)
+                    if (2 * c2 + z < s2)
+                        row[2 * c2 + z] = (uint8_t)((m >> ((x * 2 + y) * 2 + z)) & 1);
+            }
+    }
+}
+
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
               int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq,
-              const unsigned long long *gate, const int *xr, int *orange)
+              const unsigned long long *gate, const int *xr, int *orange, const uint8_t *blk)
 {
     // orange: on the paths below that ignore xr the whole result is written
     if (orange) {
@@ -160,8 +183,17 @@ int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int3
 
     const bool cap = T != INT_MIN && cap_path_ok(res, X, T);
     const bool any_per = G.ax[0].periodic || G.ax[1].periodic || G.ax[2].periodic;
-    if (cap && dilate && !any_per) // the row pass reads the image itself
-        return morph_cap_run(img, (uint16_t *)A, (uint16_t *)B, X, T, me, st, 1, gate, xr, orange);
+    if (cap && dilate && !any_per) // the row pass reads the image (or its block masks) itself
+        return morph_cap_run(img, (uint16_t *)A, (uint16_t *)B, X, T, me, st, 1, gate, xr, orange, blk);
+    if (blk) {
+        // the paths below read one byte per voxel: img is the caller's scratch
+        const long long nb = (shape[0] + 1) / 2 * ((shape[1] + 1) / 2) * ((shape[2] + 1) / 2);
+        const int ps__ = prof_begin("k_blocks_to_bytes", st);
+        k_blocks_to_bytes<<<grid_for(nb, 256, 152LL * 32), 256, 0, st>>>(blk, const_cast<uint8_t *>(img), shape[0],
+                                                                          shape[1], shape[2]);
+        prof_end(ps__, (double)nb * 9, st);
+        PMG_CHECK_LAUNCH();
+    }
     if (gate) {
         // the other paths read the seed count on the host: an empty dilation
         // source gives zeros
@@ -337,7 +369,7 @@ extern "C" int pmg_morph(const uint8_t *img, uint8_t *out, const int64_t shape[3
     float *A = (float *)((char *)buf + (((size_t)nvox + 255) & ~(size_t)255));
     float *B = A + nvox;
     int s = morph_run(img, out, shape, bc, pad, ext, res, radius, cmp64, dilate, E, A, B, st, ball_sq, nullptr,
-                      nullptr, nullptr);
+                      nullptr, nullptr, nullptr);
     int s2 = scratch_free(buf, st);
     return s != PMG_OK ? s : s2;
 }

@@ -65,10 +65,14 @@ struct SeedRange {
 // E is the unextended image of a dilation without periodic axes, read
 // directly -- the seeds are its nonzero voxels off the wall planes (the
 // logical_not of k_extend's image), so no extended copy is written.
+// With blk (raw only), the seeds come from per-block masks over the
+// ceil-halved shape (b1, b2 blocks along axes 1 and 2).
 struct RowSrc {
     int raw;
     int X1;
     int wall[6];
+    const uint8_t *blk;
+    int b1, b2;
 };
 
 // Only distances d <= W = floor(sqrt T) <= 31 give values below T + 1, so a
@@ -107,15 +111,27 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
     for (long long r = r0 + warp; r < r1; r += nwarps) {
         const uint8_t *src = E + r * X2;
         bool wrow = false;
-        if (rs.raw) {
-            const long long i = r / rs.X1, j = r - (r / rs.X1) * rs.X1;
+        const long long i = r / rs.X1, j = r - (r / rs.X1) * rs.X1;
+        if (rs.raw)
             wrow = (rs.wall[0] && i == 0) || (rs.wall[1] && i == rows / rs.X1 - 1) || (rs.wall[2] && j == 0) ||
                    (rs.wall[3] && j == rs.X1 - 1);
-        }
         if (wrow) {
             // a wall row holds no seeds
             for (int c = lane; c < nw; c += 32)
                 zw[c] = 0u;
+        } else if (rs.blk) {
+            // the row's bits of its block row: two per block, lanes 2q and
+            // 2q + 1 on block q of the chunk
+            const uint8_t *brow = rs.blk + ((i >> 1) * rs.b1 + (j >> 1)) * (long long)rs.b2;
+            const int bsh = (int)(((i & 1) * 2 + (j & 1)) * 2) + (lane & 1);
+#pragma unroll 4
+            for (int c = 0; c < nw; c++) {
+                const int x = (c << 5) + lane;
+                const bool seed = x < X2 && ((brow[x >> 1] >> bsh) & 1);
+                const unsigned zm = __ballot_sync(FULL, seed);
+                if (lane == 0)
+                    zw[c] = zm;
+            }
         } else {
             const uint8_t want = rs.raw ? 0 : 1; // a seed is a voxel != want (raw) or == 0
 #pragma unroll 4
@@ -126,13 +142,13 @@ __global__ void __launch_bounds__(256) k_cap_rows(const uint8_t *__restrict__ E,
                 if (lane == 0)
                     zw[c] = zm;
             }
-            if (rs.raw && lane == 0) {
-                // wall planes at the row ends hold no seeds
-                if (rs.wall[4])
-                    zw[0] &= ~1u;
-                if (rs.wall[5])
-                    zw[(X2 - 1) >> 5] &= ~(1u << ((X2 - 1) & 31));
-            }
+        }
+        if (!wrow && rs.raw && lane == 0) {
+            // wall planes at the row ends hold no seeds (lane 0 wrote every word)
+            if (rs.wall[4])
+                zw[0] &= ~1u;
+            if (rs.wall[5])
+                zw[(X2 - 1) >> 5] &= ~(1u << ((X2 - 1) & 31));
         }
         __syncwarp();
         uint16_t *dst = KA + r * X2;
@@ -446,11 +462,15 @@ bool cap_path_ok(const float *res, const int64_t *X, int T)
 }
 
 int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X, int T, const MorphEpi &me,
-                  cudaStream_t st, int raw_dilate, const unsigned long long *gate, const int *xr, int *orange)
+                  cudaStream_t st, int raw_dilate, const unsigned long long *gate, const int *xr, int *orange,
+                  const uint8_t *blk)
 {
     RowSrc rs{};
     rs.raw = raw_dilate;
     rs.X1 = (int)X[1];
+    rs.blk = raw_dilate ? blk : nullptr;
+    rs.b1 = (int)((X[1] + 1) / 2);
+    rs.b2 = (int)((X[2] + 1) / 2);
     for (int q = 0; q < 6; q++)
         rs.wall[q] = me.wall[q];
     int W = 0;
@@ -472,7 +492,8 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
         const int ps__ = prof_begin("k_cap_rows", st);
         k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W, rs,
                                                                                 gate, xr, prof_units(kUnitsCapRows));
-        prof_end_units(ps__, kUnitsCapRows, 3.0, st); // 1 B read + 2 B written per voxel
+        // 1 B read (1/8 B from block masks) + 2 B written per voxel
+        prof_end_units(ps__, kUnitsCapRows, rs.blk ? 2.125 : 3.0, st);
         (void)vox;
     }
     PMG_CHECK_LAUNCH();

@@ -5,10 +5,14 @@
 
 namespace pmg {
 
+// blk (dilation): the seeds as per-block masks (bit (x * 2 + y) * 2 + z over
+// the ceil-halved shape); img is then scratch of one byte per voxel, written
+// only on the paths that need the seeds as bytes.
 int morph_run(const uint8_t *img, uint8_t *out, const int64_t *shape, const int32_t *bc,
               const int32_t *pad, const int32_t *ext, const float *res, double radius, int cmp64,
               int dilate, uint8_t *E, float *A, float *B, cudaStream_t st, double thr_sq = -1.0,
-              const unsigned long long *gate = nullptr, const int *xr = nullptr, int *orange = nullptr);
+              const unsigned long long *gate = nullptr, const int *xr = nullptr, int *orange = nullptr,
+              const uint8_t *blk = nullptr);
 size_t morph_scratch_bytes(const int64_t *shape, const int32_t *bc, const int32_t *ext);
 int erosion_edt_run(const uint8_t *img, float *D, const int64_t *shape, const int32_t *bc,
                     const int32_t *pad, const float *res, int unit_res, uint8_t *E, float *A,
@@ -78,9 +82,11 @@ int grow_marks_step(GrowSel &g, const uint8_t *S, int k, const int64_t *shape, c
                     const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
 // ... and the inlet selection of a constrained by b (when *b_count > 0) in one
 // pass; kept counts a's inlet-connected voxels.
-// xr (optional): the x range of the output's set (kRangeBig encoding)
+// xr (optional): the x range of the output's set (kRangeBig encoding);
+// blocks: out holds one mask per 2x2x2 block (bit (x * 2 + y) * 2 + z)
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,
-                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept, int *xr = nullptr);
+                     const int64_t *shape, int *err, cudaStream_t st, unsigned long long *kept, int *xr = nullptr,
+                     bool blocks = false);
 // Selection of a set that only shrinks (the drainage's wetting phase): full
 // block union-find every step, but tiles the producer did not flag reuse
 // their tile-local parents Pl.  Scratch of shrink_sel_bytes(shape) bytes.
