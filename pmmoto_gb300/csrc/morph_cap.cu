@@ -305,6 +305,91 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
     }
 }
 
+// ---- pass B for small W: direct minima on line pairs ----------------------------
+// E_B(y) = min over |d| <= W of E_A(y + d) + d^2: heights above T are stored
+// as T + 1 and every term with |d| > W exceeds T, so the capped envelope is
+// this minimum over 2W + 1 terms.  Two adjacent lines (x2 and x2 + 1) share a
+// thread, packed in the halves of a 32-bit word, and each pair of terms costs
+// two packed add-min instructions (values stay below 2^11: no carries between
+// the halves).  The heights of a segment live in a register ring of
+// R = 2W + 1 + kPairAhead words whose slots are fixed at compile time: at
+// step u of a group of R outputs starting at y0, slot s holds position
+// y0 - W + s (s >= u) or y0 - W + s + R (s < u), so the term at y + d sits in
+// slot (u + W + d) mod R, and the slot of y - W, dead after output y, takes
+// position y + W + 1 + kPairAhead (loaded kPairAhead steps before its use).
+constexpr int kPairAhead = 8;
+constexpr int kPairMaxW = 8;
+
+// Lines of a pass on pairs: AX = 1, pairs over (x0 in [0, X0), x2 / 2 in
+// [k0 / 2, (k0 + nk) / 2)) along axis 1; AX = 0, pairs over (x1 in [j0, j0 +
+// nj), x2 / 2 ...) along axis 0.  Word offset of line pair li and its stride.
+template <int AX>
+__device__ __forceinline__ long long pair_base(const CapGeo &G, long long li, int np)
+{
+    const long long q = li / np;
+    const long long kp = li - q * np;
+    const long long v = AX == 1 ? q * G.X1 * G.X2 + G.k0 : (G.j0 + q) * G.X2 + G.k0;
+    return (v >> 1) + kp;
+}
+
+template <int AX, int W>
+__global__ void __launch_bounds__(256) k_cap_mid_pair(const uint16_t *__restrict__ KA, uint16_t *__restrict__ KB,
+                                                      CapGeo G, int T, const unsigned long long *__restrict__ gate,
+                                                      const int *__restrict__ xr, int seglen,
+                                                      unsigned long long *units)
+{
+    constexpr int R = 2 * W + 1 + kPairAhead;
+    if (gate && *gate == 0)
+        return;
+    SeedRange sr{0, 0x7fffffff, 0, 0};
+    if (xr)
+        sr.load(xr, G.X0, W);
+    const int np = G.nk >> 1;
+    const long long nlines = (long long)(AX == 1 ? G.X0 : G.nj) * np;
+    const long long st = AX == 1 ? (long long)(G.X2 >> 1) : (long long)G.X1 * (G.X2 >> 1);
+    const int n = AX == 1 ? G.X1 : G.X0;
+    const int nseg = (n + seglen - 1) / seglen;
+    const long long l0 = AX == 1 && xr ? (long long)max(sr.hlo, 0) * np : 0;
+    const long long l1 = AX == 1 && xr ? min(nlines, (long long)(sr.hhi + 1) * np) : nlines;
+    const long long span = l1 > l0 ? l1 - l0 : 0;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && span)
+        atomicAdd(units, (unsigned long long)(span * 2 * n));
+    const uint32_t bigp = (uint32_t)(T + 1) * 0x10001u;
+    const uint32_t *in0 = (const uint32_t *)KA;
+    uint32_t *out0 = (uint32_t *)KB;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < span * nseg;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int seg = (int)(g / span);
+        const long long base = pair_base<AX>(G, l0 + (g - (long long)seg * span), np);
+        const uint32_t *in = in0 + base;
+        uint32_t *out = out0 + base;
+        const int a = seg * seglen, b = min(n, a + seglen);
+        uint32_t win[R];
+#pragma unroll
+        for (int s = 0; s < R; s++) {
+            const int y = a - W + s;
+            win[s] = y >= 0 && y < n ? __ldg(in + y * st) : bigp;
+        }
+        for (int y0 = a; y0 < b; y0 += R) {
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int y = y0 + u;
+                uint32_t m = win[(u + W) % R];
+#pragma unroll
+                for (int d = 1; d <= W; d++) {
+                    const uint32_t dd = (uint32_t)(d * d) * 0x10001u;
+                    m = __viaddmin_u16x2(win[(u + W - d) % R], dd, m);
+                    m = __viaddmin_u16x2(win[(u + W + d) % R], dd, m);
+                }
+                if (y < b)
+                    out[y * st] = m;
+                const int yn = y + W + 1 + kPairAhead;
+                win[u] = y < b && yn < n ? __ldg(in + yn * st) : bigp;
+            }
+        }
+    }
+}
+
 // ---- pass C: intervals along axis 0, fused epilogue ----------------------------
 __device__ __forceinline__ int isqrt_small(int m)
 {
@@ -428,6 +513,164 @@ __global__ void __launch_bounds__(128) k_cap_last(const uint16_t *__restrict__ K
     }
 }
 
+// Pass C for small W on line pairs (pairs over (x1 in [j0, j0 + nj), x2 / 2)
+// along axis 0): x is within iff min over |d| <= W of E_B(x + d) + d^2 <= T,
+// the same test as the intervals of k_cap_last, then the same epilogue; the
+// two outputs of a pair are stored as one 16-bit word (o2 and x2 - e2 even).
+template <int W>
+__global__ void __launch_bounds__(256) k_cap_last_pair(const uint16_t *__restrict__ KB, CapGeo G, int T, MorphEpi me,
+                                                       const unsigned long long *__restrict__ gate,
+                                                       const int *__restrict__ xr, int *__restrict__ orange,
+                                                       int seglen, unsigned long long *units)
+{
+    constexpr int R = 2 * W + 1 + kPairAhead;
+    SeedRange sr{0, G.X0 - 1, 0, G.X0 - 1};
+    if (xr)
+        sr.load(xr, G.X0, W);
+    if (gate && *gate == 0) {
+        sr.olo = 2;
+        sr.ohi = -1;
+    }
+    if (orange && blockIdx.x == 0 && threadIdx.x == 0) {
+        orange[0] = sr.olo;
+        orange[1] = sr.ohi;
+    }
+    if (xr && sr.olo > sr.ohi)
+        return; // nothing within reach of a seed: the caller reads no output
+    if (gate && *gate == 0) {
+        const long long nl = (long long)me.o1 * me.o2, no = me.o0 * nl;
+        for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < no;
+             q += (long long)gridDim.x * blockDim.x)
+            me.out[q] = 0;
+        return;
+    }
+    const int np = G.nk >> 1;
+    const long long nlines = (long long)G.nj * np;
+    const long long st = (long long)G.X1 * (G.X2 >> 1);
+    const int n = G.X0;
+    const int xlo = max(max(0, me.e0), sr.olo), xhi = min(min(n, me.e0 + (int)me.o0), sr.ohi + 1);
+    if (xhi <= xlo)
+        return;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(units, (unsigned long long)(nlines * 2 * (xhi - xlo)));
+    const int nseg = (xhi - xlo + seglen - 1) / seglen;
+    const int hlo = sr.hlo, hend = min(n, sr.hhi + 1); // heights are read on [hlo, hend)
+    const uint32_t bigp = (uint32_t)(T + 1) * 0x10001u, tp = (uint32_t)T * 0x10001u;
+    const long long ost = me.o1 * me.o2;
+    const int xw0 = me.wall[0] ? me.e0 : -1, xw1 = me.wall[1] ? me.e0 + (int)me.o0 - 1 : -1;
+    const uint32_t *in0 = (const uint32_t *)KB;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nlines * nseg;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int seg = (int)(g / nlines);
+        const long long li = g - (long long)seg * nlines;
+        const int a = xlo + seg * seglen, b = min(xhi, a + seglen);
+        const long long q = li / np;
+        const int x1 = G.j0 + (int)q;
+        const int x2 = G.k0 + 2 * (int)(li - q * np);
+        const uint32_t *in = in0 + pair_base<0>(G, li, np);
+        const long long jo = x1 - me.e1, ko = x2 - me.e2;
+        const bool wall_j = (me.wall[2] && jo == 0) || (me.wall[3] && jo == me.o1 - 1);
+        // bytes of the pair kept off the wall lines
+        const uint32_t keep = (wall_j || (me.wall[4] && ko == 0) ? 0u : 0x00ffu) |
+                              (wall_j || (me.wall[5] && ko + 1 == me.o2 - 1) ? 0u : 0xff00u);
+        uint16_t *dst = (uint16_t *)(me.out + jo * me.o2 + ko + (long long)(a - me.e0) * ost);
+        const long long ostw = ost >> 1;
+        uint32_t win[R];
+#pragma unroll
+        for (int s = 0; s < R; s++) {
+            const int y = a - W + s;
+            win[s] = y >= hlo && y < hend ? __ldg(in + y * st) : bigp;
+        }
+        for (int y0 = a; y0 < b; y0 += R) {
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int y = y0 + u;
+                uint32_t m = win[(u + W) % R];
+#pragma unroll
+                for (int d = 1; d <= W; d++) {
+                    const uint32_t dd = (uint32_t)(d * d) * 0x10001u;
+                    m = __viaddmin_u16x2(win[(u + W - d) % R], dd, m);
+                    m = __viaddmin_u16x2(win[(u + W + d) % R], dd, m);
+                }
+                if (y < b) {
+                    uint32_t sel = __vcmpleu2(m, tp); // 0xffff in each half within reach
+                    if (!me.dilate)
+                        sel = ~sel;
+                    uint32_t v = ((sel & 1u) | ((sel >> 8) & 0x100u)) & keep;
+                    if (y == xw0 || y == xw1)
+                        v = 0u;
+                    *dst = (uint16_t)v;
+                    dst += ostw;
+                }
+                const int yn = y + W + 1 + kPairAhead;
+                win[u] = y < b && yn >= hlo && yn < hend ? __ldg(in + yn * st) : bigp;
+            }
+        }
+    }
+}
+
+// Segment length of the pair kernels: whole groups of the register ring,
+// about four per segment.
+static int pair_seglen(int W) { return 4 * (2 * W + 1 + kPairAhead); }
+
+template <int AX, int W>
+static void launch_mid_pair_w(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, cudaStream_t st,
+                              const unsigned long long *gate, const int *xr, unsigned long long *units)
+{
+    const int n = AX == 1 ? G.X1 : G.X0;
+    const int seglen = pair_seglen(W);
+    const long long lines = (long long)(AX == 1 ? G.X0 : G.nj) * (G.nk >> 1);
+    const long long work = lines * ((n + seglen - 1) / seglen);
+    k_cap_mid_pair<AX, W><<<grid_for(work, 256, 1LL << 30), 256, 0, st>>>(in, out, G, T, gate, xr, seglen, units);
+}
+
+template <int AX>
+static void launch_mid_pair(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, int W, cudaStream_t st,
+                            const unsigned long long *gate, const int *xr, unsigned long long *units)
+{
+    switch (W) {
+    case 0: launch_mid_pair_w<AX, 0>(in, out, G, T, st, gate, xr, units); break;
+    case 1: launch_mid_pair_w<AX, 1>(in, out, G, T, st, gate, xr, units); break;
+    case 2: launch_mid_pair_w<AX, 2>(in, out, G, T, st, gate, xr, units); break;
+    case 3: launch_mid_pair_w<AX, 3>(in, out, G, T, st, gate, xr, units); break;
+    case 4: launch_mid_pair_w<AX, 4>(in, out, G, T, st, gate, xr, units); break;
+    case 5: launch_mid_pair_w<AX, 5>(in, out, G, T, st, gate, xr, units); break;
+    case 6: launch_mid_pair_w<AX, 6>(in, out, G, T, st, gate, xr, units); break;
+    case 7: launch_mid_pair_w<AX, 7>(in, out, G, T, st, gate, xr, units); break;
+    default: launch_mid_pair_w<AX, kPairMaxW>(in, out, G, T, st, gate, xr, units); break;
+    }
+}
+
+template <int W>
+static void launch_last_pair_w(const uint16_t *KB, const CapGeo &G, int T, const MorphEpi &me, cudaStream_t st,
+                               const unsigned long long *gate, const int *xr, int *orange, unsigned long long *units)
+{
+    const int seglen = pair_seglen(W);
+    const long long lines = (long long)G.nj * (G.nk >> 1);
+    const long long work = lines * ((G.X0 + seglen - 1) / seglen);
+    k_cap_last_pair<W><<<grid_for(work, 256, 1LL << 30), 256, 0, st>>>(KB, G, T, me, gate, xr, orange, seglen, units);
+}
+
+static void launch_last_pair(const uint16_t *KB, const CapGeo &G, int T, int W, const MorphEpi &me, cudaStream_t st,
+                             const unsigned long long *gate, const int *xr, int *orange, unsigned long long *units)
+{
+    switch (W) {
+    case 0: launch_last_pair_w<0>(KB, G, T, me, st, gate, xr, orange, units); break;
+    case 1: launch_last_pair_w<1>(KB, G, T, me, st, gate, xr, orange, units); break;
+    case 2: launch_last_pair_w<2>(KB, G, T, me, st, gate, xr, orange, units); break;
+    case 3: launch_last_pair_w<3>(KB, G, T, me, st, gate, xr, orange, units); break;
+    case 4: launch_last_pair_w<4>(KB, G, T, me, st, gate, xr, orange, units); break;
+    case 5: launch_last_pair_w<5>(KB, G, T, me, st, gate, xr, orange, units); break;
+    case 6: launch_last_pair_w<6>(KB, G, T, me, st, gate, xr, orange, units); break;
+    case 7: launch_last_pair_w<7>(KB, G, T, me, st, gate, xr, orange, units); break;
+    default: launch_last_pair_w<kPairMaxW>(KB, G, T, me, st, gate, xr, orange, units); break;
+    }
+}
+
+// Line pairs need even x2 extents and starts (32-bit words of two heights,
+// 16-bit output words).
+static bool pair_ok(const CapGeo &G, int W) { return W <= kPairMaxW && !((G.X2 | G.k0 | G.nk) & 1); }
+
 // the ring holds the live parabolas, at most 2W + 2
 template <int AX>
 static int launch_cap_mid(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, int W, long long lines,
@@ -441,6 +684,10 @@ static int launch_cap_mid(const uint16_t *in, uint16_t *out, const CapGeo &G, in
     // axis-1 passes count their voxels (k_cap_mid); the axis-0 pass of the
     // erosion EDT (k_cap_mid0) is booked from the host
     unsigned long long *units = AX == 1 ? prof_units(kUnitsCapMid) : nullptr;
+    if (pair_ok(G, W)) {
+        launch_mid_pair<AX>(in, out, G, T, W, st, gate, xr, units);
+        return PMG_OK;
+    }
     if (2 * W + 2 <= 16)
         k_cap_mid<AX, 16><<<grid, 128, 0, st>>>(in, out, G, T, W, gate, xr, nseg, units);
     else if (2 * W + 2 <= 32)
@@ -510,8 +757,11 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
         // one segment per line: this pass is short per voxel, the extra sweep
         // of a cut costs more than the threads it adds
         const int nseg = 1;
-        k_cap_last<<<grid_for(lines * nseg, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate, xr, orange,
-                                                                           nseg, prof_units(kUnitsCapLast));
+        if (pair_ok(G, W))
+            launch_last_pair(KB, G, T, W, me, st, gate, xr, orange, prof_units(kUnitsCapLast));
+        else
+            k_cap_last<<<grid_for(lines * nseg, 128, 1LL << 30), 128, 0, st>>>(KB, G, T, W, me, gate, xr, orange,
+                                                                               nseg, prof_units(kUnitsCapLast));
         prof_end_units(ps__, kUnitsCapLast, 3.0, st); // 2 B read + 1 B written per output
     }
     PMG_CHECK_LAUNCH();

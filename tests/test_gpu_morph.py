@@ -61,3 +61,28 @@ def test_morph_errors(M):
         M.erode(sd, img, 0.01)  # radius below the resolution
     with pytest.raises(SystemExit):
         M.erode(sd, img, 1.5)  # extension beyond the subdomain
+
+
+@pytest.mark.parametrize("kinds", [("wall", "wall", "wall"), ("end", "periodic", "wall"), ("periodic", "end", "end"),
+                                   ("wall", "end", "periodic")])
+@pytest.mark.parametrize("vox", [(22, 19, 24), (21, 24, 26), (23, 20, 25)])
+def test_morph_window_widths_vs_oracle(M, kinds, vox):
+    """Power-of-two voxels (1/32) with radii of W + 1/2 voxels, W = 0 .. 9:
+    the integer passes take direct minima on line pairs for W <= 8 when the
+    contiguous extent is even, the parabola envelope otherwise."""
+    rng = np.random.default_rng(7 + sum(vox) + sum(map(ord, "".join(kinds))))
+    scale = 32
+    box = tuple((0.0, v / scale) for v in vox)
+    bts = tuple((k, k) for k in kinds)
+    from pmmoto_gb300.core import initialize
+    sd = initialize(vox, box=box, boundary_types=bts)
+    g = O.Geom(vox, boundary_types=bts, box=box)
+    # sparse seeds for the dilation, sparse holes for the erosion
+    sparse = O.update_buffer(g, (rng.random(sd.voxels) > 0.995).astype(np.uint8))
+    dense = O.update_buffer(g, (rng.random(sd.voxels) > 0.005).astype(np.uint8))
+    for w in range(0, 10):
+        r = (w + 0.5) / scale
+        if r < 1.0 / scale:
+            continue  # the reference rejects radii below the voxel size
+        np.testing.assert_array_equal(M.dilate(sd, sparse, r), O.dilate(g, sparse, r), err_msg=f"dilate W={w}")
+        np.testing.assert_array_equal(M.erode(sd, dense, r), O.erode(g, dense, r), err_msg=f"erode W={w}")
