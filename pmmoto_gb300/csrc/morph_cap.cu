@@ -27,6 +27,8 @@
 // where a warp reads and writes 32 adjacent voxels at a time.  The reference's
 // linear pass restarts at changes between nonzero values (multi-label
 // images), which depends on the axis: this pipeline serves binary images only.
+#include <type_traits>
+
 #include "edt_internal.cuh"
 
 namespace pmg {
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
 // slot (u + W + d) mod R, and the slot of y - W, dead after output y, takes
 // position y + W + 1 + kPairAhead (loaded kPairAhead steps before its use).
 constexpr int kPairAhead = 8;
-constexpr int kPairMaxW = 8;
+constexpr int kPairMaxW = 15;
 
 // Lines of a pass on pairs: AX = 1, pairs over (x0 in [0, X0), x2 / 2 in
 // [k0 / 2, (k0 + nk) / 2)) along axis 1; AX = 0, pairs over (x1 in [j0, j0 +
@@ -613,6 +615,19 @@ __global__ void __launch_bounds__(256) k_cap_last_pair(const uint16_t *__restric
 // about four per segment.
 static int pair_seglen(int W) { return 4 * (2 * W + 1 + kPairAhead); }
 
+// Calls f with std::integral_constant<int, w> for 0 <= w <= kPairMaxW.
+template <int W, class F>
+static void with_w(int w, F &&f)
+{
+    if constexpr (W < kPairMaxW) {
+        if (w > W) {
+            with_w<W + 1>(w, f);
+            return;
+        }
+    }
+    f(std::integral_constant<int, W>{});
+}
+
 template <int AX, int W>
 static void launch_mid_pair_w(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, cudaStream_t st,
                               const unsigned long long *gate, const int *xr, unsigned long long *units)
@@ -628,17 +643,7 @@ template <int AX>
 static void launch_mid_pair(const uint16_t *in, uint16_t *out, const CapGeo &G, int T, int W, cudaStream_t st,
                             const unsigned long long *gate, const int *xr, unsigned long long *units)
 {
-    switch (W) {
-    case 0: launch_mid_pair_w<AX, 0>(in, out, G, T, st, gate, xr, units); break;
-    case 1: launch_mid_pair_w<AX, 1>(in, out, G, T, st, gate, xr, units); break;
-    case 2: launch_mid_pair_w<AX, 2>(in, out, G, T, st, gate, xr, units); break;
-    case 3: launch_mid_pair_w<AX, 3>(in, out, G, T, st, gate, xr, units); break;
-    case 4: launch_mid_pair_w<AX, 4>(in, out, G, T, st, gate, xr, units); break;
-    case 5: launch_mid_pair_w<AX, 5>(in, out, G, T, st, gate, xr, units); break;
-    case 6: launch_mid_pair_w<AX, 6>(in, out, G, T, st, gate, xr, units); break;
-    case 7: launch_mid_pair_w<AX, 7>(in, out, G, T, st, gate, xr, units); break;
-    default: launch_mid_pair_w<AX, kPairMaxW>(in, out, G, T, st, gate, xr, units); break;
-    }
+    with_w<0>(W, [&](auto c) { launch_mid_pair_w<AX, decltype(c)::value>(in, out, G, T, st, gate, xr, units); });
 }
 
 template <int W>
@@ -654,17 +659,7 @@ static void launch_last_pair_w(const uint16_t *KB, const CapGeo &G, int T, const
 static void launch_last_pair(const uint16_t *KB, const CapGeo &G, int T, int W, const MorphEpi &me, cudaStream_t st,
                              const unsigned long long *gate, const int *xr, int *orange, unsigned long long *units)
 {
-    switch (W) {
-    case 0: launch_last_pair_w<0>(KB, G, T, me, st, gate, xr, orange, units); break;
-    case 1: launch_last_pair_w<1>(KB, G, T, me, st, gate, xr, orange, units); break;
-    case 2: launch_last_pair_w<2>(KB, G, T, me, st, gate, xr, orange, units); break;
-    case 3: launch_last_pair_w<3>(KB, G, T, me, st, gate, xr, orange, units); break;
-    case 4: launch_last_pair_w<4>(KB, G, T, me, st, gate, xr, orange, units); break;
-    case 5: launch_last_pair_w<5>(KB, G, T, me, st, gate, xr, orange, units); break;
-    case 6: launch_last_pair_w<6>(KB, G, T, me, st, gate, xr, orange, units); break;
-    case 7: launch_last_pair_w<7>(KB, G, T, me, st, gate, xr, orange, units); break;
-    default: launch_last_pair_w<kPairMaxW>(KB, G, T, me, st, gate, xr, orange, units); break;
-    }
+    with_w<0>(W, [&](auto c) { launch_last_pair_w<decltype(c)::value>(KB, G, T, me, st, gate, xr, orange, units); });
 }
 
 // Line pairs need even x2 extents and starts (32-bit words of two heights,
@@ -732,16 +727,14 @@ int morph_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, const int64_t *X
     G.k0 = me.e2;
     G.nk = (int)me.o2;
     const long long rows = (long long)G.X0 * G.X1;
-    const long long vox = rows * G.X2;
     {
         const int block = 256;
         const size_t smem = (size_t)(block / 32) * ((G.X2 + 31) / 32 + 2) * sizeof(uint32_t);
         const int ps__ = prof_begin("k_cap_rows", st);
-        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(E, KA, rows, G.X2, T, W, rs,
-                                                                                gate, xr, prof_units(kUnitsCapRows));
+        k_cap_rows<<<grid_for(rows * 32, block, 152LL * 16), block, smem, st>>>(
+            E, KA, rows, G.X2, T, W, rs, gate, xr, prof_units(kUnitsCapRows));
         // 1 B read (1/8 B from block masks) + 2 B written per voxel
         prof_end_units(ps__, kUnitsCapRows, rs.blk ? 2.125 : 3.0, st);
-        (void)vox;
     }
     PMG_CHECK_LAUNCH();
     {

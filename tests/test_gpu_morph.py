@@ -65,10 +65,10 @@ def test_morph_errors(M):
 
 @pytest.mark.parametrize("kinds", [("wall", "wall", "wall"), ("end", "periodic", "wall"), ("periodic", "end", "end"),
                                    ("wall", "end", "periodic")])
-@pytest.mark.parametrize("vox", [(22, 19, 24), (21, 24, 26), (23, 20, 25)])
+@pytest.mark.parametrize("vox", [(36, 35, 38), (37, 40, 36), (39, 36, 37)])
 def test_morph_window_widths_vs_oracle(M, kinds, vox):
-    """Power-of-two voxels (1/32) with radii of W + 1/2 voxels, W = 0 .. 9:
-    the integer passes take direct minima on line pairs for W <= 8 when the
+    """Power-of-two voxels (1/32) with radii of W + 1/2 voxels, W = 0 .. 16:
+    the integer passes take direct minima on line pairs for W <= 15 when the
     contiguous extent is even, the parabola envelope otherwise."""
     rng = np.random.default_rng(7 + sum(vox) + sum(map(ord, "".join(kinds))))
     scale = 32
@@ -77,10 +77,12 @@ def test_morph_window_widths_vs_oracle(M, kinds, vox):
     from pmmoto_gb300.core import initialize
     sd = initialize(vox, box=box, boundary_types=bts)
     g = O.Geom(vox, boundary_types=bts, box=box)
-    # sparse seeds for the dilation, sparse holes for the erosion
-    sparse = O.update_buffer(g, (rng.random(sd.voxels) > 0.995).astype(np.uint8))
-    dense = O.update_buffer(g, (rng.random(sd.voxels) > 0.005).astype(np.uint8))
-    for w in range(0, 10):
+    # a few seeds for the dilation, a few holes for the erosion
+    few = np.zeros(sd.voxels, np.uint8)
+    few[tuple(rng.integers(0, v, 6) for v in sd.voxels)] = 1
+    sparse = O.update_buffer(g, few)
+    dense = O.update_buffer(g, 1 - few)
+    for w in range(0, 17):
         r = (w + 0.5) / scale
         if r < 1.0 / scale:
             continue  # the reference rejects radii below the voxel size
