@@ -1990,18 +1990,7 @@ static SrcErode erode_src(const uint16_t *E, int T, const int64_t *shape, const 
     return src;
 }
 
-// Root of block b with its parent flattened to it (-1 for an empty block).
-__device__ __forceinline__ int root_flatten(int *P, int b, int *err)
-{
-    int p = ld(P + b);
-    if (p >= 0 && p != b) {
-        const int q = find_root(P, p, err);
-        if (q != p)
-            P[b] = q;
-        p = q;
-    }
-    return p;
-}
+constexpr int kPairBatch = 4;
 
 // Inlet selections of two growing sets A and B in one pass: out = 1 where A
 // is inlet-connected and, when *b_count > 0, B is inlet-connected too
@@ -2020,50 +2009,89 @@ __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, cons
     const bool constrain = *b_count > 0;
     unsigned int cnt = 0;
     int xmax = 0, xmin = 0; // block-plane range of the output's voxels, encoded as in XRange
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
-        const int r = b / G.b2;
-        const int c2 = b - r * G.b2;
-        const int c0 = r / G.b1;
-        const int c1 = r - c0 * G.b1;
-        unsigned m = MA[b];
-        const unsigned mb = MB[b];
-        if (m) {
-            const int ra = root_flatten(PA, b, err);
-            if (ra < 0 || !(markA[ra] & 1))
-                m = 0;
-        }
-        unsigned keepB = 0;
-        if (mb) {
-            const int rb = root_flatten(PB, b, err);
-            if (rb >= 0 && (markB[rb] & 1))
-                keepB = mb;
-        }
-        cnt += __popc(m);
-        if (constrain)
-            m &= keepB;
-        if (m) {
-            xmax = max(xmax, c0 + 1);
-            xmin = max(xmin, kRangeBig - c0);
-        }
-        if (BLK) {
-            out[b] = (uint8_t)m;
-            continue;
+    // kPairBatch blocks per thread, each level of the root lookups (masks,
+    // parents, their parents, marks) loaded for all of them before any is
+    // used: the lookups are chains of dependent loads
+    constexpr int NB = kPairBatch;
+    for (int base = blockIdx.x * blockDim.x * NB + threadIdx.x; base < nb; base += gridDim.x * blockDim.x * NB) {
+        int bb[NB], pa[NB], pb[NB], ga[NB], gb[NB];
+        unsigned m[NB], mb[NB], ka[NB], kb[NB];
+#pragma unroll
+        for (int q = 0; q < NB; q++) {
+            bb[q] = base + q * blockDim.x;
+            const bool in = bb[q] < nb;
+            m[q] = in ? MA[bb[q]] : 0u;
+            mb[q] = in ? MB[bb[q]] : 0u;
         }
 #pragma unroll
-        for (int x = 0; x < 2; x++)
+        for (int q = 0; q < NB; q++) {
+            pa[q] = m[q] ? ld(PA + bb[q]) : -1;
+            pb[q] = mb[q] ? ld(PB + bb[q]) : -1;
+        }
 #pragma unroll
-            for (int y = 0; y < 2; y++) {
-                const int i = 2 * c0 + x, j = 2 * c1 + y;
-                if (i >= G.s0 || j >= G.s1)
-                    continue;
-                uint8_t *row = out + ((long long)i * G.s1 + j) * G.s2;
+        for (int q = 0; q < NB; q++) {
+            ga[q] = pa[q] >= 0 && pa[q] != bb[q] ? ld(PA + pa[q]) : pa[q];
+            gb[q] = pb[q] >= 0 && pb[q] != bb[q] ? ld(PB + pb[q]) : pb[q];
+        }
 #pragma unroll
-                for (int z = 0; z < 2; z++) {
-                    const int k = 2 * c2 + z;
-                    if (k < G.s2)
-                        row[k] = (uint8_t)((m >> ((x * 2 + y) * 2 + z)) & 1);
-                }
+        for (int q = 0; q < NB; q++) {
+            // the root: the parent when it is its own parent, else further up
+            // (rare once the parents were flattened); parents flattened to it
+            int ra = pa[q], rb = pb[q];
+            if (ra >= 0 && ra != bb[q] && ga[q] != ra)
+                ra = find_root(PA, ga[q], err);
+            if (rb >= 0 && rb != bb[q] && gb[q] != rb)
+                rb = find_root(PB, gb[q], err);
+            if (ra != pa[q])
+                PA[bb[q]] = ra;
+            if (rb != pb[q])
+                PB[bb[q]] = rb;
+            pa[q] = ra;
+            pb[q] = rb;
+        }
+#pragma unroll
+        for (int q = 0; q < NB; q++) {
+            ka[q] = pa[q] >= 0 ? markA[pa[q]] : 0u;
+            kb[q] = pb[q] >= 0 ? markB[pb[q]] : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < NB; q++) {
+            const int b = bb[q];
+            if (b >= nb)
+                continue;
+            const int r = b / G.b2;
+            const int c2 = b - r * G.b2;
+            const int c0 = r / G.b1;
+            const int c1 = r - c0 * G.b1;
+            unsigned mm = ka[q] & 1u ? m[q] : 0u;
+            const unsigned keepB = kb[q] & 1u ? mb[q] : 0u;
+            cnt += __popc(mm);
+            if (constrain)
+                mm &= keepB;
+            if (mm) {
+                xmax = max(xmax, c0 + 1);
+                xmin = max(xmin, kRangeBig - c0);
             }
+            if (BLK) {
+                out[b] = (uint8_t)mm;
+                continue;
+            }
+#pragma unroll
+            for (int x = 0; x < 2; x++)
+#pragma unroll
+                for (int y = 0; y < 2; y++) {
+                    const int i = 2 * c0 + x, j = 2 * c1 + y;
+                    if (i >= G.s0 || j >= G.s1)
+                        continue;
+                    uint8_t *row = out + ((long long)i * G.s1 + j) * G.s2;
+#pragma unroll
+                    for (int z = 0; z < 2; z++) {
+                        const int k = 2 * c2 + z;
+                        if (k < G.s2)
+                            row[k] = (uint8_t)((mm >> ((x * 2 + y) * 2 + z)) & 1);
+                    }
+                }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         cnt += __shfl_down_sync(0xffffffffu, cnt, o);
@@ -2272,7 +2300,7 @@ int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, 
     const int ps__ = prof_begin("k_grow_pair_select", st);
     if (xr)
         PMG_CUDA(cudaMemsetAsync(xr, 0, 2 * sizeof(int), st));
-    const unsigned grid = grid_for(nb, 256, 152LL * 64);
+    const unsigned grid = grid_for((nb + kPairBatch - 1) / kPairBatch, 256, 152LL * 64);
     if (blocks)
         k_grow_pair_select<true><<<grid, 256, 0, st>>>(a.M, a.P, a.mark, b.M, b.P, b.mark, b_count, G, out, kept,
                                                         err, xr);
