@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <type_traits>
 #include <array>
 #include <unordered_map>
 #include <unordered_set>
@@ -1124,6 +1125,12 @@ struct SrcStep {
     }
 };
 
+// ... or the block masks themselves, kept current by the producer of the set
+// (the drainage update keeps the wetting phase's).
+struct SrcMask {
+    const uint8_t *M;
+};
+
 // Mask of block (c0, c1, c2): bit (x * 2 + y) * 2 + z for a foreground voxel
 // (2 c0 + x, 2 c1 + y, 2 c2 + z) inside the volume.
 template <class Src>
@@ -1154,6 +1161,11 @@ __device__ __forceinline__ unsigned block_mask(const Src &src, const BGrid &G, i
                 }
     }
     return m;
+}
+
+__device__ __forceinline__ unsigned block_mask(const SrcMask &src, const BGrid &G, int c0, int c1, int c2)
+{
+    return src.M[((long long)c0 * G.b1 + c1) * G.b2 + c2];
 }
 
 // Phase 1 on tiles of 4 x 8 x 32 blocks (8 x 16 x 64 voxels), one thread per
@@ -1227,7 +1239,8 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
     __syncthreads();
     if (inside) {
         const int bidx = (c0 * G.b1 + c1) * G.b2 + c2;
-        M[bidx] = (uint8_t)m;
+        if constexpr (!std::is_same<Src, SrcMask>::value)
+            M[bidx] = (uint8_t)m;
         int out = -1;
         if (m) {
             const int r = L[t];
@@ -1361,13 +1374,15 @@ __global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int 
 // Phase 2b: the listed border blocks unite with touching earlier neighbours in
 // other tiles; neighbours reached through an in-tile neighbour are skipped.
 __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G, int *err, const int *hard,
-                                  const int *nhard)
+                                  const int *nhard, unsigned long long *units)
 {
     __shared__ BTabs tb;
     load_btabs(tb);
     __syncthreads();
     const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
     const int cnt = *nhard;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0)
+        atomicAdd(units, (unsigned long long)cnt);
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < cnt; h += gridDim.x * blockDim.x) {
         int bi, c0, c1, c2, a, b, c;
         if (!border_item(hard[h], G, nt1, nt2, bi, c0, c1, c2, a, b, c))
@@ -1577,6 +1592,13 @@ __global__ void k_bcc_select(const uint8_t *__restrict__ M, int *P, const uint8_
 __host__ __device__ inline const uint8_t *src_elem(const SrcImg &s) { return s.img; }
 __host__ __device__ inline const uint16_t *src_elem(const SrcErode &s) { return s.E; }
 __host__ __device__ inline const uint8_t *src_elem(const SrcStep &s) { return s.S; }
+// bytes a tile pass reads from its source: one element per voxel, or one mask per block
+template <class Src>
+static double src_bytes(const Src &src, long long n, long long nb)
+{
+    return std::is_same<Src, SrcMask>::value ? (double)nb : (double)n * sizeof(*src_elem(src));
+}
+__host__ __device__ inline const uint8_t *src_elem(const SrcMask &s) { return s.M; }
 
 static BGrid bgrid_of(const int64_t *shape)
 {
@@ -1607,7 +1629,7 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
         const int nt = ((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
         const int ps__ = prof_begin("k_bcc_tile", st);
         k_bcc_tile<Src><<<nt, kTile, 0, st>>>(src, P, M, G, Pl, dirty);
-        prof_end(ps__, (double)n * sizeof(*src_elem(src)) + (double)nb * 5, st);
+        prof_end(ps__, src_bytes(src, n, nb) + (double)nb * 5, st);
     }
     PMG_CHECK_LAUNCH();
     {
@@ -1628,8 +1650,10 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
         PMG_CHECK_LAUNCH();
         {
             const int ps__ = prof_begin("k_bcc_cross_unite", st);
-            k_bcc_cross_unite<<<152 * 16, 256, 0, st>>>(P, M, G, err, hard, nhard);
-            prof_end(ps__, 0.0, st);
+            k_bcc_cross_unite<<<152 * 16, 256, 0, st>>>(P, M, G, err, hard, nhard, prof_units(kUnitsCrossUnite));
+            // per listed border block: its entry and mask, the masks of its 13
+            // earlier neighbours, two parents per union
+            prof_end_units(ps__, kUnitsCrossUnite, 4 + 1 + 13 + 8, st);
         }
         PMG_CHECK_LAUNCH();
         PMG_TRY(scratch_free(hard, st));
@@ -1834,7 +1858,8 @@ __device__ __forceinline__ unsigned touch_bits(int d0, int d1, int d2)
 // lane per distinct parent unites (neighbours with one parent are in one
 // component already).
 __global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, const int *__restrict__ list,
-                             const int *__restrict__ count, const int *__restrict__ off, int *err)
+                             const int *__restrict__ count, const int *__restrict__ off, int *err,
+                             unsigned long long *units)
 {
     int cnt;
     if (off) {
@@ -1843,6 +1868,8 @@ __global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, con
     } else {
         cnt = *count;
     }
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0)
+        atomicAdd(units, (unsigned long long)cnt);
     const int lane = threadIdx.x & 31;
     const int q = lane < 13 ? lane : lane + 1; // offset code (d0 + 1) * 9 + (d1 + 1) * 3 + d2 + 1, 13 skipped
     const int d0 = q / 9 - 1, d1 = (q / 3) % 3 - 1, d2 = q % 3 - 1;
@@ -1905,9 +1932,12 @@ void grow_sel_init(GrowSel &g, void *mem, const int64_t *shape)
 // Listed blocks take their masks from the source (steps known in advance).
 template <class Src>
 __global__ void k_grow_apply(Src src, uint8_t *__restrict__ M, int *__restrict__ P, BGrid G,
-                             const int *__restrict__ list, const int *__restrict__ off, int *err)
+                             const int *__restrict__ list, const int *__restrict__ off, int *err,
+                             unsigned long long *units)
 {
     const int a = off[0], cnt = off[1] - a;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0)
+        atomicAdd(units, (unsigned long long)cnt);
     for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
         const int b = list[a + it];
         const int r = b / G.b2;
@@ -1940,8 +1970,10 @@ static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int
     const long long n = shape[0] * shape[1] * shape[2];
     if (off) {
         const int ps__ = prof_begin("k_grow_apply", st);
-        k_grow_apply<Src><<<152 * 8, 256, 0, st>>>(src, g.M, g.P, G, g.ev, off, err);
-        prof_end(ps__, 0.0, st);
+        k_grow_apply<Src><<<152 * 8, 256, 0, st>>>(src, g.M, g.P, G, g.ev, off, err, prof_units(kUnitsGrowApply));
+        // per listed block: its list entry, eight source elements, mask read
+        // and written, parent written
+        prof_end_units(ps__, kUnitsGrowApply, 4 + 8 * sizeof(*src_elem(src)) + 2 + 4, st);
         PMG_CHECK_LAUNCH();
     } else if (g.pending) {
         g.pending = false;
@@ -1954,8 +1986,14 @@ static int grow_step(GrowSel &g, const Src &src, const int64_t *shape, const int
     }
     {
         const int ps__ = prof_begin(g.unite_label, st);
-        k_grow_unite<<<152 * 32, 256, 0, st>>>(g.P, g.M, G, off ? g.ev : g.list, g.count, off, err);
-        prof_end(ps__, 0.0, st);
+        k_grow_unite<<<152 * 32, 256, 0, st>>>(g.P, g.M, G, off ? g.ev : g.list, g.count, off, err,
+                                               prof_units(g.unite_units));
+        // per listed block: its list entry, mask and parent, and the masks and
+        // parents of its 26 neighbours
+        if (g.unite_units >= 0)
+            prof_end_units(ps__, g.unite_units, 4 + 5 + 26 * 5, st);
+        else
+            prof_end(ps__, 0.0, st);
     }
     PMG_CHECK_LAUNCH();
     if (any_periodic(bc)) {
@@ -2383,8 +2421,13 @@ int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64
     PMG_TRY(check_boxes(shape, inlet_box, outlet_box));
     if (!g.built)
         PMG_CUDA(cudaMemsetAsync(g.dirty, 0, sizeof(int) * (size_t)g.ntiles, st));
-    SrcImg src{img, fgval};
-    PMG_TRY(bcc_build(src, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, g.built ? g.dirty : nullptr));
+    if (g.built) {
+        // the producer of the changes kept the block masks current
+        PMG_TRY(bcc_build(SrcMask{g.M}, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, g.dirty));
+    } else {
+        SrcImg src{img, fgval};
+        PMG_TRY(bcc_build(src, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, nullptr));
+    }
     g.built = true;
     return bcc_marks(shape, inlet_box, outlet_box, g.P, g.M, g.mark, err, st);
 }
@@ -2415,12 +2458,14 @@ __device__ __forceinline__ unsigned eq2(unsigned pair, unsigned v)
     return (unsigned)((pair & 0xffu) == v) | ((unsigned)((pair >> 8) == v) << 1);
 }
 
-__global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ morph, int *Pw,
+constexpr int kUpdateBatch = 2;
+
+__global__ void k_drain_update_blocks(uint8_t *__restrict__ mp, const uint8_t *__restrict__ morph, int *Pw,
                                       uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
-                                      Boxes B, uint8_t *Mn, int *Pn, int *list, int *count,
-                                      unsigned long long *cnt2, unsigned long long *cnt1, int *err,
-                                      int *wdirty, const int *__restrict__ orange, int ranged,
-                                      unsigned long long *units)
+                                      Boxes B, uint8_t *__restrict__ Mn, int *__restrict__ Pn,
+                                      int *__restrict__ list, int *count, unsigned long long *cnt2,
+                                      unsigned long long *cnt1, int *err, int *__restrict__ wdirty,
+                                      const int *__restrict__ orange, int ranged, unsigned long long *units)
 {
     // orange: the x range [olo, ohi] (whole blocks) where the dilation result
     // is defined; outside it the dilation is empty.  ranged: only blocks that
@@ -2440,120 +2485,138 @@ __global__ void k_drain_update_blocks(uint8_t *mp, const uint8_t *__restrict__ m
     unsigned int c2 = 0, c1 = 0;
     const bool pairs = !(G.s2 & 1);
     const long long sx = (long long)G.s1 * G.s2, sy = G.s2;
-    for (int base = bstart + blockIdx.x * blockDim.x; base < bend; base += gridDim.x * blockDim.x) {
-        const int b = base + threadIdx.x;
-        bool changed = false;
-        const int rr = b / G.b2, cc0 = rr / G.b1;
-        const bool in_dil = cc0 >= bxlo && cc0 <= bxhi;
-        if (b < bend && (in_dil || !ranged)) {
-            const int r = b / G.b2;
-            const int c2b = b - r * G.b2, c0 = r / G.b1, c1b = r - (r / G.b1) * G.b1;
+    // kUpdateBatch blocks per thread: every load of all of them is issued
+    // before any of them is updated
+    constexpr int NB = kUpdateBatch;
+    for (int base = bstart + blockIdx.x * blockDim.x * NB; base < bend; base += gridDim.x * blockDim.x * NB) {
+        int bq[NB];
+        bool act[NB], ind[NB];
+        unsigned vol[NB], wold[NB], oldn[NB], pv[NB][4], mv[NB][4];
+        long long base0[NB];
+#pragma unroll
+        for (int q = 0; q < NB; q++) {
+            const int b = base + q * blockDim.x + threadIdx.x;
+            bq[q] = b;
+            const int r = b / G.b2, c0 = r / G.b1;
+            ind[q] = c0 >= bxlo && c0 <= bxhi;
+            act[q] = b < bend && (ind[q] || !ranged);
+            const int c2b = b - r * G.b2, c1b = r - c0 * G.b1;
             const int i0 = 2 * c0, j0 = 2 * c1b, k0 = 2 * c2b;
-            // voxels inside the volume, the own box and the reservoir slabs
-            const unsigned vK = in2(k0, 0, G.s2);
-            const unsigned vol = spread_x(in2(i0, 0, G.s0)) & spread_y(in2(j0, 0, G.s1)) & spread_z(vK);
-            const unsigned own = spread_x(in2(i0, B.own[0], B.own[1])) & spread_y(in2(j0, B.own[2], B.own[3])) &
-                                 spread_z(in2(k0, B.own[4], B.own[5]));
-            const unsigned res = (spread_x(~in2(i0, B.rpad[0], (long long)G.s0 - B.rpad[1]) & 3u) |
-                                  spread_y(~in2(j0, B.rpad[2], (long long)G.s1 - B.rpad[3]) & 3u) |
-                                  spread_z(~in2(k0, B.rpad[4], (long long)G.s2 - B.rpad[5]) & 3u)) &
-                                 vol;
-            const unsigned wold = Mw[b];
-            unsigned wet = wold;
-            // the four rows of the block: old values and the morph == 1 bits
-            const long long base0 = (long long)i0 * sx + (long long)j0 * sy + k0;
-            unsigned pv[4], m1 = 0, is1 = 0, is2o = 0;
+            vol[q] = act[q] ? spread_x(in2(i0, 0, G.s0)) & spread_y(in2(j0, 0, G.s1)) & spread_z(in2(k0, 0, G.s2)) : 0u;
+            base0[q] = (long long)i0 * sx + (long long)j0 * sy + k0;
+            wold[q] = act[q] ? Mw[b] : 0u;
+            oldn[q] = act[q] && Mn ? Mn[b] : 0u;
 #pragma unroll
             for (int t = 0; t < 4; t++) {
-                const int x = t >> 1, y = t & 1;
-                pv[t] = 0;
-                unsigned mv = 0;
-                if ((vol >> (2 * t)) & 3u) {
-                    const long long a = base0 + x * sx + y * sy;
+                pv[q][t] = 0;
+                mv[q][t] = 0;
+                if ((vol[q] >> (2 * t)) & 3u) {
+                    const long long a = base0[q] + (t >> 1) * sx + (t & 1) * sy;
                     if (pairs) {
-                        pv[t] = *(const uint16_t *)(mp + a);
-                        if (in_dil)
-                            mv = *(const uint16_t *)(morph + a);
+                        pv[q][t] = *(const uint16_t *)(mp + a);
+                        if (ind[q])
+                            mv[q][t] = *(const uint16_t *)(morph + a);
                     } else {
-                        pv[t] = mp[a];
-                        if (in_dil)
-                            mv = morph[a];
-                        if (vK & 2u) {
-                            pv[t] |= (unsigned)mp[a + 1] << 8;
-                            if (in_dil)
-                                mv |= (unsigned)morph[a + 1] << 8;
+                        pv[q][t] = mp[a];
+                        if (ind[q])
+                            mv[q][t] = morph[a];
+                        if ((vol[q] >> (2 * t)) & 2u) {
+                            pv[q][t] |= (unsigned)mp[a + 1] << 8;
+                            if (ind[q])
+                                mv[q][t] |= (unsigned)morph[a + 1] << 8;
                         }
                     }
                 }
-                m1 |= eq2(mv, 1) << (2 * t);
-                is1 |= eq2(pv[t], 1) << (2 * t);
-                is2o |= eq2(pv[t], 2) << (2 * t);
             }
-            // the wetting phase's outlet connection matters only where the
-            // dilation meets it
-            if (m1 & wet) {
-                const int rw = find_root(Pw, ld(Pw + b), err);
-                if (rw < 0 || !(markw[rw] & 2))
-                    wet = 0;
-            }
-            // voxels set to 1: invaded wetting voxels and reservoir slabs
-            const unsigned set1 = ((m1 & wet) | res) & vol;
-            unsigned is2 = 0;
+        }
 #pragma unroll
-            for (int t = 0; t < 4; t++) {
-                const unsigned bits = (set1 >> (2 * t)) & 3u;
-                if (bits) {
-                    const unsigned bm = (bits & 1u ? 0x00ffu : 0u) | (bits & 2u ? 0xff00u : 0u);
-                    pv[t] = (pv[t] & ~bm) | (0x0101u & bm);
-                    const long long a = base0 + (t >> 1) * sx + (t & 1) * sy;
-                    if (pairs) {
-                        *(uint16_t *)(mp + a) = (uint16_t)pv[t];
-                    } else {
-                        if (bits & 1u)
-                            mp[a] = 1;
-                        if (bits & 2u)
-                            mp[a + 1] = 1;
-                    }
+        for (int q = 0; q < NB; q++) {
+            const int b = bq[q];
+            bool changed = false;
+            if (act[q]) {
+                const int r = b / G.b2;
+                const int c2b = b - r * G.b2, c0 = r / G.b1, c1b = r - (r / G.b1) * G.b1;
+                const int i0 = 2 * c0, j0 = 2 * c1b, k0 = 2 * c2b;
+                // voxels inside the own box and the reservoir slabs
+                const unsigned v = vol[q];
+                const unsigned own = spread_x(in2(i0, B.own[0], B.own[1])) & spread_y(in2(j0, B.own[2], B.own[3])) &
+                                     spread_z(in2(k0, B.own[4], B.own[5]));
+                const unsigned res = (spread_x(~in2(i0, B.rpad[0], (long long)G.s0 - B.rpad[1]) & 3u) |
+                                      spread_y(~in2(j0, B.rpad[2], (long long)G.s1 - B.rpad[3]) & 3u) |
+                                      spread_z(~in2(k0, B.rpad[4], (long long)G.s2 - B.rpad[5]) & 3u)) &
+                                     v;
+                unsigned wet = wold[q];
+                unsigned m1 = 0, is1 = 0, is2o = 0;
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    m1 |= eq2(mv[q][t], 1) << (2 * t);
+                    is1 |= eq2(pv[q][t], 1) << (2 * t);
+                    is2o |= eq2(pv[q][t], 2) << (2 * t);
                 }
-                is2 |= eq2(pv[t], 2) << (2 * t);
-            }
-            const unsigned nwm = (is1 | set1) & vol;
-            if (wdirty && (is2 & vol) != wold) {
-                // the wetting phase changed here: its tile is recomputed next step
-                Mw[b] = (uint8_t)(is2 & vol);
-                const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
-                const int tl = ((c0 / kT0) * nt1 + c1b / kT1) * nt2 + c2b / kT2;
-                if (!wdirty[tl])
-                    wdirty[tl] = 1;
-            }
-            if (ranged) {
-                c2 += __popc(set1 & is2o & own & vol);
-                c1 += __popc(set1 & ~is1 & vol);
-            } else {
-                c2 += __popc(is2 & own & vol);
-                c1 += __popc(nwm);
-            }
-            if (Mn) {
-                const unsigned old = Mn[b];
-                if (nwm != old) {
-                    if (old & ~nwm)
+                // the wetting phase's outlet connection matters only where the
+                // dilation meets it
+                if (m1 & wet) {
+                    const int rw = find_root(Pw, ld(Pw + b), err);
+                    if (rw < 0 || !(markw[rw] & 2))
+                        wet = 0;
+                }
+                // voxels set to 1: invaded wetting voxels and reservoir slabs
+                const unsigned set1 = ((m1 & wet) | res) & v;
+                unsigned is2 = 0;
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const unsigned bits = (set1 >> (2 * t)) & 3u;
+                    unsigned p = pv[q][t];
+                    if (bits) {
+                        const unsigned bm = (bits & 1u ? 0x00ffu : 0u) | (bits & 2u ? 0xff00u : 0u);
+                        p = (p & ~bm) | (0x0101u & bm);
+                        const long long a = base0[q] + (t >> 1) * sx + (t & 1) * sy;
+                        if (pairs) {
+                            *(uint16_t *)(mp + a) = (uint16_t)p;
+                        } else {
+                            if (bits & 1u)
+                                mp[a] = 1;
+                            if (bits & 2u)
+                                mp[a + 1] = 1;
+                        }
+                    }
+                    is2 |= eq2(p, 2) << (2 * t);
+                }
+                const unsigned nwm = (is1 | set1) & v;
+                if (wdirty && (is2 & v) != wold[q]) {
+                    // the wetting phase changed here: its tile is recomputed next step
+                    Mw[b] = (uint8_t)(is2 & v);
+                    const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
+                    const int tl = ((c0 / kT0) * nt1 + c1b / kT1) * nt2 + c2b / kT2;
+                    if (!wdirty[tl])
+                        wdirty[tl] = 1;
+                }
+                if (ranged) {
+                    c2 += __popc(set1 & is2o & own & v);
+                    c1 += __popc(set1 & ~is1 & v);
+                } else {
+                    c2 += __popc(is2 & own & v);
+                    c1 += __popc(nwm);
+                }
+                if (Mn && nwm != oldn[q]) {
+                    if (oldn[q] & ~nwm)
                         atomicExch(err, 3);
                     Mn[b] = (uint8_t)nwm;
-                    if (!old)
+                    if (!oldn[q])
                         Pn[b] = b;
                     changed = true;
                 }
             }
-        }
-        if (Mn) {
-            const unsigned bal = __ballot_sync(0xffffffffu, changed);
-            if (bal) {
-                int pos = 0;
-                if (lane == 0)
-                    pos = atomicAdd(count, __popc(bal));
-                pos = __shfl_sync(0xffffffffu, pos, 0);
-                if (changed)
-                    list[pos + __popc(bal & ((1u << lane) - 1u))] = b;
+            if (Mn) {
+                const unsigned bal = __ballot_sync(0xffffffffu, changed);
+                if (bal) {
+                    int pos = 0;
+                    if (lane == 0)
+                        pos = atomicAdd(count, __popc(bal));
+                    pos = __shfl_sync(0xffffffffu, pos, 0);
+                    if (changed)
+                        list[pos + __popc(bal & ((1u << lane) - 1u))] = b;
+                }
             }
         }
     }
@@ -2602,7 +2665,7 @@ int drain_update_blocks(uint8_t *mp, const uint8_t *morph, const int64_t *shape,
     const int nb = G.b0 * G.b1 * G.b2;
     const long long n = shape[0] * shape[1] * shape[2];
     const int ps__ = prof_begin("k_drain_update_blocks", st);
-    k_drain_update_blocks<<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(
+    k_drain_update_blocks<<<grid_for((nb + kUpdateBatch - 1) / kUpdateBatch, 256, 152LL * 64), 256, 0, st>>>(
         mp, morph, P, M, mark, G, B, g_nw ? g_nw->M : nullptr, g_nw ? g_nw->P : nullptr,
         g_nw ? g_nw->list : nullptr, g_nw ? g_nw->count : nullptr, cnt2_own, cnt1, err, wdirty, orange,
         ranged ? 1 : 0, prof_units(kUnitsDrainUpdate));

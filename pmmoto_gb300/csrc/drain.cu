@@ -522,9 +522,11 @@ extern "C" int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const in
     if (s == PMG_OK) {
         grow_sel_init(g_nw, grow_mem, shape);
         g_nw.unite_label = "k_grow_unite[nonwetting]";
+        g_nw.unite_units = kUnitsGrowUniteB;
         if (grow_er) {
             grow_sel_init(g_er, (char *)grow_mem + gb, shape);
             g_er.unite_label = "k_grow_unite[eroded]";
+            g_er.unite_units = kUnitsGrowUniteA;
         }
     }
     // the blocks of the eroded space that grow at each radius, listed once

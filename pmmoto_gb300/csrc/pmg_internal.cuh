@@ -58,8 +58,9 @@ struct GrowSel {
     // step k's blocks are ev[off[k] .. off[k + 1])
     int *ev = nullptr;
     int *off = nullptr;
-    // profiler label of the union step
+    // profiler label of the union step, and its unit counter (-1: none)
     const char *unite_label = "k_grow_unite";
+    int unite_units = -1;
 };
 // Per-step lists of the blocks of a step volume S (steps < nsteps; 255:
 // never) that grow at that step, in one allocation *mem (freed by the caller).
