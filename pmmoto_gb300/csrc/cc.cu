@@ -2110,25 +2110,25 @@ __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, cons
                 xmax = max(xmax, c0 + 1);
                 xmin = max(xmin, kRangeBig - c0);
             }
-            if (BLK) {
+            if constexpr (BLK) {
                 out[b] = (uint8_t)mm;
-                continue;
-            }
+            } else {
 #pragma unroll
-            for (int x = 0; x < 2; x++)
+                for (int x = 0; x < 2; x++)
 #pragma unroll
-                for (int y = 0; y < 2; y++) {
-                    const int i = 2 * c0 + x, j = 2 * c1 + y;
-                    if (i >= G.s0 || j >= G.s1)
-                        continue;
-                    uint8_t *row = out + ((long long)i * G.s1 + j) * G.s2;
+                    for (int y = 0; y < 2; y++) {
+                        const int i = 2 * c0 + x, j = 2 * c1 + y;
+                        if (i >= G.s0 || j >= G.s1)
+                            continue;
+                        uint8_t *row = out + ((long long)i * G.s1 + j) * G.s2;
 #pragma unroll
-                    for (int z = 0; z < 2; z++) {
-                        const int k = 2 * c2 + z;
-                        if (k < G.s2)
-                            row[k] = (uint8_t)((mm >> ((x * 2 + y) * 2 + z)) & 1);
+                        for (int z = 0; z < 2; z++) {
+                            const int k = 2 * c2 + z;
+                            if (k < G.s2)
+                                row[k] = (uint8_t)((mm >> ((x * 2 + y) * 2 + z)) & 1);
+                        }
                     }
-                }
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
