@@ -1265,6 +1265,7 @@ constexpr int kBorderPlane = kT1 * kT2;
 constexpr int kBorderRows = (kT0 - 1) * 2 * kT2;
 constexpr int kBorderEnds = (kT0 - 1) * (kT1 - 2) * 2;
 constexpr int kBorder = kBorderPlane + kBorderRows + kBorderEnds;
+static_assert(kBorder <= 512, "a tile's border items fit one 512-thread block");
 
 __device__ __forceinline__ void border_block(int q, int &a, int &b, int &c)
 {
@@ -1319,55 +1320,64 @@ __device__ __forceinline__ void border_conn(const uint8_t *__restrict__ M, const
     }
 }
 
-__device__ __forceinline__ bool border_item(long long it, const BGrid &G, int nt1, int nt2, int &bi, int &c0, int &c1,
-                                            int &c2, int &a, int &b, int &c)
-{
-    const int tile = (int)(it / kBorder);
-    border_block((int)(it - (long long)tile * kBorder), a, b, c);
-    c0 = (tile / (nt1 * nt2)) * kT0 + a;
-    c1 = ((tile / nt2) % nt1) * kT1 + b;
-    c2 = (tile % nt2) * kT2 + c;
-    if (c0 >= G.b0 || c1 >= G.b1 || c2 >= G.b2)
-        return false;
-    bi = (c0 * G.b1 + c1) * G.b2 + c2;
-    return true;
-}
-
 // Phase 2a: border blocks whose cross-tile links need no union (empty, no
 // touching neighbour outside the tile, or dense with an in-tile neighbour
-// that links them all) stop here; the others are listed for phase 2b, so
-// that its warps run full.
-__global__ void k_bcc_cross(int *P, const uint8_t *__restrict__ M, BGrid G, int *err, int *hard, int *nhard)
+// that links them all) stop here; the others are listed for phase 2b (as
+// block indices), so that its warps run full.  One thread block per tile,
+// border item t on thread t.  The in-tile neighbours matter only for the
+// dense rule, so only full blocks read their masks.
+__global__ void __launch_bounds__(512) k_bcc_cross(const uint8_t *__restrict__ M, BGrid G, int *hard, int *nhard)
 {
     const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
-    const long long items = (long long)((G.b0 + kT0 - 1) / kT0) * nt1 * nt2 * kBorder;
-    const int lane = threadIdx.x & 31;
-    for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < items;
-         base += (long long)gridDim.x * blockDim.x) {
-        const long long it = base + lane;
-        bool need = false;
-        int bi, c0, c1, c2, a, b, c;
-        if (it < items && border_item(it, G, nt1, nt2, bi, c0, c1, c2, a, b, c)) {
-            const unsigned m = M[bi];
-            if (m) {
-                unsigned conn, local;
-                bool full;
-                uint64_t mlo, mhi;
-                border_conn(M, G, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
-                // in-tile neighbours were united in phase 1, and so was
-                // everything touching them
-                need = (conn & ~local) != 0 && !(full && ((conn >> kCentre) & 1u) && local);
+    const int tile = blockIdx.x;
+    const int ti = tile / (nt1 * nt2), tj = (tile / nt2) % nt1, tk = tile % nt2;
+    const int t = threadIdx.x;
+    bool need = false;
+    int bi = -1;
+    if (t < kBorder) {
+        int a, b, c;
+        border_block(t, a, b, c);
+        const int c0 = ti * kT0 + a, c1 = tj * kT1 + b, c2 = tk * kT2 + c;
+        const unsigned m = c0 < G.b0 && c1 < G.b1 && c2 < G.b2 ? M[(c0 * G.b1 + c1) * G.b2 + c2] : 0u;
+        bi = (c0 * G.b1 + c1) * G.b2 + c2;
+        if (m) {
+            unsigned conn = 0, local = 0;
+            bool full = m == 0xffu;
+#pragma unroll
+            for (int q = 0; q < 13; q++) {
+                const int a0 = c0 + c_nb[q][0], a1 = c1 + c_nb[q][1], a2 = c2 + c_nb[q][2];
+                if (a0 < 0 || a1 < 0 || a2 < 0 || a1 >= G.b1 || a2 >= G.b2)
+                    continue;
+                if (!(m & c_bt_self[q]))
+                    continue;
+                const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
+                const bool in_tile = aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2;
+                if (in_tile && m != 0xffu)
+                    continue;
+                const unsigned mn = M[(a0 * G.b1 + a1) * G.b2 + a2];
+                if (!(mn & c_bt_nb[q]))
+                    continue;
+                conn |= 1u << q;
+                full = full && mn == 0xffu;
+                if (in_tile)
+                    local |= 1u << q;
             }
+            // in-tile neighbours were united in phase 1, and so was
+            // everything touching them
+            need = (conn & ~local) != 0 && !(full && ((conn >> kCentre) & 1u) && local);
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, need);
-        if (bal) {
-            int pos = 0;
-            if (lane == 0)
-                pos = atomicAdd(nhard, __popc(bal));
-            pos = __shfl_sync(0xffffffffu, pos, 0);
-            if (need)
-                hard[pos + __popc(bal & ((1u << lane) - 1u))] = (int)it;
-        }
+    }
+    if (t >= (kBorder + 31) / 32 * 32)
+        return; // warps without border items
+    const int lane = t & 31;
+    const unsigned bal = __ballot_sync(0xffffffffu, need);
+    if (bal) {
+        int pos = 0;
+        if (lane == 0)
+            pos = atomicAdd(nhard, __popc(bal));
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (need)
+            hard[pos + __popc(bal & ((1u << lane) - 1u))] = bi;
     }
 }
 
@@ -1379,14 +1389,15 @@ __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G
     __shared__ BTabs tb;
     load_btabs(tb);
     __syncthreads();
-    const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
     const int cnt = *nhard;
     if (units && blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0)
         atomicAdd(units, (unsigned long long)cnt);
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < cnt; h += gridDim.x * blockDim.x) {
-        int bi, c0, c1, c2, a, b, c;
-        if (!border_item(hard[h], G, nt1, nt2, bi, c0, c1, c2, a, b, c))
-            continue;
+        // listed border blocks (block indices) and their offsets in their tile
+        const int bi = hard[h];
+        const int r = bi / G.b2;
+        const int c2 = bi - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+        const int a = c0 % kT0, b = c1 % kT1, c = c2 % kT2;
         const unsigned m = M[bi];
         unsigned conn, local;
         bool full;
@@ -1507,17 +1518,44 @@ __global__ void k_bcc_flatten(int *P, int nb, int *err)
     }
 }
 
+// two consecutive coordinates v0, v0 + 1 inside [lo, hi): bits 0, 1
+__device__ __forceinline__ unsigned in2(int v0, long long lo, long long hi)
+{
+    return (unsigned)(v0 >= lo && v0 < hi) | ((unsigned)(v0 + 1 >= lo && v0 + 1 < hi) << 1);
+}
+
+// per-axis 2-bit masks spread over the block's bit layout (x * 2 + y) * 2 + z
+__device__ __forceinline__ unsigned spread_x(unsigned a) { return (a & 1 ? 0x0Fu : 0u) | (a & 2 ? 0xF0u : 0u); }
+__device__ __forceinline__ unsigned spread_y(unsigned a) { return (a & 1 ? 0x33u : 0u) | (a & 2 ? 0xCCu : 0u); }
+__device__ __forceinline__ unsigned spread_z(unsigned a) { return (a & 1 ? 0x55u : 0u) | (a & 2 ? 0xAAu : 0u); }
+
+// bytes 0 and 1 of a 16-bit pair equal to v: bits 0, 1
+__device__ __forceinline__ unsigned eq2(unsigned pair, unsigned v)
+{
+    return (unsigned)((pair & 0xffu) == v) | ((unsigned)((pair >> 8) == v) << 1);
+}
+
+// Marks of the roots of the blocks with a foreground voxel inside the box:
+// one thread per block that meets the box.
 __global__ void k_bcc_mark(const uint8_t *__restrict__ M, const int *__restrict__ P, BGrid G, Box bx,
                            uint8_t *mark, uint8_t bit, int *err)
 {
-    const long long n = bx.size();
-    const long long w = bx.hi[2] - bx.lo[2], h = bx.hi[1] - bx.lo[1];
+    long long lo[3], nbk[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = bx.lo[d] >> 1;
+        nbk[d] = ((bx.hi[d] + 1) >> 1) - lo[d];
+    }
+    const long long n = nbk[0] * nbk[1] * nbk[2];
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
-        const long long k = bx.lo[2] + q % w, j = bx.lo[1] + (q / w) % h, i = bx.lo[0] + q / (w * h);
-        if (!mfg(M, G, i, j, k))
+        const int c2 = (int)(lo[2] + q % nbk[2]), c1 = (int)(lo[1] + (q / nbk[2]) % nbk[1]),
+                  c0 = (int)(lo[0] + q / (nbk[2] * nbk[1]));
+        const int b = (c0 * G.b1 + c1) * G.b2 + c2;
+        const unsigned inbox = spread_x(in2(2 * c0, bx.lo[0], bx.hi[0])) & spread_y(in2(2 * c1, bx.lo[1], bx.hi[1])) &
+                               spread_z(in2(2 * c2, bx.lo[2], bx.hi[2]));
+        if (!(M[b] & inbox))
             continue;
-        int p = ld(P + ((int)(i >> 1) * G.b1 + (int)(j >> 1)) * G.b2 + (int)(k >> 1));
+        int p = ld(P + b);
         if (p >= 0)
             p = find_root(P, p, err);
         if (p >= 0 && !(mark[p] & bit))
@@ -1642,7 +1680,8 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
         PMG_CUDA(cudaMemsetAsync(nhard, 0, sizeof(int), st));
         {
             const int ps__ = prof_begin("k_bcc_cross", st);
-            k_bcc_cross<<<grid_for(border, 256, 152LL * 64), 256, 0, st>>>(P, M, G, err, hard, nhard);
+            const int nt = (int)(border / kBorder);
+            k_bcc_cross<<<nt, 512, 0, st>>>(M, G, hard, nhard);
             // per border block: its mask, the mask facing it across the tile
             // border
             prof_end(ps__, (double)border * 2, st);
@@ -1710,10 +1749,13 @@ static int bcc_marks(const int64_t *shape, const int64_t *inlet_box, const int64
             b.hi[d] = bxp[2 * d + 1];
         }
         if (b.size() > 0) {
+            long long nbk = 1;
+            for (int d = 0; d < 3; d++)
+                nbk *= ((b.hi[d] + 1) >> 1) - (b.lo[d] >> 1);
             const int ps__ = prof_begin("k_bcc_mark", st);
-            k_bcc_mark<<<grid_for(b.size(), 256, 1LL << 30), 256, 0, st>>>(M, P, G, b, mark, (uint8_t)(1 << w),
-                                                                          err);
-            prof_end(ps__, (double)b.size() * 5, st);
+            k_bcc_mark<<<grid_for(nbk, 256, 1LL << 30), 256, 0, st>>>(M, P, G, b, mark, (uint8_t)(1 << w), err);
+            // per block meeting the box: mask, parent, root parent
+            prof_end(ps__, (double)nbk * 9, st);
             PMG_CHECK_LAUNCH();
         }
     }
@@ -2441,22 +2483,6 @@ int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64
 // union-find (outlet mark bit 1), so no selected image is written.  With Mn,
 // the block masks of the non-wetting phase (value 1) are brought up to date
 // and grown blocks are listed for its next growing-selection step.
-// two consecutive coordinates v0, v0 + 1 inside [lo, hi): bits 0, 1
-__device__ __forceinline__ unsigned in2(int v0, long long lo, long long hi)
-{
-    return (unsigned)(v0 >= lo && v0 < hi) | ((unsigned)(v0 + 1 >= lo && v0 + 1 < hi) << 1);
-}
-
-// per-axis 2-bit masks spread over the block's bit layout (x * 2 + y) * 2 + z
-__device__ __forceinline__ unsigned spread_x(unsigned a) { return (a & 1 ? 0x0Fu : 0u) | (a & 2 ? 0xF0u : 0u); }
-__device__ __forceinline__ unsigned spread_y(unsigned a) { return (a & 1 ? 0x33u : 0u) | (a & 2 ? 0xCCu : 0u); }
-__device__ __forceinline__ unsigned spread_z(unsigned a) { return (a & 1 ? 0x55u : 0u) | (a & 2 ? 0xAAu : 0u); }
-
-// bytes 0 and 1 of a 16-bit pair equal to v: bits 0, 1
-__device__ __forceinline__ unsigned eq2(unsigned pair, unsigned v)
-{
-    return (unsigned)((pair & 0xffu) == v) | ((unsigned)((pair >> 8) == v) << 1);
-}
 
 constexpr int kUpdateBatch = 2;
 
