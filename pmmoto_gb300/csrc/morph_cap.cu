@@ -314,13 +314,14 @@ __global__ void __launch_bounds__(128) k_cap_mid(const uint16_t *__restrict__ KA
 // thread, packed in the halves of a 32-bit word, and each pair of terms costs
 // two packed add-min instructions (values stay below 2^11: no carries between
 // the halves).  The heights of a segment live in a register ring of
-// R = 2W + 1 + kPairAhead words whose slots are fixed at compile time: at
+// R = 2W + 1 + pair_ahead(W) words whose slots are fixed at compile time: at
 // step u of a group of R outputs starting at y0, slot s holds position
 // y0 - W + s (s >= u) or y0 - W + s + R (s < u), so the term at y + d sits in
 // slot (u + W + d) mod R, and the slot of y - W, dead after output y, takes
-// position y + W + 1 + kPairAhead (loaded kPairAhead steps before its use).
-constexpr int kPairAhead = 8;
-constexpr int kPairMaxW = 15;
+// position y + W + 1 + pair_ahead(W) (loaded that many steps before its use).
+constexpr int kPairMaxW = 20;
+// heights loaded ahead: fewer for the wide windows, whose rings hold more
+__host__ __device__ constexpr int pair_ahead(int W) { return W <= 12 ? 8 : 4; }
 
 // Lines of a pass on pairs: AX = 1, pairs over (x0 in [0, X0), x2 / 2 in
 // [k0 / 2, (k0 + nk) / 2)) along axis 1; AX = 0, pairs over (x1 in [j0, j0 +
@@ -340,7 +341,7 @@ __global__ void __launch_bounds__(256) k_cap_mid_pair(const uint16_t *__restrict
                                                       const int *__restrict__ xr, int seglen,
                                                       unsigned long long *units)
 {
-    constexpr int R = 2 * W + 1 + kPairAhead;
+    constexpr int R = 2 * W + 1 + pair_ahead(W);
     if (gate && *gate == 0)
         return;
     SeedRange sr{0, 0x7fffffff, 0, 0};
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(256) k_cap_mid_pair(const uint16_t *__restrict
                 }
                 if (y < b)
                     out[y * st] = m;
-                const int yn = y + W + 1 + kPairAhead;
+                const int yn = y + W + 1 + pair_ahead(W);
                 win[u] = y < b && yn < n ? __ldg(in + yn * st) : bigp;
             }
         }
@@ -525,7 +526,7 @@ __global__ void __launch_bounds__(256) k_cap_last_pair(const uint16_t *__restric
                                                        const int *__restrict__ xr, int *__restrict__ orange,
                                                        int seglen, unsigned long long *units)
 {
-    constexpr int R = 2 * W + 1 + kPairAhead;
+    constexpr int R = 2 * W + 1 + pair_ahead(W);
     SeedRange sr{0, G.X0 - 1, 0, G.X0 - 1};
     if (xr)
         sr.load(xr, G.X0, W);
@@ -604,7 +605,7 @@ __global__ void __launch_bounds__(256) k_cap_last_pair(const uint16_t *__restric
                     *dst = (uint16_t)v;
                     dst += ostw;
                 }
-                const int yn = y + W + 1 + kPairAhead;
+                const int yn = y + W + 1 + pair_ahead(W);
                 win[u] = y < b && yn >= hlo && yn < hend ? __ldg(in + yn * st) : bigp;
             }
         }
@@ -613,7 +614,7 @@ __global__ void __launch_bounds__(256) k_cap_last_pair(const uint16_t *__restric
 
 // Segment length of the pair kernels: whole groups of the register ring,
 // about four per segment.
-static int pair_seglen(int W) { return 4 * (2 * W + 1 + kPairAhead); }
+static int pair_seglen(int W) { return 4 * (2 * W + 1 + pair_ahead(W)); }
 
 // Calls f with std::integral_constant<int, w> for 0 <= w <= kPairMaxW.
 template <int W, class F>

@@ -67,8 +67,8 @@ def test_morph_errors(M):
                                    ("wall", "end", "periodic")])
 @pytest.mark.parametrize("vox", [(36, 35, 38), (37, 40, 36), (39, 36, 37)])
 def test_morph_window_widths_vs_oracle(M, kinds, vox):
-    """Power-of-two voxels (1/32) with radii of W + 1/2 voxels, W = 0 .. 16:
-    the integer passes take direct minima on line pairs for W <= 15 when the
+    """Power-of-two voxels (1/32) with radii of W + 1/2 voxels, W = 0 .. 21:
+    the integer passes take direct minima on line pairs for W <= 20 when the
     contiguous extent is even, the parabola envelope otherwise."""
     rng = np.random.default_rng(7 + sum(vox) + sum(map(ord, "".join(kinds))))
     scale = 32
@@ -82,7 +82,7 @@ def test_morph_window_widths_vs_oracle(M, kinds, vox):
     few[tuple(rng.integers(0, v, 6) for v in sd.voxels)] = 1
     sparse = O.update_buffer(g, few)
     dense = O.update_buffer(g, 1 - few)
-    for w in range(0, 17):
+    for w in range(0, 22):
         r = (w + 0.5) / scale
         if r < 1.0 / scale:
             continue  # the reference rejects radii below the voxel size
