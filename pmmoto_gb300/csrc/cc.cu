@@ -1168,6 +1168,23 @@ __device__ __forceinline__ unsigned block_mask(const SrcMask &src, const BGrid &
     return src.M[((long long)c0 * G.b1 + c1) * G.b2 + c2];
 }
 
+// The 13 earlier neighbours in the order of c_nb, as arithmetic of the index
+// (constants once a loop over q is unrolled): (-1, q / 3 - 1, q % 3 - 1) for
+// q < 9, (0, -1, q - 10) for q < 12, (0, 0, -1) for q = 12.
+__device__ __forceinline__ int nb_d0(int q) { return q < 9 ? -1 : 0; }
+__device__ __forceinline__ int nb_d1(int q) { return q < 9 ? q / 3 - 1 : (q < 12 ? -1 : 0); }
+__device__ __forceinline__ int nb_d2(int q) { return q < 9 ? q % 3 - 1 : (q < 12 ? q - 10 : -1); }
+
+// Voxels of a block that touch its neighbour at offset (d0, d1, d2): bit
+// (x * 2 + y) * 2 + z, x on the d0 side and so on.
+__device__ __forceinline__ unsigned touch_bits(int d0, int d1, int d2)
+{
+    const unsigned X = d0 < 0 ? 0x0Fu : d0 > 0 ? 0xF0u : 0xFFu;
+    const unsigned Y = d1 < 0 ? 0x33u : d1 > 0 ? 0xCCu : 0xFFu;
+    const unsigned Z = d2 < 0 ? 0x55u : d2 > 0 ? 0xAAu : 0xFFu;
+    return X & Y & Z;
+}
+
 // Phase 1 on tiles of 4 x 8 x 32 blocks (8 x 16 x 64 voxels), one thread per
 // block: block masks from the source, then a shared-memory union-find of the
 // tile whose roots are the smallest block index of each tile-local part.
@@ -1208,13 +1225,13 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
         bool full = m == 0xffu; // this block and every connected neighbour full
 #pragma unroll
         for (int q = 0; q < 13; q++) {
-            const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
+            const int aa = a + nb_d0(q), bb = b + nb_d1(q), cc = c + nb_d2(q);
             if (aa < 0 || bb < 0 || bb >= kT1 || cc < 0 || cc >= kT2)
                 continue;
-            if (!(m & c_bt_self[q]))
+            if (!(m & touch_bits(nb_d0(q), nb_d1(q), nb_d2(q))))
                 continue;
             const unsigned mn = sm[(aa * kT1 + bb) * kT2 + cc];
-            if (mn & c_bt_nb[q]) {
+            if (mn & touch_bits(-nb_d0(q), -nb_d1(q), -nb_d2(q))) {
                 conn |= 1u << q;
                 full = full && mn == 0xffu;
                 if (q < 8)
@@ -1289,35 +1306,56 @@ __device__ __forceinline__ void border_block(int q, int &a, int &b, int &c)
 // Touching earlier neighbours of border block (c0, c1, c2) at tile offset
 // (a, b, c): conn, those inside the tile (local), the dense flag and their
 // masks (mlo: neighbours 0-7, mhi: 8-12).
-__device__ __forceinline__ void border_conn(const uint8_t *__restrict__ M, const BGrid &G, int c0, int c1, int c2,
-                                            int a, int b, int c, unsigned m, unsigned &conn, unsigned &local,
-                                            bool &full, uint64_t &mlo, uint64_t &mhi)
+// Touching earlier neighbours of border block bi = (c0, c1, c2) at tile
+// offset (a, b, c): conn, those inside the tile (local), the dense flag and
+// their masks (MASKS: mlo for neighbours 0-7, mhi for 8-12).  INTERIOR: all
+// 13 neighbours lie inside the volume (no bounds checks).  LAZY: in-tile
+// neighbours are read only when the block is full (their only use in the
+// cross-tile test is the dense rule).
+template <bool INTERIOR, bool LAZY, bool MASKS>
+__device__ __forceinline__ void border_conn(const uint8_t *__restrict__ M, const BGrid &G, int bi, int c0, int c1,
+                                            int c2, int a, int b, int c, unsigned m, unsigned &conn,
+                                            unsigned &local, bool &full, uint64_t &mlo, uint64_t &mhi)
 {
     conn = 0;
     local = 0;
     mlo = 0;
     mhi = 0;
     full = m == 0xffu;
+    const int plane = G.b1 * G.b2;
 #pragma unroll
     for (int q = 0; q < 13; q++) {
-        const int a0 = c0 + c_nb[q][0], a1 = c1 + c_nb[q][1], a2 = c2 + c_nb[q][2];
-        if (a0 < 0 || a1 < 0 || a2 < 0 || a1 >= G.b1 || a2 >= G.b2)
+        const int d0 = nb_d0(q), d1 = nb_d1(q), d2 = nb_d2(q);
+        if (!INTERIOR) {
+            const int a0 = c0 + d0, a1 = c1 + d1, a2 = c2 + d2;
+            if (a0 < 0 || a1 < 0 || a2 < 0 || a1 >= G.b1 || a2 >= G.b2)
+                continue;
+        }
+        if (!(m & touch_bits(d0, d1, d2)))
             continue;
-        if (!(m & c_bt_self[q]))
+        const bool in_tile = a + d0 >= 0 && b + d1 >= 0 && b + d1 < kT1 && c + d2 >= 0 && c + d2 < kT2;
+        if (LAZY && in_tile && m != 0xffu)
             continue;
-        const unsigned mn = M[(a0 * G.b1 + a1) * G.b2 + a2];
-        if (!(mn & c_bt_nb[q]))
+        const unsigned mn = M[bi + d0 * plane + d1 * G.b2 + d2];
+        if (!(mn & touch_bits(-d0, -d1, -d2)))
             continue;
         conn |= 1u << q;
         full = full && mn == 0xffu;
-        if (q < 8)
-            mlo |= (uint64_t)mn << (8 * q);
-        else
-            mhi |= (uint64_t)mn << (8 * (q - 8));
-        const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
-        if (aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2)
+        if (MASKS) {
+            if (q < 8)
+                mlo |= (uint64_t)mn << (8 * q);
+            else
+                mhi |= (uint64_t)mn << (8 * (q - 8));
+        }
+        if (in_tile)
             local |= 1u << q;
     }
+}
+
+// All 13 earlier neighbours of block (c0, c1, c2) inside the volume.
+__device__ __forceinline__ bool nb_interior(const BGrid &G, int c0, int c1, int c2)
+{
+    return c0 >= 1 && c1 >= 1 && c1 + 1 < G.b1 && c2 >= 1 && c2 + 1 < G.b2;
 }
 
 // Phase 2a: border blocks whose cross-tile links need no union (empty, no
@@ -1341,27 +1379,13 @@ __global__ void __launch_bounds__(512) k_bcc_cross(const uint8_t *__restrict__ M
         const unsigned m = c0 < G.b0 && c1 < G.b1 && c2 < G.b2 ? M[(c0 * G.b1 + c1) * G.b2 + c2] : 0u;
         bi = (c0 * G.b1 + c1) * G.b2 + c2;
         if (m) {
-            unsigned conn = 0, local = 0;
-            bool full = m == 0xffu;
-#pragma unroll
-            for (int q = 0; q < 13; q++) {
-                const int a0 = c0 + c_nb[q][0], a1 = c1 + c_nb[q][1], a2 = c2 + c_nb[q][2];
-                if (a0 < 0 || a1 < 0 || a2 < 0 || a1 >= G.b1 || a2 >= G.b2)
-                    continue;
-                if (!(m & c_bt_self[q]))
-                    continue;
-                const int aa = a + c_nb[q][0], bb = b + c_nb[q][1], cc = c + c_nb[q][2];
-                const bool in_tile = aa >= 0 && bb >= 0 && bb < kT1 && cc >= 0 && cc < kT2;
-                if (in_tile && m != 0xffu)
-                    continue;
-                const unsigned mn = M[(a0 * G.b1 + a1) * G.b2 + a2];
-                if (!(mn & c_bt_nb[q]))
-                    continue;
-                conn |= 1u << q;
-                full = full && mn == 0xffu;
-                if (in_tile)
-                    local |= 1u << q;
-            }
+            unsigned conn, local;
+            bool full;
+            uint64_t mlo, mhi;
+            if (nb_interior(G, c0, c1, c2))
+                border_conn<true, true, false>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+            else
+                border_conn<false, true, false>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
             // in-tile neighbours were united in phase 1, and so was
             // everything touching them
             need = (conn & ~local) != 0 && !(full && ((conn >> kCentre) & 1u) && local);
@@ -1402,7 +1426,10 @@ __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G
         unsigned conn, local;
         bool full;
         uint64_t mlo, mhi;
-        border_conn(M, G, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+        if (nb_interior(G, c0, c1, c2))
+            border_conn<true, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+        else
+            border_conn<false, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
         unsigned covered = 0;
         if (full && ((conn >> kCentre) & 1u))
             covered = conn & ~(1u << kCentre); // the centre links all of them
@@ -1883,15 +1910,6 @@ __global__ void k_grow_masks(Src src, uint8_t *__restrict__ M, int *__restrict__
     }
 }
 
-// Voxels of a block that touch its neighbour at offset (d0, d1, d2): bit
-// (x * 2 + y) * 2 + z, x on the d0 side and so on.
-__device__ __forceinline__ unsigned touch_bits(int d0, int d1, int d2)
-{
-    const unsigned X = d0 < 0 ? 0x0Fu : d0 > 0 ? 0xF0u : 0xFFu;
-    const unsigned Y = d1 < 0 ? 0x33u : d1 > 0 ? 0xCCu : 0xFFu;
-    const unsigned Z = d2 < 0 ? 0x55u : d2 > 0 ? 0xAAu : 0xFFu;
-    return X & Y & Z;
-}
 
 // One warp per listed block, one lane per neighbour (lanes 0-25): every lane
 // loads its neighbour's mask and parent at once.  The parents were flattened
