@@ -1246,7 +1246,7 @@ __global__ void __launch_bounds__(kTile, 2) k_bcc_tile(Src src, int *__restrict_
         while (conn & ~covered) {
             const unsigned rest = conn & ~covered;
             const int q = next_cover(rest);
-            sunite(L, t, ((a + c_nb[q][0]) * kT1 + b + c_nb[q][1]) * kT2 + c + c_nb[q][2]);
+            sunite(L, t, ((a + nb_d0(q)) * kT1 + b + nb_d1(q)) * kT2 + c + nb_d2(q));
             covered |= bcover1(q, rest, mlo, mhi, tb);
         }
     }
@@ -1440,7 +1440,7 @@ __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G
         while (conn & ~covered) {
             const unsigned rest = conn & ~covered;
             const int q = next_cover(rest);
-            unite(P, bi, ((c0 + c_nb[q][0]) * G.b1 + c1 + c_nb[q][1]) * G.b2 + c2 + c_nb[q][2], err);
+            unite(P, bi, bi + nb_d0(q) * G.b1 * G.b2 + nb_d1(q) * G.b2 + nb_d2(q), err);
             covered |= bcover(q, rest, mlo, mhi, tb);
         }
     }
