@@ -2504,7 +2504,7 @@ int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64
 
 constexpr int kUpdateBatch = 2;
 
-__global__ void k_drain_update_blocks(uint8_t *__restrict__ mp, const uint8_t *__restrict__ morph, int *Pw,
+__global__ void __launch_bounds__(256, 5) k_drain_update_blocks(uint8_t *__restrict__ mp, const uint8_t *__restrict__ morph, int *Pw,
                                       uint8_t *__restrict__ Mw, const uint8_t *__restrict__ markw, BGrid G,
                                       Boxes B, uint8_t *__restrict__ Mn, int *__restrict__ Pn,
                                       int *__restrict__ list, int *count, unsigned long long *cnt2,
