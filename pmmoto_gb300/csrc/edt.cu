@@ -26,13 +26,13 @@
 // multiply-add contraction, in the reference's operation order.
 #include <cfloat>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 
 #include "edt_internal.cuh"
 
 namespace pmg {
 
-constexpr int kMaxHull = 8; // imported hulls per side (reference keeps <= 5)
 
 // ---------------------------------------------------------------------------
 // pass 0: squared_edt_1d along axis `ax`
@@ -796,7 +796,7 @@ static bool window_path_ok(float res, int n)
 
 int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                     const pmg_axis_cfg &cfg, int num_hull, int form, const MorphEpi &me,
-                    cudaStream_t st, int cap)
+                    cudaStream_t st, int cap, int *flag_buf, long long flag_cap)
 {
     const int n = (int)(Ls.ax == 0 ? Ls.s0 : Ls.ax == 1 ? Ls.s1 : Ls.s2);
     int block = envelope_block(n);
@@ -808,26 +808,42 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
         // windowed exact minimum everywhere, the float envelope on the end
         // segments of periodic lines (or whole lines) the window kernel flags
         const long long nl = Ls.count();
-        int *flag = nullptr;
-        PMG_TRY(scratch_alloc((void **)&flag, sizeof(int) * (size_t)nl, st));
-        int s = cudaMemsetAsync(flag, 0, sizeof(int) * (size_t)nl, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-        if (s == PMG_OK) {
-            const float a = res * res;
-            const int ps__ = prof_begin("k_env_window", st);
-            const bool contiguous = Ls.ax == 2;
-            k_env_window<<<grid_for(contiguous ? nl * 32 : nl * ((n + 63) / 64), 256, 152LL * 32), 256, 0, st>>>(
-                fin, fout, Ls, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
-            prof_end(ps__, (double)nl * n * 8, st);
-            s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        int *flag = flag_buf;
+        if (!flag)
+            PMG_TRY(scratch_alloc((void **)&flag, sizeof(int) * (size_t)nl, st));
+        // a caller-supplied flag buffer smaller than the line count is used
+        // for one block of rows (lines along the first other axis) at a time
+        const int rows = flag_buf ? (int)std::min<long long>(Ls.nb1, std::max<long long>(1, flag_cap / Ls.nb2))
+                                  : Ls.nb1;
+        int s = PMG_OK;
+        if (flag_buf && (long long)Ls.nb2 > flag_cap) {
+            set_error("envelope: flag buffer of %lld lines holds less than one row of %d lines", flag_cap, Ls.nb2);
+            s = PMG_EINVAL;
         }
-        if (s == PMG_OK) {
-            const int ps__ = prof_begin("k_envelope_ends", st);
-            k_envelope_ends<<<grid_for(nl, block, 1LL << 30), block, smem, st>>>(fin, fout, Ls, res, cfg, num_hull,
-                                                                                form, flag);
-            prof_end(ps__, 0.0, st);
-            s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+        for (int r0 = 0; s == PMG_OK && r0 < Ls.nb1; r0 += rows) {
+            Lines C = Ls;
+            C.b1lo = Ls.b1lo + r0;
+            C.nb1 = std::min(rows, Ls.nb1 - r0);
+            const long long nc = C.count();
+            s = cudaMemsetAsync(flag, 0, sizeof(int) * (size_t)nc, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            if (s == PMG_OK) {
+                const float a = res * res;
+                const int ps__ = prof_begin("k_env_window", st);
+                const bool contiguous = C.ax == 2;
+                k_env_window<<<grid_for(contiguous ? nc * 32 : nc * ((n + 63) / 64), 256, 152LL * 32), 256, 0, st>>>(
+                    fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
+                prof_end(ps__, (double)nc * n * 8, st);
+                s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            }
+            if (s == PMG_OK) {
+                const int ps__ = prof_begin("k_envelope_ends", st);
+                k_envelope_ends<<<grid_for(nc, block, 1LL << 30), block, smem, st>>>(fin, fout, C, res, cfg, num_hull,
+                                                                                    form, flag);
+                prof_end(ps__, 0.0, st);
+                s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            }
         }
-        const int s2 = scratch_free(flag, st);
+        const int s2 = flag_buf ? PMG_OK : scratch_free(flag, st);
         return s != PMG_OK ? s : s2;
     }
     int redo = 0;
@@ -865,14 +881,15 @@ static int check_shape(const int64_t *shape, int nd)
 // EDT with one ping-pong buffer: pass 0 -> out, envelope 1: out -> tmp,
 // envelope 2: tmp -> out.
 int edt3d_run(const uint8_t *img, float *out, float *tmp, const int64_t *shape, const float *res,
-              const pmg_axis_cfg *cfg, int num_hull, int form, cudaStream_t st)
+              const pmg_axis_cfg *cfg, int num_hull, int form, cudaStream_t st, int *flag_buf,
+              long long flag_cap)
 {
     MorphEpi none{};
     PMG_TRY(launch_pass0(img, out, all_lines(shape, 0), res[0], cfg[0], st));
     PMG_TRY(launch_envelope(out, tmp, all_lines(shape, 1), res[1], cfg[1], num_hull,
-                            PMG_EDT_SQUARED, none, st));
+                            PMG_EDT_SQUARED, none, st, INT_MAX, flag_buf, flag_cap));
     PMG_TRY(launch_envelope(tmp, out, all_lines(shape, 2), res[2], cfg[2], num_hull, form, none,
-                            st));
+                            st, INT_MAX, flag_buf, flag_cap));
     return PMG_OK;
 }
 

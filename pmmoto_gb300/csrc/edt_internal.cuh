@@ -8,6 +8,10 @@
 
 namespace pmg {
 
+// Imported boundary hulls per side the envelope kernels hold (the reference
+// keeps at most num_hull + 1 = 5); entry points accept num_hull + 1 <= kMaxHull.
+constexpr int kMaxHull = 8;
+
 // Lines of a pass: all lines along axis `ax` whose coordinates on the other
 // two axes (d1 < d2) lie in [b1lo, b1lo + nb1) x [b2lo, b2lo + nb2).
 struct Lines {
@@ -157,10 +161,13 @@ int edt_cap_run(const uint8_t *E, uint16_t *KA, uint16_t *KB, uint16_t *KC, cons
 
 int launch_pass0(const uint8_t *img, float *out, const Lines &Ls, float res,
                  const pmg_axis_cfg &cfg, cudaStream_t st);
+// flag_buf (optional): per-line flags of the windowed path, flag_cap lines
+// long; without it the flags come from the stream-ordered scratch pool.
 int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                     const pmg_axis_cfg &cfg, int num_hull, int form, const MorphEpi &me,
-                    cudaStream_t st, int cap = INT_MAX);
+                    cudaStream_t st, int cap = INT_MAX, int *flag_buf = nullptr, long long flag_cap = 0);
 int edt3d_run(const uint8_t *img, float *out, float *tmp, const int64_t *shape, const float *res,
-              const pmg_axis_cfg *cfg, int num_hull, int form, cudaStream_t st);
+              const pmg_axis_cfg *cfg, int num_hull, int form, cudaStream_t st, int *flag_buf = nullptr,
+              long long flag_cap = 0);
 
 } // namespace pmg

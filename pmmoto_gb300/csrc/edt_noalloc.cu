@@ -9,11 +9,14 @@
 // pmg_edt3d_noalloc uses a fixed scratch array reserved in this file instead
 // of allocating; the caller still passes the input and output buffers.
 //
-// The array is a file-scope __device__ variable: every GPU that loads this
-// library holds it (64 MiB) until the process exits.  Host code may not use
-// the array's name as a device address, so the first call on each device
-// resolves the address with cudaGetSymbolAddress while that device is
-// current and caches it.
+// The arrays are file-scope __device__ variables: every GPU that loads this
+// library holds them (64 MiB for the intermediate volume, 4 MiB for the
+// per-line flags of the windowed envelope path) until the process exits.
+// Host code may not use an array's name as a device address, so the first
+// call on each device resolves both addresses with cudaGetSymbolAddress
+// while that device is current and caches them.  The cache is not
+// invalidated by cudaDeviceReset: calls after a reset of the device are not
+// supported.
 #include <mutex>
 
 #include "edt_internal.cuh"
@@ -23,14 +26,21 @@ namespace pmg {
 // 16 Mi float32 = 64 MiB: volumes of up to 16,777,216 voxels (e.g. 256^3).
 constexpr long long kNoAllocMaxVoxels = 16LL * 1024 * 1024;
 
+// 1 Mi int32 = 4 MiB of per-line flags; an envelope pass with more lines
+// runs in blocks of rows that fit (one row is at most PMG_MAX_LINE lines).
+constexpr long long kNoAllocMaxFlagLines = 1LL << 20;
+static_assert(kNoAllocMaxFlagLines >= PMG_MAX_LINE, "a row of lines must fit the flag array");
+
 static __device__ __align__(256) float g_edt_noalloc_scratch[kNoAllocMaxVoxels];
+static __device__ __align__(256) int g_edt_noalloc_flags[kNoAllocMaxFlagLines];
 
 static std::mutex g_noalloc_mu;
 static float *g_noalloc_ptr[64] = {nullptr};
+static int *g_noalloc_flags[64] = {nullptr};
 
-// Address of this device's scratch array (resolved once per device, with the
-// device current).
-static int noalloc_scratch(float **out)
+// Addresses of this device's scratch arrays (resolved once per device, with
+// the device current).
+static int noalloc_scratch(float **out, int **flags)
 {
     int dev = 0;
     PMG_CUDA(cudaGetDevice(&dev));
@@ -46,9 +56,17 @@ static int noalloc_scratch(float **out)
             set_error("pmg_edt3d_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return PMG_ECUDA;
         }
+        void *q = nullptr;
+        const cudaError_t e2 = cudaGetSymbolAddress(&q, g_edt_noalloc_flags);
+        if (e2 != cudaSuccess || !q) {
+            set_error("pmg_edt3d_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e2));
+            return PMG_ECUDA;
+        }
         g_noalloc_ptr[dev] = (float *)p;
+        g_noalloc_flags[dev] = (int *)q;
     }
     *out = g_noalloc_ptr[dev];
+    *flags = g_noalloc_flags[dev];
     return PMG_OK;
 }
 
@@ -82,8 +100,8 @@ extern "C" int pmg_edt3d_noalloc(const uint8_t *img, float *out, const int64_t s
                   n, kNoAllocMaxVoxels);
         return PMG_ERANGE;
     }
-    if (num_hull < 0 || num_hull > 7) {
-        set_error("pmg_edt3d_noalloc: num_hull %d outside [0, 7]", num_hull);
+    if (num_hull < 0 || num_hull + 1 > kMaxHull) {
+        set_error("pmg_edt3d_noalloc: num_hull %d outside [0, %d]", num_hull, kMaxHull - 1);
         return PMG_ERANGE;
     }
     if (form != PMG_EDT_SQUARED && form != PMG_EDT_DIST) {
@@ -91,8 +109,11 @@ extern "C" int pmg_edt3d_noalloc(const uint8_t *img, float *out, const int64_t s
         return PMG_EINVAL;
     }
     float *tmp = nullptr;
-    PMG_TRY(noalloc_scratch(&tmp));
+    int *flags = nullptr;
+    PMG_TRY(noalloc_scratch(&tmp, &flags));
     // every scratch element read by the second envelope pass is written by the
-    // first one, so nothing left by an earlier call needs clearing
-    return edt3d_run(img, out, tmp, shape, res, cfg, num_hull, form, as_stream(stream));
+    // first one, and the envelope clears the flags of each block of lines
+    // before it uses them, so nothing left by an earlier call leaks through
+    return edt3d_run(img, out, tmp, shape, res, cfg, num_hull, form, as_stream(stream), flags,
+                     kNoAllocMaxFlagLines);
 }

@@ -34,8 +34,8 @@ void set_error(const char *fmt, ...);
             return s__;                                                       \
     } while (0)
 
-// Stream-ordered scratch from the device's default memory pool (kept
-// resident between calls by raising the pool's release threshold once).
+// Stream-ordered scratch from a memory pool the library owns on each device
+// (unlimited release threshold, so it stays resident between calls).
 int scratch_alloc(void **p, size_t bytes, cudaStream_t st);
 int scratch_free(void *p, cudaStream_t st);
 

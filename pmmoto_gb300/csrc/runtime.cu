@@ -21,35 +21,48 @@ void set_error(const char *fmt, ...)
     va_end(ap);
 }
 
-// The first scratch request on a device raises the release threshold of its
-// default memory pool, so freed scratch stays mapped and later requests of
-// the same size are served without new allocations.
+// Scratch comes from a memory pool the library creates on each device (the
+// device's default pool, which other code in the process may use, is left
+// as it is).  Its release threshold is unlimited, so freed scratch stays
+// mapped and later requests of the same size are served without new
+// allocations from the driver.
 static std::mutex g_pool_mu;
-static bool g_pool_ready[64] = {false};
+static cudaMemPool_t g_pool[64] = {nullptr};
+static std::atomic<long long> g_scratch_allocs{0};
 
-static int ensure_pool()
+static int library_pool(cudaMemPool_t *out)
 {
     int dev = 0;
     PMG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64)
-        return PMG_OK;
+    if (dev < 0 || dev >= 64) {
+        set_error("scratch: device index %d outside the supported range", dev);
+        return PMG_ERANGE;
+    }
     std::lock_guard<std::mutex> lk(g_pool_mu);
-    if (g_pool_ready[dev])
-        return PMG_OK;
-    cudaMemPool_t pool;
-    PMG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
-    uint64_t thr = UINT64_MAX;
-    PMG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-    g_pool_ready[dev] = true;
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        PMG_CUDA(cudaMemPoolCreate(&pool, &props));
+        uint64_t thr = UINT64_MAX;
+        PMG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        g_pool[dev] = pool;
+    }
+    *out = g_pool[dev];
     return PMG_OK;
 }
 
 int scratch_alloc(void **p, size_t bytes, cudaStream_t st)
 {
-    PMG_TRY(ensure_pool());
+    cudaMemPool_t pool = nullptr;
+    PMG_TRY(library_pool(&pool));
     if (bytes == 0)
         bytes = 256;
-    PMG_CUDA(cudaMallocAsync(p, bytes, st));
+    g_scratch_allocs.fetch_add(1);
+    PMG_CUDA(cudaMallocFromPoolAsync(p, bytes, pool, st));
     return PMG_OK;
 }
 
@@ -161,6 +174,8 @@ static void prof_resolve()
 } // namespace pmg
 
 extern "C" long long pmg_launch_count(void) { return pmg::g_launches.load(); }
+
+extern "C" long long pmg_scratch_alloc_count(void) { return pmg::g_scratch_allocs.load(); }
 
 extern "C" int pmg_prof_enable(int32_t on)
 {
