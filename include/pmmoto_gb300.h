@@ -81,13 +81,15 @@ int pmg_edt3d(const uint8_t *img, float *out, const int64_t shape[3],
  * memory -- a host framework that owns all device memory through its own
  * pool or budget, or a latency-critical loop where a pool allocation could
  * block or fail mid-run.  Same arguments and results as pmg_edt3d; the
- * intermediate volume lives in a fixed 64 MiB array reserved by the library
- * on every device that loads it (held until the process exits), so volumes
- * are limited to 16,777,216 voxels (256^3); larger ones return PMG_ERANGE
- * with a message.  The first call on a device looks up that device's array
- * address, so make the first call before any stream capture.  All calls
- * share the one array: calls that overlap on the GPU (concurrent streams,
- * threads) race and must be serialized by the caller.
+ * intermediate volume lives in a fixed 64 MiB array and the per-line flags
+ * of the envelope passes in a fixed 4 MiB array, both reserved by the
+ * library on every device that loads it (held until the process exits), so
+ * volumes are limited to 16,777,216 voxels (256^3); larger ones return
+ * PMG_ERANGE with a message.  The first call on a device looks up that
+ * device's array addresses, so make the first call before any stream
+ * capture; calls after a cudaDeviceReset of that device are not supported.
+ * All calls share the arrays: calls that overlap on the GPU (concurrent
+ * streams, threads) race and must be serialized by the caller.
  */
 int pmg_edt3d_noalloc(const uint8_t *img, float *out, const int64_t shape[3],
                       const float res[3], const pmg_axis_cfg cfg[3], int32_t num_hull,
@@ -256,6 +258,15 @@ int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape
 long long pmg_launch_count(void);
 
 /*
+ * Number of scratch allocations this library has requested in the process
+ * (stream-ordered, from a memory pool the library owns on each device; the
+ * device's default pool is not touched).  A diagnostic with no counterpart
+ * in the reference: it lets a caller check that an entry point allocated
+ * nothing.
+ */
+long long pmg_scratch_alloc_count(void);
+
+/*
  * Per-kernel timing: when enabled, every launch records a CUDA event pair on
  * its stream with the launch's algorithmic bytes.  pmg_prof_read resolves
  * them (synchronizing on the events) into per-kernel totals: `names` gets
@@ -266,6 +277,18 @@ int pmg_prof_enable(int32_t on);
 int pmg_prof_reset(void);
 int pmg_prof_read(char *names, size_t names_len, double *ms, double *bytes,
                   long long *launches, int32_t cap, int32_t *count);
+
+/*
+ * Testing aid with no counterpart in the reference: every data-dependent
+ * device loop of the union-find (root searches, union retries) is bounded by
+ * the longest chain a valid parent array allows and returns PMG_EITER, with
+ * the CUDA context intact, when a loop runs past it.  This call lowers all
+ * those bounds to `cap` iterations (cap <= 0 restores the defaults) on the
+ * current device, so that a test can make a bound run out on an ordinary
+ * input.  Not for production use: results of calls that return PMG_EITER
+ * are undefined.
+ */
+int pmg_set_iteration_cap(int32_t cap);
 
 /* Message of the last failure on this host thread (empty if none). */
 int pmg_last_error(char *buf, size_t len);

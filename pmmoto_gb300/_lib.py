@@ -55,6 +55,7 @@ def _declare(L):
         "pmg_drainage": [P, P, P, P, P, P, P, P, P, P, i32, P, P, P, P, P, P, P],
         "pmg_drainage_ext": [P, P, P, P, P, P, P, P, P, P, i32, P, P, P, P, P, P, P, P, P],
         "pmg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
+        "pmg_set_iteration_cap": [i32],
     }
     for name, args in sig.items():
         if hasattr(L, name):
@@ -62,7 +63,8 @@ def _declare(L):
             fn.argtypes = args
             fn.restype = ctypes.c_int
     L.pmg_version.restype = ctypes.c_char_p
-    _ = i64
+    L.pmg_launch_count.restype = ctypes.c_longlong
+    L.pmg_scratch_alloc_count.restype = ctypes.c_longlong
 
 
 def lib():

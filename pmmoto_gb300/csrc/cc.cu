@@ -3081,3 +3081,12 @@ extern "C" int pmg_cc_select(const uint8_t *img, void *out, int32_t out_bytes,
     PMG_TRY(scratch_free(err, st));
     return s;
 }
+
+// Testing aid: lower every union-find iteration cap (c_uf_cap) to `cap`
+// (<= 0 restores the default bounds).
+extern "C" int pmg_set_iteration_cap(int32_t cap)
+{
+    const int v = cap > 0 ? cap : INT_MAX;
+    PMG_CUDA(cudaMemcpyToSymbol(c_uf_cap, &v, sizeof(int)));
+    return PMG_OK;
+}

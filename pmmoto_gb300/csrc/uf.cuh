@@ -3,30 +3,50 @@
 // Parents live in an int32 array; a root points to itself; unions link the
 // larger root under the smaller with atomicMin (Playne and Hawick's
 // lock-free scheme), so every component's root is its smallest index.  All
-// searches and unions stop after a fixed number of steps and record an error
-// code instead of spinning.
+// searches and unions stop after a bounded number of steps and record an
+// error code instead of spinning.
 #pragma once
+
+#include <climits>
 
 #include "pmg_common.cuh"
 
 namespace pmg {
 
-constexpr int kFindCap = 1 << 24;
-constexpr int kUniteCap = 1 << 20;
+// Iteration caps.  Parents always point to smaller indices, so a root
+// search from x legitimately takes at most x steps, and every retry of a
+// union lowers the larger of its two roots, so a union retries at most
+// max(a, b) + 1 times: the caps below are those bounds (a loop that exceeds
+// one has met a corrupted parent array, e.g. a cycle).  A loop also gives up
+// as soon as another thread has recorded an error (checked every
+// kErrPoll steps).  c_uf_cap (constant memory, default INT_MAX) lowers every
+// cap further -- a testing aid (pmg_set_iteration_cap) that makes the caps
+// run out on ordinary inputs.
+// (Defined here: only cc.cu includes this header, so there is one copy.)
+static __constant__ int c_uf_cap = INT_MAX;
+constexpr int kErrPoll = 256;
 
 __device__ __forceinline__ int ld(const int *p) { return __ldcg(p); }
 
+__device__ __forceinline__ bool uf_gave_up(int it, const int *err)
+{
+    return (it & (kErrPoll - 1)) == 0 && *(volatile const int *)err != 0;
+}
+
 __device__ __forceinline__ int find_root(const int *P, int x, int *err)
 {
+    const int cap = min(x + 1, c_uf_cap);
     int p = ld(P + x);
     int it = 0;
     while (p != x) {
         x = p;
         p = ld(P + x);
-        if (++it > kFindCap) {
+        if (++it > cap) {
             atomicExch(err, 1);
             break;
         }
+        if (uf_gave_up(it, err))
+            break;
     }
     return x;
 }
@@ -38,6 +58,7 @@ __device__ __forceinline__ int find_root(const int *P, int x, int *err)
 // harmless because that union retries with the value the atomic returned.
 __device__ __forceinline__ int find_root_halve(int *P, int x, int *err)
 {
+    const int cap = min(x + 1, c_uf_cap);
     int p = ld(P + x);
     int it = 0;
     while (p != x) {
@@ -47,10 +68,12 @@ __device__ __forceinline__ int find_root_halve(int *P, int x, int *err)
         P[x] = g;
         x = g;
         p = ld(P + x);
-        if (++it > kFindCap) {
+        if (++it > cap) {
             atomicExch(err, 1);
             break;
         }
+        if (uf_gave_up(it, err))
+            break;
     }
     return x;
 }
@@ -58,7 +81,8 @@ __device__ __forceinline__ int find_root_halve(int *P, int x, int *err)
 // Playne-Hawick union (atomicMin links the larger root under the smaller).
 __device__ __forceinline__ void unite(int *P, int a, int b, int *err)
 {
-    for (int it = 0; it < kUniteCap; it++) {
+    const int cap = min(max(a, b) + 1, c_uf_cap);
+    for (int it = 0; it < cap; it++) {
         a = find_root_halve(P, a, err);
         b = find_root_halve(P, b, err);
         if (a == b)
