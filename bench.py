@@ -12,8 +12,11 @@ drainage(..., mode="distance") with the standard method.  Inputs are
 synthetic (seeded), the image stays resident in HBM for `value`; `e2e` feeds
 host buffers through the package's C ABI each step.
 
-Prints one JSON line.  `--impl reference` times the CPU restatement of the
-same path (the oracle, all host threads) on a bounded sample.
+Prints one JSON line, which also carries the large EDT + connected-components
+configuration (1024^3 periodic Gaussian-random-field medium: Gvox/s and the
+HBM roofline fraction of each operator).  `--impl reference` times the CPU
+restatement of the same path (the oracle, all host threads) over whole
+curves in sweep order.
 """
 
 from __future__ import annotations
@@ -241,11 +244,13 @@ def run_gpu(args):
     def e2e_step():
         dev_pm.copy_(host_pm, non_blocking=True)
         dev_mp.copy_(host_mp, non_blocking=True)
+        # a new medium each step: its porosity and maximum distance (one EDT)
+        # are computed here, as drainage needs them
         pm_e = P.domain_generation.PorousMedia(sd, dev_pm)
-        pm_e._porosity, pm_e._max_distance = phi, pm.max_distance
         mp_e = P.domain_generation.Multiphase(pm_e, dev_mp, 2)
         c, _ = ED.drainage_counts(mp_e, radii, mode="distance")
-        return [float(x / np.prod(sd.domain.voxels)) / phi for x in c]  # counts came back to the host
+        phi_e = pm_e.porosity
+        return [float(x / np.prod(sd.domain.voxels)) / phi_e for x in c]  # counts came back to the host
 
     e2e_step()
     torch.cuda.synchronize()
@@ -292,6 +297,8 @@ def run_gpu(args):
         "porosity": phi,
         "setup_s": round(setup_s, 3),
     }
+    if not args.no_large:
+        out["edt_cc_1024"] = measure_large(args, local, peak, peak_kind)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(sd_voxels=sd.voxels, pm_img=pm_t.img.cpu().numpy(), pcs=pcs)
     print(json.dumps(out), flush=True)
@@ -313,10 +320,15 @@ def load_traffic(kernel):
 # CPU baseline (the oracle: CPU restatement of the reference, all host threads)
 # ---------------------------------------------------------------------------
 
-SAMPLE_IDX = (20,)
+SAMPLE_IDX = (0, 10, 20, 30)
 
 
 def cpu_baseline(sd_voxels=None, pm_img=None, pcs=None):
+    """The oracle (OpenMP C restatement of the reference) on a stratified
+    sample of the curve: radii #0, #10, #20, #30 evaluated in sweep order with
+    the multiphase image carried from one to the next, plus the per-medium
+    porosity and maximum distance; the radii's time is scaled x10 to a
+    curve."""
     from oracle import oracle as O
 
     L = O.lib()
@@ -328,64 +340,139 @@ def cpu_baseline(sd_voxels=None, pm_img=None, pcs=None):
     if pcs is None:
         pcs, _ = radii_for(g.resolution[0])
     sample = [pcs[i] for i in SAMPLE_IDX]
-    dmax = O.max_distance(g, pm_img)  # once per medium in the reference (PorousMedia caches it)
     t0 = time.perf_counter()
-    O.drainage(g, pm_img, sample, dmax=dmax)
-    dt = time.perf_counter() - t0
-    per_curve = dt * N_RADII / len(sample)
+    dmax = O.max_distance(g, pm_img)  # once per medium (PorousMedia caches it)
+    phi = O.porosity(g, pm_img)
+    t1 = time.perf_counter()
+    O.drainage(g, pm_img, sample, dmax=dmax, phi=phi)
+    t2 = time.perf_counter()
+    scale = N_RADII / len(sample)
+    per_curve = (t1 - t0) + (t2 - t1) * scale
     return {"value": 1.0 / per_curve, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{len(sample)} of {N_RADII} radii (capillary pressures #{SAMPLE_IDX}) of the same 512^3 "
-                      f"drainage, {dt:.1f} s, scaled x{N_RADII / len(sample):g} to one curve"}
+            "sample": f"radii #{list(SAMPLE_IDX)} of the 40 (sweep order, multiphase state carried between "
+                      f"them) of the same 512^3 drainage, {t2 - t1:.1f} s scaled x{scale:g}, plus the "
+                      f"medium's porosity and max distance ({t1 - t0:.1f} s, once per curve)"}
 
 
 def run_reference(args):
+    """Reference arm: the CPU path (the oracle port, all host threads) times
+    whole curves of the same workload in sweep order with carried state.  The
+    K timed steps split ceil(K / 40) curves into K runs of consecutive radii,
+    each step continuing from the multiphase image the previous one left; the
+    first step of every curve also computes the medium's porosity and maximum
+    distance.  Nothing is extrapolated: value = curves / total time."""
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return
     from oracle import oracle as O
 
+    L = O.lib()
+    L.or_num_threads.restype = ctypes.c_int
+    cores = int(L.or_num_threads())
     g = O.Geom((N_VOX,) * 3, **geom_kwargs())
     pm_img = O.gen_pm_spheres_domain(g, make_pack(1234))
     pcs, _ = radii_for(g.resolution[0])
+    n_curves = max(1, -(-args.steps // N_RADII))
+    seq = [(c, k) for c in range(n_curves) for k in range(N_RADII)]
+    bounds = np.linspace(0, len(seq), args.steps + 1).round().astype(int)
+    # the CPU path has nothing to warm up; one porosity count touches the image
     for _ in range(min(args.warmup, 1)):
-        pass  # the CPU path has nothing to warm up beyond its first call
-    vals = []
-    cb = None
-    for _ in range(args.steps):
-        cb = cpu_baseline(pm_img=pm_img, pcs=pcs)
-        vals.append(1.0 / cb["value"])
-    v = len(vals) / sum(vals)
-    cb["value"] = v
+        O.porosity(g, pm_img)
+    step_s = []
+    mp, dmax, phi, sat = None, None, None, []
+    t_all = time.perf_counter()
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        part = seq[bounds[i]:bounds[i + 1]]
+        for c, k in part:
+            if k == 0:
+                mp = None
+                dmax = O.max_distance(g, pm_img)
+                phi = O.porosity(g, pm_img)
+                sat = []
+            s_k, mp = O.drainage(g, pm_img, [pcs[k]], dmax=dmax, mp_img=mp, phi=phi)
+            sat.append(float(s_k[0]))
+        step_s.append(time.perf_counter() - t0)
+    total = time.perf_counter() - t_all
+    v = n_curves / total
+    cb = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+          "sample": f"{n_curves} whole 40-radius curve(s) of the 512^3 drainage in sweep order with carried "
+                    f"state, split over the {args.steps} timed steps ({total:.1f} s)"}
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
-           "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": dict(workload_config(), parallelism="single GPU" if world == 1 else f"replicas x{world}"),
+           "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "saturation_first_last": [sat[0], sat[-1]] if sat else None,
+           "step_s_min_max": [min(step_s), max(step_s)]}
     print(json.dumps(out), flush=True)
 
 
-def grf_medium(n, sigma=4.0, porosity=0.35, seed=7):
-    """Gaussian random field medium of the large EDT + CC configuration: seeded
-    white noise N(0, 1), filtered by a periodic Gaussian of sigma voxels in
-    Fourier space, pore (1) where the field is at or below its 35th
-    percentile; n^3 uint8 on the device."""
-    import math
-
+def measure_large(args, local, peak, peak_kind):
+    """Large EDT + connected-components configuration: the 1024^3 Gaussian
+    random field medium (sigma 4 voxels, porosity 0.35, periodic), its
+    periodic squared edt3d (own volume) and its connected components (labels
+    of the padded 1026^3 periodic subdomain image, seam merge and numbering
+    included), each timed over `steps` calls after `warmup` with CUDA events
+    and clocks sampled; Gvox/s per voxel of the operator's input, achieved
+    GB/s = algorithmic bytes (EDT 21 B, CC 17 B per voxel) / time."""
     import torch
 
-    g = torch.Generator(device="cuda")
-    g.manual_seed(seed)
-    field = torch.randn((n, n, n), device="cuda", generator=g)
-    F = torch.fft.rfftn(field)
-    del field
-    k = torch.fft.fftfreq(n, device="cuda")
-    kz = torch.fft.rfftfreq(n, device="cuda")
-    F *= torch.exp(-2.0 * math.pi ** 2 * sigma ** 2 * (k[:, None, None] ** 2 + k[None, :, None] ** 2))
-    F *= torch.exp(-2.0 * math.pi ** 2 * sigma ** 2 * kz[None, None, :] ** 2)
-    field = torch.fft.irfftn(F, s=(n, n, n))
-    del F
-    flat = field.reshape(-1)
-    q = torch.kthvalue(flat, max(1, int(round(porosity * flat.numel())))).values
-    return (field <= q).to(torch.uint8)
+    import pmmoto_gb300 as P
+    from pmmoto_gb300 import _lib
+    from pmmoto_gb300.core.geometry import geo_of
+    from pmmoto_gb300.domain_generation import grf
+    from pmmoto_gb300.filters import connected_components as CC
+    from pmmoto_gb300.filters import distance as D
+
+    n = 1024
+    own = grf.gen_grf_medium(n)
+    idx = torch.arange(-1, n + 1, device="cuda") % n
+    img = own[idx][:, idx][:, :, idx].contiguous()
+    torch.cuda.synchronize()
+    out = torch.empty(own.shape, dtype=torch.float32, device="cuda")
+    cfg = D.edt3d_cfg((True, True, True))
+    res = np.ones(3, np.float32)
+    sd = P.initialize((n,) * 3, boundary_types=(("periodic", "periodic"),) * 3)
+    geo = geo_of(sd)
+    L = _lib.lib()
+    ops = {"edt": (lambda: D.edt3d_device(own, res, cfg, True, out), own.numel(), 21.0),
+           "cc": (lambda: CC.connect_components_device(img, geo), img.numel(), 17.0)}
+    res_out = {"workload": "1024^3 GRF medium (sigma 4, porosity 0.35, periodic); edt3d squared on the own "
+                           "1024^3 volume, connected components on the padded 1026^3 image",
+               "l2": "inputs larger than L2 (1 GB image, 4 GB distances, 8.6 GB labels)"}
+    steps = max(3, min(args.steps, 10))
+    for name, (op, vox, bpv) in ops.items():
+        for _ in range(max(3, args.warmup)):
+            op()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = L.pmg_launch_count()
+        with Clocks(local) as clk:
+            e0.record()
+            for _ in range(steps):
+                op()
+            e1.record()
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        launches = (L.pmg_launch_count() - n0) // steps
+        L.pmg_prof_reset()
+        L.pmg_prof_enable(1)
+        op()
+        torch.cuda.synchronize()
+        L.pmg_prof_enable(0)
+        prof = prof_read(L)
+        ach = bpv * vox / (ms / 1e3) / 1e9
+        res_out[name] = {"ms": round(ms, 3), "gvox_s": round(vox / ms / 1e6, 2), "voxels": vox,
+                         "bytes_per_voxel": bpv, "achieved_GBps": round(ach, 1), "peak": peak,
+                         "peak_kind": peak_kind, "frac": round(ach / peak, 4), "launches_per_call": launches,
+                         "clocks": clk.summary(), "steps": steps,
+                         "kernels": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                                         "GBps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] else None}
+                                     for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}}
+    del own, img, out
+    torch.cuda.empty_cache()
+    return res_out
 
 
 def batch_packs(count, seed=99):
@@ -482,7 +569,9 @@ def run_case(args):
 
     n = args.n
     if args.medium == "grf":
-        img = grf_medium(n)
+        from pmmoto_gb300.domain_generation import grf
+
+        img = grf.gen_grf_medium(n)
     else:
         g = torch.Generator(device="cuda")
         g.manual_seed(7)
@@ -545,6 +634,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-large", action="store_true", help="skip the 1024^3 EDT + CC measurement")
     ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph", "select", "batch"])
     ap.add_argument("--packs", type=int, default=256, help="packs of the batched case")
     ap.add_argument("--workers", type=int, default=8, help="host threads / CUDA streams of the batched case")

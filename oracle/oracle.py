@@ -636,17 +636,20 @@ def max_distance(geom: Geom, pm_img):
 
 
 def drainage(geom: Geom, pm_img, capillary_pressures, gamma=1, mode="distance", dmax=None, contact_angle=0,
-             method="standard"):
+             method="standard", mp_img=None, phi=None):
     """drainage with _standard_method, _contact_angle_method or
-    _extended_contact_angle_method (equilibrium_distribution.py:25-289).
+    _extended_contact_angle_method (equilibrium_distribution.py:25-289),
+    starting from mp_img (default: gen_mp_constant(pm, 2)).
 
     Returns (saturations, final multiphase image)."""
     if isinstance(capillary_pressures, (int, float)):
         capillary_pressures = [capillary_pressures]
     elif isinstance(capillary_pressures, list):
         capillary_pressures = sorted(capillary_pressures)
-    mp_img = np.where(pm_img == 1, 2, 0).astype(np.uint8)
-    phi = porosity(geom, pm_img)
+    if mp_img is None:
+        mp_img = np.where(pm_img == 1, 2, 0).astype(np.uint8)
+    if phi is None:
+        phi = porosity(geom, pm_img)
     sat = np.zeros(len(capillary_pressures))
     theta = contact_angle if method != "standard" else 0
     for n, pc in enumerate(capillary_pressures):

@@ -31,15 +31,24 @@ def _radius(pc, gamma, contact_angle):
     return 2.0 * gamma / pc * np.cos(np.deg2rad(contact_angle))
 
 
-def drainage_counts(multiphase, radii, mode="distance", radii_dilate=None):
+def _inactive(multiphase, r, rd):
+    """The reference's empty-morph rule (equilibrium_distribution.py:158-166,
+    :206-214, :262-270): a radius below the finest resolution or above the
+    medium's largest distance."""
+    return min(r, rd) < min(multiphase.subdomain.domain.resolution) or max(r, rd) > \
+        multiphase.porous_media.max_distance
+
+
+def drainage_counts(multiphase, radii, mode="distance", radii_dilate=None, start=None):
     """Run the drainage sweep for the given probe radii on the device; returns
     (per-radius own-region phase-2 counts, final multiphase CUDA tensor).
     radii_dilate: dilation radii when they differ from the erosion radii
-    (extended contact-angle method)."""
+    (extended contact-angle method); start: the multiphase image to start
+    from (default multiphase.img)."""
     sd = multiphase.subdomain
     g = geo_of(sd)
     pm, _ = morph.to_u8(multiphase.porous_media.img)
-    mp, _ = morph.to_u8(multiphase.img)
+    mp, _ = morph.to_u8(multiphase.img if start is None else start)
     mp = mp.clone()
     n = len(radii)
     if radii_dilate is None:
@@ -51,11 +60,10 @@ def drainage_counts(multiphase, radii, mode="distance", radii_dilate=None):
     rad_d = np.zeros(max(n, 1), dtype=np.float64)
     be = np.full(max(n, 1), -1.0)
     bd = np.full(max(n, 1), -1.0)
-    min_res = min(sd.domain.resolution)
     for k, (r, rd) in enumerate(zip(radii, radii_dilate)):
         rad[k] = float(r)
         rad_d[k] = float(rd)
-        if min(r, rd) < min_res or max(r, rd) > multiphase.porous_media.max_distance:
+        if _inactive(multiphase, r, rd):
             continue
         morph.check_radii(sd, [r, rd])
         active[k] = 1
@@ -81,6 +89,32 @@ def drainage_counts(multiphase, radii, mode="distance", radii_dilate=None):
     return counts[:n], mp
 
 
+def _drainage_saving(multiphase, capillary_pressures, radii, radii_d, mode, out_folder):
+    """drainage(save=True) (equilibrium_distribution.py:93-121): the sweep one
+    pressure at a time, writing after each update the multiphase image with
+    that pressure's morph image to
+    <out_folder>/capillary_pressure_<pc with 3 decimals, '.' -> '_'>.vti."""
+    from ..io.output import save_img
+    from .porosimetry import porosimetry_device
+
+    g = geo_of(multiphase.subdomain)
+    pm, _ = morph.to_u8(multiphase.porous_media.img)
+    mp, _ = morph.to_u8(multiphase.img)
+    counts = np.zeros(len(radii), dtype=np.int64)
+    for k, pc in enumerate(capillary_pressures):
+        r = radii[k]
+        rd = r if radii_d is None else radii_d[k]
+        if _inactive(multiphase, r, rd):
+            m = torch.zeros_like(pm)
+        else:
+            m = porosimetry_device(g, pm, r, rd, True, mp, mode)
+        c, mp = drainage_counts(multiphase, [r], mode, None if radii_d is None else [rd], start=mp)
+        counts[k] = c[0]
+        file_out = out_folder + (f"/capillary_pressure_{pc:.3f}".replace(".", "_"))
+        save_img(file_out, multiphase.subdomain, mp, additional_img={"morph": m})
+    return counts, mp
+
+
 def drainage(multiphase, capillary_pressures, gamma=1, contact_angle=0, method="standard", mode="hybrid",
              save=False, out_folder="drainage_out"):
     """Wetting-phase saturation at each capillary pressure
@@ -103,15 +137,16 @@ def drainage(multiphase, capillary_pressures, gamma=1, contact_angle=0, method="
         raise ValueError(f"{method} is not implemented. ")
     if mode not in MODES:
         raise ValueError(f"mode {mode} must be one of {MODES}")
-    if save:
-        raise NotImplementedError("saving VTK images is not part of the GPU build")
     # probe radii as Multiphase.get_probe_radius forms them (float64); the
     # extended method (Schulz and Wargo, :230-289) dilates by r |cos(theta)|
     radii = [_radius(pc, gamma, contact_angle) for pc in capillary_pressures]
     radii_d = None
     if method == "extended_contact_angle":
         radii_d = [r * np.abs(np.cos(np.deg2rad(contact_angle))) for r in radii]
-    counts, mp = drainage_counts(multiphase, radii, mode, radii_d)
+    if save:
+        counts, mp = _drainage_saving(multiphase, capillary_pressures, radii, radii_d, mode, out_folder)
+    else:
+        counts, mp = drainage_counts(multiphase, radii, mode, radii_d)
     total = np.prod(multiphase.subdomain.domain.voxels)
     phi = multiphase.porous_media.porosity
     sat = np.zeros(len(capillary_pressures))
