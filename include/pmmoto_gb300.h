@@ -254,6 +254,49 @@ int pmg_drainage_ext(const uint8_t *pm_img, uint8_t *mp_img, const int64_t shape
                      const double *ball_erode, const double *ball_dilate, int64_t *counts,
                      const double *radii_dilate, const int32_t *ratios_dilate, void *stream);
 
+/*
+ * Learned radius schedule: kernels of the 3-D CNN that predicts a drainage
+ * curve (no counterpart in the reference, whose drainage loop,
+ * filters/equilibrium_distribution.py:93-128, evaluates every radius).
+ * Activations are bf16, channels last ([batch][z][y][x][c]); convolutions
+ * are 3x3x3 with stride 2 and padding 1 from a cubic side di to
+ * (di + 1) / 2, computed on the tensor cores (tcgen05, fp32 accumulate);
+ * c_in is 1, 16, 32 or 64 and c_out 16, 32 or 64.  Weights are fp32
+ * [c_out][c_in][27] (tap = (kz * 3 + ky) * 3 + kx); pmg_cnn_pack_weights
+ * writes their bf16 operands: wk [c_out][kp], kp = 27 c_in rounded up to 64,
+ * and (c_in >= 16) wkt [c_in][kpt], kpt = 27 c_out rounded up to 64.
+ * err: a device int that a pipeline wait which runs out of time sets (read
+ * by pmg_cnn_check, which returns PMG_EITER then).
+ */
+int pmg_cnn_pack_weights(const float *w, int32_t cin, int32_t cout, void *wk, void *wkt, void *stream);
+/* y = ReLU(conv(x, w) + bias), bf16. */
+int pmg_cnn_conv_fwd(const void *x, const void *wk, const float *bias, void *y, int32_t batch, int32_t di,
+                     int32_t cin, int32_t cout, int32_t *err, void *stream);
+/* dx = conv_transpose(dz, w) masked where xact (the layer input, a ReLU
+   output) is 0: the gradient of the lower layer's pre-activation, bf16. */
+int pmg_cnn_conv_dgrad(const void *dz, const void *wkt, const void *xact, void *dx, int32_t batch, int32_t di,
+                       int32_t cin, int32_t cout, int32_t *err, void *stream);
+/* grad [c_out][c_in][27] and dbias [c_out] (fp32) of the loss given dz;
+   dw is fp32 scratch of 27 c_in c_out values. */
+int pmg_cnn_conv_wgrad(const void *x, const void *dz, float *dw, float *grad, float *dbias, int32_t batch,
+                       int32_t di, int32_t cin, int32_t cout, int32_t *err, void *stream);
+/* Head on y4 [batch][64][64]: average pool, MLP 64-64 (ReLU) -64, sigmoid ->
+   pred [batch][64].  params: w5 [64][64], b5, w6 [64][64], b6 (fp32).  With a
+   target: *loss += mean squared error, grads (same layout) += gradients,
+   dy4 = gradient of y4's pre-activation. */
+int pmg_cnn_head(const void *y4, const float *params, int32_t batch, const float *target, float *pred,
+                 float *loss, float *grads, void *dy4, void *stream);
+/* One bias-corrected Adam step (step >= 1) over n fp32 parameters. */
+int pmg_cnn_adam(float *w, const float *g, float *m, float *v, int64_t n, double lr, double b1, double b2,
+                 double eps, int64_t step, double weight_decay, void *stream);
+/* Network input: the float32 distance field's box {lo0,hi0,lo1,hi1,lo2,hi2}
+   (at least 64 voxels per axis) averaged over 64^3 cells, divided by scale,
+   as bf16 [64][64][64]. */
+int pmg_cnn_downsample(const float *dist, const int64_t shape[3], const int64_t box[6], double scale, void *out,
+                       void *stream);
+/* PMG_EITER (and a message) if a kernel above recorded a timed-out wait. */
+int pmg_cnn_check(int32_t *err, void *stream);
+
 /* Number of kernels this library has launched in the process. */
 long long pmg_launch_count(void);
 
