@@ -299,6 +299,8 @@ def run_gpu(args):
     }
     if not args.no_large:
         out["edt_cc_1024"] = measure_large(args, local, peak, peak_kind)
+    if not args.no_learned:
+        out["learned_schedule"] = measure_learned(args)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(sd_voxels=sd.voxels, pm_img=pm_t.img.cpu().numpy(), pcs=pcs)
     print(json.dumps(out), flush=True)
@@ -406,6 +408,29 @@ def run_reference(args):
            "saturation_first_last": [sat[0], sat[-1]] if sat else None,
            "step_s_min_max": [min(step_s), max(step_s)]}
     print(json.dumps(out), flush=True)
+
+
+def measure_learned(args):
+    """Learned radius schedule against the dense exact sweep: held-out 512^3
+    sphere packs of this configuration's generator (seeds the timed curve does
+    not use), 64 radii r_max (k + 1) / 64; per pack the dense curve (64 exact
+    radii) and the learned curve (schedule network + at most 12 exact radii,
+    dense fallback on a failed residual check) are each timed from the pore
+    image on the device to the curve on the host, the medium's distance
+    transform included; curves/s over the packs and the largest |dS| of the
+    learned curve against the dense one."""
+    import os
+
+    from pmmoto_gb300.learned import evaluate, schedule
+
+    if not os.path.exists(schedule.default_weights_path()):
+        return {"status": "no trained weights in the package"}
+    sched = schedule.LearnedSchedule(schedule.load_default())
+    res = evaluate.run(packs=args.learned_packs, grfs=0, seed0=7000, sched=sched)["sphere512"]["summary"]
+    res["workload"] = (f"{args.learned_packs} held-out 512^3 packs (3000 spheres r~U[0.02,0.05], walls y/z, inlet x-, "
+                       "outlet x+), 64 radii r_max (k+1)/64; learned <= 12 exact radii + dense fallback")
+    res["target"] = {"max_abs_dS": 0.01, "speedup": 5.0}
+    return res
 
 
 def measure_large(args, local, peak, peak_kind):
@@ -635,6 +660,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-large", action="store_true", help="skip the 1024^3 EDT + CC measurement")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule measurement")
+    ap.add_argument("--learned-packs", type=int, default=6, help="held-out packs of the learned-schedule leg")
     ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph", "select", "batch"])
     ap.add_argument("--packs", type=int, default=256, help="packs of the batched case")
     ap.add_argument("--workers", type=int, default=8, help="host threads / CUDA streams of the batched case")

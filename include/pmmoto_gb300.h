@@ -297,6 +297,18 @@ int pmg_cnn_downsample(const float *dist, const int64_t shape[3], const int64_t 
 /* PMG_EITER (and a message) if a kernel above recorded a timed-out wait. */
 int pmg_cnn_check(int32_t *err, void *stream);
 
+/*
+ * Workload generator (no counterpart in the reference): one periodic
+ * smoothing pass along `axis` of `batch` float64 volumes of `shape`
+ * (in != out) with the (order + 1) weights w (host array, order <= 256):
+ * out[i] = w_0 in[i - order/2] + ... + w_order in[i + order/2], summed in
+ * that order with each product and sum rounded once.  The Gaussian random
+ * field media of the large EDT + CC configuration and of the schedule
+ * network's training set apply it with the binomial weights C(order, k) / 2^order.
+ */
+int pmg_grf_smooth(const double *in, double *out, int64_t batch, const int64_t shape[3], int32_t axis,
+                   const double *weights, int32_t order, void *stream);
+
 /* Number of kernels this library has launched in the process. */
 long long pmg_launch_count(void);
 

@@ -56,6 +56,7 @@ def _declare(L):
         "pmg_drainage_ext": [P, P, P, P, P, P, P, P, P, P, i32, P, P, P, P, P, P, P, P, P],
         "pmg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
         "pmg_set_iteration_cap": [i32],
+        "pmg_grf_smooth": [P, P, i64, P, i32, P, i32, P],
     }
     for name, args in sig.items():
         if hasattr(L, name):
