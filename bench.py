@@ -577,6 +577,50 @@ def run_batch(args):
                       "gpu_launches_per_batch": launches, "final_saturation_sample": res[0][0]}), flush=True)
 
 
+def run_cnn(args):
+    """Schedule network on the tensor cores: one training step (forward,
+    backward, Adam) on a synthetic batch of `--batch` 64^3 inputs, timed with
+    CUDA events; per-kernel TFLOP/s = algorithmic flops (2 x MACs of each
+    convolution; dgrad counts the 1/8 of taps that a stride-2 transpose
+    touches) / CUDA-event time, against the measured dense bf16 peak."""
+    import torch
+
+    from pmmoto_gb300 import _lib
+    from pmmoto_gb300.learned import ScheduleNet
+
+    torch.manual_seed(0)
+    x = torch.rand((args.batch, 64 ** 3), device="cuda").to(torch.bfloat16)
+    y = torch.rand((args.batch, 64), device="cuda")
+    net = ScheduleNet(seed=0)
+    for _ in range(max(3, args.warmup)):
+        net.train_step(x, y)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        net.train_step(x, y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    L = _lib.lib()
+    L.pmg_prof_reset()
+    L.pmg_prof_enable(1)
+    for _ in range(args.steps):
+        net.train_step(x, y)
+    torch.cuda.synchronize()
+    L.pmg_prof_enable(0)
+    prof = prof_read(L)
+    net.check_status()
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    peak = json.load(open(p))["bf16_tflops"] if os.path.exists(p) else 1900.0
+    print(json.dumps({"case": "cnn", "batch": args.batch, "ms_per_train_step": ms,
+                      "samples_s": args.batch / (ms / 1e3), "bf16_peak_tflops": peak,
+                      "kernels": {k: {"ms_per_step": v["ms"] / args.steps, "launches": v["launches"],
+                                      "TFLOPs": v["bytes"] / (v["ms"] / 1e3) / 1e12 if v["ms"] else None,
+                                      "frac": v["bytes"] / (v["ms"] / 1e3) / 1e12 / peak if v["ms"] else None}
+                                  for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}}), flush=True)
+
+
 def run_case(args):
     """Single-operator cases on a seeded random medium (for ncu captures and
     per-operator rates): 'edt' = edt3d, 'cc' = connected components (with the
@@ -662,7 +706,9 @@ def main():
     ap.add_argument("--no-large", action="store_true", help="skip the 1024^3 EDT + CC measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule measurement")
     ap.add_argument("--learned-packs", type=int, default=6, help="held-out packs of the learned-schedule leg")
-    ap.add_argument("--case", default="drainage", choices=["drainage", "edt", "cc", "morph", "select", "batch"])
+    ap.add_argument("--case", default="drainage",
+                    choices=["drainage", "edt", "cc", "morph", "select", "batch", "cnn"])
+    ap.add_argument("--batch", type=int, default=64, help="samples per training step of the cnn case")
     ap.add_argument("--packs", type=int, default=256, help="packs of the batched case")
     ap.add_argument("--workers", type=int, default=8, help="host threads / CUDA streams of the batched case")
     ap.add_argument("--n", type=int, default=512, help="volume side of the single-operator cases")
@@ -674,6 +720,8 @@ def main():
     args = ap.parse_args()
     if args.case == "batch":
         run_batch(args)
+    elif args.case == "cnn":
+        run_cnn(args)
     elif args.case != "drainage":
         run_case(args)
     elif args.impl == "reference":

@@ -663,6 +663,275 @@ __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ 
     }
 }
 
+// The per-voxel scan as an out-of-line call (the rare slow path of the
+// line-pair kernels: inlining it at every unrolled position would bloat the
+// ring loop).
+__device__ __noinline__ bool window_voxel_call(const float *line, long long st, int n, int x, float inv_a, float kmax,
+                                               int periodic, float *best, int *need)
+{
+    float b = 0.0f;
+    int nd = 0;
+    const bool ok = window_voxel(line, st, n, x, inv_a, kmax, periodic, b, nd);
+    *best = b;
+    *need = nd;
+    return ok;
+}
+
+// Strided lines, two at a time (adjacent along the contiguous axis, packed
+// as the halves of 32-bit words of integer heights K = f / res^2): the exact
+// minimum of K(x + d) + d^2 over |d| <= W by packed add-min, walking each
+// line segment with a register ring of 2W + 1 words.  A minimum m <= (W+1)^2
+// is final (every position beyond the window adds at least (W+1)^2); a
+// larger one, a window holding a height that is not an integer below 2^16
+// (clamped, so no sum wraps) or a periodic line end within reach ((x+1)^2 or
+// (n-x)^2 <= m: the per-voxel scan would run off the line there) falls back
+// to window_voxel for that voxel, which sets the same line flags as
+// k_env_window.  Outputs are those of k_env_window, with far fewer
+// divergent loops.
+template <int W>
+__global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
+                                                  float a, float inv_a, int periodic, int form, int *__restrict__ flag,
+                                                  int seglen)
+{
+    constexpr int R = 2 * W + 1;
+    constexpr unsigned kClamp = 65535u - (unsigned)(W * W) - 1u;
+    constexpr unsigned kFinal = (unsigned)((W + 1) * (W + 1));
+    const long long nlines = Ls.count();
+    const long long npairs = nlines >> 1;
+    const LineGeo g0 = line_addr(Ls, 0);
+    const int n = g0.n;
+    const long long st = g0.stride;
+    const int nseg = (n + seglen - 1) / seglen;
+    const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
+    const uint32_t big = kClamp * 0x10001u;
+    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < npairs * nseg;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int seg = (int)(it / npairs);
+        const long long li = (it - (long long)seg * npairs) * 2;
+        const LineGeo g = line_addr(Ls, li);
+        const float *line = fin + g.base;
+        float *o = fout + g.base;
+        const int x0 = seg * seglen, x1 = min(n, x0 + seglen);
+        // big_until*: the last output position whose window holds a height
+        // that does not fit 16 bits (clamped); those outputs take the scan
+        int big_until0 = -1, big_until1 = -1;
+        auto load = [&](int y) -> uint32_t {
+            if (y < 0 || y >= n)
+                return big;
+            const float2 f = __ldg(reinterpret_cast<const float2 *>(line + y * st));
+            const float k0 = fmul(f.x, inv_a), k1 = fmul(f.y, inv_a);
+            // heights are integers K res^2 when every axis has the same
+            // power-of-two voxel size; any other height takes the scan
+            unsigned u0 = kClamp, u1 = kClamp;
+            if (k0 < (float)kClamp && k0 == truncf(k0))
+                u0 = (unsigned)k0;
+            else
+                big_until0 = y + W;
+            if (k1 < (float)kClamp && k1 == truncf(k1))
+                u1 = (unsigned)k1;
+            else
+                big_until1 = y + W;
+            return u0 | (u1 << 16);
+        };
+        uint32_t win[R];
+#pragma unroll
+        for (int s2 = 0; s2 < R; s2++)
+            win[s2] = load(x0 - W + s2);
+        int need0 = 0, need1 = 0;
+        for (int y0 = x0; y0 < x1; y0 += R) {
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int x = y0 + u;
+                if (x < x1) {
+                    uint32_t m = win[(u + W) % R];
+#pragma unroll
+                    for (int d = 1; d <= W; d++) {
+                        const uint32_t dd = (uint32_t)(d * d) * 0x10001u;
+                        m = __viaddmin_u16x2(win[(u + W - d) % R], dd, m);
+                        m = __viaddmin_u16x2(win[(u + W + d) % R], dd, m);
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
+                        bool fin_ok = mh <= kFinal && x > (h ? big_until1 : big_until0);
+                        if (fin_ok && periodic &&
+                            ((unsigned)((x + 1) * (x + 1)) <= mh || (unsigned)((n - x) * (n - x)) <= mh))
+                            fin_ok = false;
+                        float val;
+                        if (fin_ok) {
+                            val = fmul((float)mh, a);
+                        } else {
+                            float best = 0.0f;
+                            int nd = 0;
+                            if (!window_voxel_call(line + h, st, n, x, inv_a, kmax, periodic, &best, &nd)) {
+                                if (h)
+                                    need1 |= nd;
+                                else
+                                    need0 |= nd;
+                                continue;
+                            }
+                            val = fmul(best, a);
+                        }
+                        if (form == PMG_EDT_DIST)
+                            val = __fsqrt_rn(val);
+                        o[x * st + h] = val;
+                    }
+                }
+                win[u] = load(x + W + 1);
+            }
+        }
+        if (need0)
+            atomicOr(flag + li, need0);
+        if (need1)
+            atomicOr(flag + li + 1, need1);
+    }
+}
+
+// Contiguous lines (the last axis), 64 rows at a time: the rows' heights over
+// kRowsTX columns plus a W halo on each side are staged in shared memory as
+// packed 16-bit pairs (rows 2p, 2p + 1 in one word; a padded row stride keeps
+// the column walk free of bank conflicts), each thread walks 16 columns of
+// one row pair with the same register ring as k_env_pair, results go through
+// a shared tile to coalesced stores.  A row with a clamped height anywhere in
+// its staged span, an inconclusive minimum or a periodic end within reach
+// takes window_voxel on the row in global memory, as k_env_window does.
+constexpr int kRowsTX = 128;
+
+template <int W>
+constexpr size_t rows_smem_bytes()
+{
+    return sizeof(uint32_t) * 32 * (kRowsTX + 2 * W + 1) + sizeof(float) * 64 * (kRowsTX + 1) + sizeof(int) * 64;
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__ fin, float *__restrict__ fout,
+                                                       Lines Ls, float a, float inv_a, int periodic, int form,
+                                                       int *__restrict__ flag)
+{
+    constexpr int R = 2 * W + 1;
+    constexpr int SPAN = kRowsTX + 2 * W;
+    constexpr int SROW = SPAN + 1; // padded word stride of a pair row
+    constexpr unsigned kClamp = 65535u - (unsigned)(W * W) - 1u;
+    constexpr unsigned kFinal = (unsigned)((W + 1) * (W + 1));
+    constexpr float kSkip = -1.0f; // "left to the end-segment replay"
+    extern __shared__ uint32_t rows_smem[];
+    uint32_t *sin = rows_smem;                                // [32][SROW]
+    float *sout = reinterpret_cast<float *>(sin + 32 * SROW); // [64][kRowsTX + 1]
+    int *sbig = reinterpret_cast<int *>(sout + 64 * (kRowsTX + 1));
+    const long long nlines = Ls.count();
+    const int n = (int)Ls.s2;
+    const int ntx = (n + kRowsTX - 1) / kRowsTX;
+    const long long ntiles = ((nlines + 63) / 64) * ntx;
+    const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
+    const uint32_t big = kClamp * 0x10001u;
+    const int tid = threadIdx.x;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long li0 = (tile / ntx) * 64;
+        const int c0 = (int)(tile % ntx) * kRowsTX;
+        const int rows = (int)min(64LL, nlines - li0);
+        if (tid < 64)
+            sbig[tid] = 0;
+        __syncthreads();
+        // stage: (pair, column) items, columns fastest (coalesced rows)
+        for (int it = tid; it < 32 * SPAN; it += blockDim.x) {
+            const int pr = it / SPAN, cc = it - pr * SPAN;
+            const int c = c0 - W + cc;
+            uint32_t wv = big;
+            if (2 * pr < rows && c >= 0 && c < n) {
+                const LineGeo g = line_addr(Ls, li0 + 2 * pr);
+                const float f0 = fin[g.base + c], f1 = fin[g.base + (long long)n + c];
+                const float k0 = fmul(f0, inv_a), k1 = fmul(f1, inv_a);
+                unsigned u0 = kClamp, u1 = kClamp;
+                if (k0 < (float)kClamp && k0 == truncf(k0))
+                    u0 = (unsigned)k0;
+                else
+                    sbig[2 * pr] = 1;
+                if (k1 < (float)kClamp && k1 == truncf(k1))
+                    u1 = (unsigned)k1;
+                else
+                    sbig[2 * pr + 1] = 1;
+                wv = u0 | (u1 << 16);
+            }
+            sin[pr * SROW + cc] = wv;
+        }
+        __syncthreads();
+        {
+            const int pr = tid & 31, seg = tid >> 5; // 8 segments of 16 columns
+            const uint32_t *row = sin + pr * SROW;
+            const int xs = c0 + seg * 16, xe = min(n, xs + 16);
+            int need0 = 0, need1 = 0;
+            const long long lia = li0 + 2 * pr;
+            if (2 * pr < rows && xs < xe) {
+                const LineGeo g = line_addr(Ls, lia);
+                uint32_t win[R];
+#pragma unroll
+                for (int s2 = 0; s2 < R; s2++)
+                    win[s2] = row[seg * 16 + s2];
+#pragma unroll
+                for (int u = 0; u < 16; u++) {
+                    const int x = xs + u;
+                    if (x < xe) {
+                        uint32_t m = win[(u + W) % R];
+#pragma unroll
+                        for (int d = 1; d <= W; d++) {
+                            const uint32_t dd = (uint32_t)(d * d) * 0x10001u;
+                            m = __viaddmin_u16x2(win[(u + W - d) % R], dd, m);
+                            m = __viaddmin_u16x2(win[(u + W + d) % R], dd, m);
+                        }
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
+                            bool fin_ok = mh <= kFinal && !sbig[2 * pr + h];
+                            if (fin_ok && periodic &&
+                                ((unsigned)((x + 1) * (x + 1)) <= mh || (unsigned)((n - x) * (n - x)) <= mh))
+                                fin_ok = false;
+                            float val;
+                            if (fin_ok) {
+                                val = fmul((float)mh, a);
+                            } else {
+                                float best = 0.0f;
+                                int nd = 0;
+                                if (!window_voxel_call(fin + g.base + (h ? (long long)n : 0), 1, n, x, inv_a, kmax,
+                                                       periodic, &best, &nd)) {
+                                    if (h)
+                                        need1 |= nd;
+                                    else
+                                        need0 |= nd;
+                                    sout[(2 * pr + h) * (kRowsTX + 1) + (x - c0)] = kSkip;
+                                    continue;
+                                }
+                                val = fmul(best, a);
+                            }
+                            if (form == PMG_EDT_DIST)
+                                val = __fsqrt_rn(val);
+                            sout[(2 * pr + h) * (kRowsTX + 1) + (x - c0)] = val;
+                        }
+                    }
+                    win[u % R] = row[seg * 16 + u + R < SPAN ? seg * 16 + u + R : SPAN - 1];
+                }
+            }
+            if (need0)
+                atomicOr(flag + lia, need0);
+            if (need1)
+                atomicOr(flag + lia + 1, need1);
+        }
+        __syncthreads();
+        // coalesced stores of the tile
+        const int tw = min(kRowsTX, n - c0);
+        for (int it = tid; it < rows * kRowsTX; it += blockDim.x) {
+            const int r = it / kRowsTX, c = it - r * kRowsTX;
+            if (c >= tw)
+                continue;
+            const float v = sout[r * (kRowsTX + 1) + c];
+            if (v != kSkip) {
+                const LineGeo g = line_addr(Ls, li0 + r);
+                fout[g.base + c0 + c] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void k_envelope_ends(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
                                 pmg_axis_cfg cfg, int num_hull, int form, const int *__restrict__ flag)
 {
@@ -828,12 +1097,35 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
             s = cudaMemsetAsync(flag, 0, sizeof(int) * (size_t)nc, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
             if (s == PMG_OK) {
                 const float a = res * res;
-                const int ps__ = prof_begin("k_env_window", st);
                 const bool contiguous = C.ax == 2;
-                k_env_window<<<grid_for(contiguous ? nc * 32 : nc * ((n + 63) / 64), 256, 152LL * 32), 256, 0, st>>>(
-                    fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
-                prof_end(ps__, (double)nc * n * 8, st);
-                s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+                constexpr int kPairW = 16;
+                if (!contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
+                    // line pairs along the contiguous axis (float2 aligned)
+                    constexpr int kSeg = 256;
+                    const long long work = (nc >> 1) * ((n + kSeg - 1) / kSeg);
+                    const int ps__ = prof_begin("k_env_pair", st);
+                    k_env_pair<kPairW><<<grid_for(work, 256, 152LL * 32), 256, 0, st>>>(
+                        fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, kSeg);
+                    prof_end(ps__, (double)nc * n * 8, st);
+                } else if (contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
+                    // row pairs through shared-memory tiles
+                    const long long tiles = ((nc + 63) / 64) * ((n + kRowsTX - 1) / kRowsTX);
+                    const size_t sm = rows_smem_bytes<kPairW>();
+                    s = cudaFuncSetAttribute(k_env_pair_rows<kPairW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sm) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+                    const int ps__ = prof_begin("k_env_pair_rows", st);
+                    if (s == PMG_OK)
+                        k_env_pair_rows<kPairW><<<(unsigned)std::min<long long>(tiles, 152LL * 16), 256, sm, st>>>(
+                            fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
+                    prof_end(ps__, (double)nc * n * 8, st);
+                } else {
+                    const int ps__ = prof_begin("k_env_window", st);
+                    k_env_window<<<grid_for(contiguous ? nc * 32 : nc * ((n + 63) / 64), 256, 152LL * 32), 256, 0,
+                                   st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
+                    prof_end(ps__, (double)nc * n * 8, st);
+                }
+                if (s == PMG_OK)
+                    s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
             }
             if (s == PMG_OK) {
                 const int ps__ = prof_begin("k_envelope_ends", st);

@@ -170,6 +170,8 @@ def test_training_lowers_the_loss_and_resumes(tmp_path):
     net2 = ScheduleNet.load(p)
     assert net2.step == net.step
     assert torch.equal(net2.predict(x), net.predict(x))
+    # the split-K weight gradients add fp32 partial sums with atomics, whose
+    # order varies between runs: equal up to that rounding
     l1 = float(net.train_step(x, target, lr=3e-3).item())
     l2 = float(net2.train_step(x, target, lr=3e-3).item())
-    assert l1 == l2
+    assert abs(l1 - l2) <= 1e-5 * abs(l1)

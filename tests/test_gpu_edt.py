@@ -76,6 +76,25 @@ def test_edt3d_periodic_pow2_vs_oracle(D, seed):
     np.testing.assert_array_equal(got, want)
 
 
+@pytest.mark.parametrize("seed", range(10))
+def test_edt3d_line_pairs_vs_oracle(D, seed):
+    """Envelope passes over pairs of lines (even extents): packed direct
+    minima within +-16, the per-voxel scan beyond it, for clamped heights
+    (lines without a solid voxel) and near periodic line ends; lines longer
+    than one 256-voxel segment or one 128-column tile; porosities from 30 %
+    to 99.9 %."""
+    rng = np.random.default_rng(900 + seed)
+    shape = [(300, 90, 64), (70, 520, 32), (64, 64, 128), (33, 270, 18), (260, 40, 2)][seed % 5]
+    p0 = float([0.7, 0.3, 0.05, 0.01, 0.001][seed % 5 if seed < 5 else (seed + 2) % 5])
+    img = (rng.random(shape) >= p0).astype(np.uint8)
+    per = [(True, True, True), (False, False, False), (True, False, True), (False, True, False)][seed % 4]
+    res = [(1.0, 1.0, 1.0), (0.5, 0.5, 0.5), (1 / 128, 1 / 128, 1 / 128)][seed % 3]
+    for squared in (True, False):
+        got = D.edt3d(img, periodic=per, resolution=res, squared=squared)
+        want = O.edt3d(img, periodic=per, resolution=res, squared=squared)
+        np.testing.assert_array_equal(got, want)
+
+
 def test_edt_subdomain_golden(D, golden, golden_meta):
     from tests._helpers import geom_from_meta
     for ci, case in enumerate(golden_meta["sub_cases"]):
