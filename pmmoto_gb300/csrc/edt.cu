@@ -688,12 +688,13 @@ __device__ __noinline__ bool window_voxel_call(const float *line, long long st, 
 // to window_voxel for that voxel, which sets the same line flags as
 // k_env_window.  Outputs are those of k_env_window, with far fewer
 // divergent loops.
-template <int W>
+template <int W, int A>
 __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
                                                   float a, float inv_a, int periodic, int form, int *__restrict__ flag,
                                                   int seglen)
 {
-    constexpr int R = 2 * W + 1;
+    constexpr int R = 2 * W + 1; // the window of packed heights
+    static_assert(R % A == 0, "the raw ring's slots must repeat with the window's");
     constexpr unsigned kClamp = 65535u - (unsigned)(W * W) - 1u;
     constexpr unsigned kFinal = (unsigned)((W + 1) * (W + 1));
     const long long nlines = Ls.count();
@@ -704,6 +705,7 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
     const int nseg = (n + seglen - 1) / seglen;
     const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
     const uint32_t big = kClamp * 0x10001u;
+    const float2 kOut = make_float2(-1.0f, -1.0f); // marks a position outside the line
     for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < npairs * nseg;
          it += (long long)gridDim.x * blockDim.x) {
         const int seg = (int)(it / npairs);
@@ -713,15 +715,19 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
         float *o = fout + g.base;
         const int x0 = seg * seglen, x1 = min(n, x0 + seglen);
         // big_until*: the last output position whose window holds a height
-        // that does not fit 16 bits (clamped); those outputs take the scan
+        // that is not an integer below 2^16 (clamped); those outputs take the scan
         int big_until0 = -1, big_until1 = -1;
-        auto load = [&](int y) -> uint32_t {
-            if (y < 0 || y >= n)
+        auto raw = [&](int y) -> float2 {
+            return (y < 0 || y >= n) ? kOut : __ldg(reinterpret_cast<const float2 *>(line + y * st));
+        };
+        // packing happens when a position enters the window, A positions
+        // after its load was issued, so the warp does not wait on the load
+        auto pack = [&](float2 f, int y) -> uint32_t {
+            if (f.x < 0.0f)
                 return big;
-            const float2 f = __ldg(reinterpret_cast<const float2 *>(line + y * st));
-            const float k0 = fmul(f.x, inv_a), k1 = fmul(f.y, inv_a);
             // heights are integers K res^2 when every axis has the same
             // power-of-two voxel size; any other height takes the scan
+            const float k0 = fmul(f.x, inv_a), k1 = fmul(f.y, inv_a);
             unsigned u0 = kClamp, u1 = kClamp;
             if (k0 < (float)kClamp && k0 == truncf(k0))
                 u0 = (unsigned)k0;
@@ -734,9 +740,13 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
             return u0 | (u1 << 16);
         };
         uint32_t win[R];
+        float2 ahead[A];
 #pragma unroll
         for (int s2 = 0; s2 < R; s2++)
-            win[s2] = load(x0 - W + s2);
+            win[s2] = pack(raw(x0 - W + s2), x0 - W + s2);
+#pragma unroll
+        for (int q = 0; q < A; q++)
+            ahead[q] = raw(x0 + W + 1 + q);
         int need0 = 0, need1 = 0;
         for (int y0 = x0; y0 < x1; y0 += R) {
 #pragma unroll
@@ -777,7 +787,10 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
                         o[x * st + h] = val;
                     }
                 }
-                win[u] = load(x + W + 1);
+                // position x + W + 1 enters the window (loaded A outputs ago),
+                // position x + W + 1 + A is loaded
+                win[u] = pack(ahead[u % A], x + W + 1);
+                ahead[u % A] = raw(x + W + 1 + A);
             }
         }
         if (need0)
@@ -818,6 +831,7 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
     uint32_t *sin = rows_smem;                                // [32][SROW]
     float *sout = reinterpret_cast<float *>(sin + 32 * SROW); // [64][kRowsTX + 1]
     int *sbig = reinterpret_cast<int *>(sout + 64 * (kRowsTX + 1));
+    __shared__ long long sbase[64]; // first element of each staged row
     const long long nlines = Ls.count();
     const int n = (int)Ls.s2;
     const int ntx = (n + kRowsTX - 1) / kRowsTX;
@@ -825,34 +839,57 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
     const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
     const uint32_t big = kClamp * 0x10001u;
     const int tid = threadIdx.x;
+    // rows start on 16-byte boundaries when the row length is a multiple of 4
+    // (and the volume starts on one)
+    const bool vec4 = !(n & 3) && !(reinterpret_cast<uintptr_t>(fin) & 15);
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long li0 = (tile / ntx) * 64;
         const int c0 = (int)(tile % ntx) * kRowsTX;
         const int rows = (int)min(64LL, nlines - li0);
-        if (tid < 64)
+        if (tid < 64) {
             sbig[tid] = 0;
+            sbase[tid] = tid < rows ? line_addr(Ls, li0 + tid).base : 0;
+        }
         __syncthreads();
-        // stage: (pair, column) items, columns fastest (coalesced rows)
-        for (int it = tid; it < 32 * SPAN; it += blockDim.x) {
-            const int pr = it / SPAN, cc = it - pr * SPAN;
+        // stage: (pair, 4-column group) items, columns fastest (coalesced
+        // rows); 16-byte loads where the rows allow them
+        auto pack = [&](int pr, float f0, float f1) -> uint32_t {
+            const float k0 = fmul(f0, inv_a), k1 = fmul(f1, inv_a);
+            unsigned u0 = kClamp, u1 = kClamp;
+            if (k0 < (float)kClamp && k0 == truncf(k0))
+                u0 = (unsigned)k0;
+            else
+                sbig[2 * pr] = 1;
+            if (k1 < (float)kClamp && k1 == truncf(k1))
+                u1 = (unsigned)k1;
+            else
+                sbig[2 * pr + 1] = 1;
+            return u0 | (u1 << 16);
+        };
+        static_assert(SPAN % 4 == 0 && W % 4 == 0, "4-column groups");
+        for (int it = tid; it < 32 * (SPAN / 4); it += blockDim.x) {
+            const int pr = it / (SPAN / 4), cc = (it - pr * (SPAN / 4)) * 4;
             const int c = c0 - W + cc;
-            uint32_t wv = big;
-            if (2 * pr < rows && c >= 0 && c < n) {
-                const LineGeo g = line_addr(Ls, li0 + 2 * pr);
-                const float f0 = fin[g.base + c], f1 = fin[g.base + (long long)n + c];
-                const float k0 = fmul(f0, inv_a), k1 = fmul(f1, inv_a);
-                unsigned u0 = kClamp, u1 = kClamp;
-                if (k0 < (float)kClamp && k0 == truncf(k0))
-                    u0 = (unsigned)k0;
-                else
-                    sbig[2 * pr] = 1;
-                if (k1 < (float)kClamp && k1 == truncf(k1))
-                    u1 = (unsigned)k1;
-                else
-                    sbig[2 * pr + 1] = 1;
-                wv = u0 | (u1 << 16);
+            uint32_t wv[4] = {big, big, big, big};
+            if (2 * pr < rows) {
+                const long long b0 = sbase[2 * pr];
+                if (vec4 && c >= 0 && c + 3 < n) {
+                    const float4 f0 = __ldg(reinterpret_cast<const float4 *>(fin + b0 + c));
+                    const float4 f1 = __ldg(reinterpret_cast<const float4 *>(fin + b0 + (long long)n + c));
+                    wv[0] = pack(pr, f0.x, f1.x);
+                    wv[1] = pack(pr, f0.y, f1.y);
+                    wv[2] = pack(pr, f0.z, f1.z);
+                    wv[3] = pack(pr, f0.w, f1.w);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (c + q >= 0 && c + q < n)
+                            wv[q] = pack(pr, fin[b0 + c + q], fin[b0 + (long long)n + c + q]);
+                }
             }
-            sin[pr * SROW + cc] = wv;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                sin[pr * SROW + cc + q] = wv[q];
         }
         __syncthreads();
         {
@@ -862,7 +899,7 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
             int need0 = 0, need1 = 0;
             const long long lia = li0 + 2 * pr;
             if (2 * pr < rows && xs < xe) {
-                const LineGeo g = line_addr(Ls, lia);
+                const long long rbase = sbase[2 * pr];
                 uint32_t win[R];
 #pragma unroll
                 for (int s2 = 0; s2 < R; s2++)
@@ -891,7 +928,7 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
                             } else {
                                 float best = 0.0f;
                                 int nd = 0;
-                                if (!window_voxel_call(fin + g.base + (h ? (long long)n : 0), 1, n, x, inv_a, kmax,
+                                if (!window_voxel_call(fin + rbase + (h ? (long long)n : 0), 1, n, x, inv_a, kmax,
                                                        periodic, &best, &nd)) {
                                     if (h)
                                         need1 |= nd;
@@ -923,10 +960,8 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
             if (c >= tw)
                 continue;
             const float v = sout[r * (kRowsTX + 1) + c];
-            if (v != kSkip) {
-                const LineGeo g = line_addr(Ls, li0 + r);
-                fout[g.base + c0 + c] = v;
-            }
+            if (v != kSkip)
+                fout[sbase[r] + c0 + c] = v;
         }
         __syncthreads();
     }
@@ -1098,13 +1133,13 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
             if (s == PMG_OK) {
                 const float a = res * res;
                 const bool contiguous = C.ax == 2;
-                constexpr int kPairW = 16;
+                constexpr int kPairW = 12, kAhead = 5;
                 if (!contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
                     // line pairs along the contiguous axis (float2 aligned)
                     constexpr int kSeg = 256;
                     const long long work = (nc >> 1) * ((n + kSeg - 1) / kSeg);
                     const int ps__ = prof_begin("k_env_pair", st);
-                    k_env_pair<kPairW><<<grid_for(work, 256, 152LL * 32), 256, 0, st>>>(
+                    k_env_pair<kPairW, kAhead><<<grid_for(work, 256, 152LL * 32), 256, 0, st>>>(
                         fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, kSeg);
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else if (contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {

@@ -79,7 +79,7 @@ def test_edt3d_periodic_pow2_vs_oracle(D, seed):
 @pytest.mark.parametrize("seed", range(10))
 def test_edt3d_line_pairs_vs_oracle(D, seed):
     """Envelope passes over pairs of lines (even extents): packed direct
-    minima within +-16, the per-voxel scan beyond it, for clamped heights
+    minima within +-12, the per-voxel scan beyond it, for clamped heights
     (lines without a solid voxel) and near periodic line ends; lines longer
     than one 256-voxel segment or one 128-column tile; porosities from 30 %
     to 99.9 %."""
