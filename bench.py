@@ -451,6 +451,9 @@ def measure_large(args, local, peak, peak_kind):
     from pmmoto_gb300.filters import distance as D
 
     n = 1024
+    from pmmoto_gb300 import tune
+
+    tuned = tune.tune_edt((n, n, n))  # launch parameters of this shape class (cached)
     own = grf.gen_grf_medium(n)
     idx = torch.arange(-1, n + 1, device="cuda") % n
     img = own[idx][:, idx][:, :, idx].contiguous()
@@ -465,6 +468,7 @@ def measure_large(args, local, peak, peak_kind):
            "cc": (lambda: CC.connect_components_device(img, geo), img.numel(), 17.0)}
     res_out = {"workload": "1024^3 GRF medium (sigma 4, porosity 0.35, periodic); edt3d squared on the own "
                            "1024^3 volume, connected components on the padded 1026^3 image",
+               "edt_tuned": tuned,
                "l2": "inputs larger than L2 (1 GB image, 4 GB distances, 8.6 GB labels)"}
     steps = max(3, min(args.steps, 10))
     for name, (op, vox, bpv) in ops.items():
@@ -556,21 +560,29 @@ def run_batch(args):
         sat = ED.drainage(mp, pcs, mode="distance")
         return float(sat[-1]), int(nlab)
 
+    workers = args.workers
+    tuned = None
+    if workers <= 0:  # autotune the stream count on the first 64 packs (cached per shape class)
+        from pmmoto_gb300 import tune
+
+        items = [(p[0], m) for p, m in zip(packs, media)][:64]
+        tuned = tune.tune_batch(items, lambda it: one(it[1]))
+        workers = tuned["batch.workers"]
     for _ in range(args.warmup):
-        batch.map_streams(one, media, workers=args.workers)
+        batch.map_streams(one, media, workers=workers)
     torch.cuda.synchronize()
     n0 = L.pmg_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     t0 = time.time()
     for _ in range(args.steps):
-        res = batch.map_streams(one, media, workers=args.workers)
+        res = batch.map_streams(one, media, workers=workers)
     e1.record()
     torch.cuda.synchronize()
     wall = (time.time() - t0) / args.steps
     launches = (L.pmg_launch_count() - n0) // args.steps
     vox = sum(int(np.prod([v + 2 for v in p[0]])) for p in packs)
-    print(json.dumps({"case": "batch", "packs": len(packs), "workers": args.workers,
+    print(json.dumps({"case": "batch", "packs": len(packs), "workers": workers, "tuned": tuned,
                       "metric": "batched packs/s (EDT + CC + 24-radius drainage per pack)",
                       "value": len(packs) / wall, "unit": "packs/s", "ms_per_batch": wall * 1e3,
                       "gpu_ms_per_batch": e0.elapsed_time(e1) / args.steps, "voxels": vox,
@@ -710,7 +722,8 @@ def main():
                     choices=["drainage", "edt", "cc", "morph", "select", "batch", "cnn"])
     ap.add_argument("--batch", type=int, default=64, help="samples per training step of the cnn case")
     ap.add_argument("--packs", type=int, default=256, help="packs of the batched case")
-    ap.add_argument("--workers", type=int, default=8, help="host threads / CUDA streams of the batched case")
+    ap.add_argument("--workers", type=int, default=8,
+                    help="host threads / CUDA streams of the batched case (0: autotune, cached per shape class)")
     ap.add_argument("--n", type=int, default=512, help="volume side of the single-operator cases")
     ap.add_argument("--bc", default="periodic", choices=["periodic", "wall"],
                     help="boundary type of every face in the single-operator cases")

@@ -345,6 +345,18 @@ int pmg_prof_read(char *names, size_t names_len, double *ms, double *bytes,
  */
 int pmg_set_iteration_cap(int32_t cap);
 
+/*
+ * Tunable launch parameters (no counterpart in the reference): results never
+ * depend on them, only speed.  Names: "edt.pair_seg" (positions per thread
+ * of the strided line-pair envelope pass, default 256), "edt.pair_ctas" and
+ * "edt.rows_ctas" (CTAs per SM of the strided and contiguous line-pair
+ * passes, defaults 32 and 16).  value 0 restores the default; values are
+ * process-wide and apply to launches that follow.  pmmoto_gb300.tune sets
+ * them from its cached measurements.
+ */
+int pmg_tune_set(const char *name, int32_t value);
+int pmg_tune_get(const char *name, int32_t *value);
+
 /* Message of the last failure on this host thread (empty if none). */
 int pmg_last_error(char *buf, size_t len);
 

@@ -57,6 +57,8 @@ def _declare(L):
         "pmg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
         "pmg_set_iteration_cap": [i32],
         "pmg_grf_smooth": [P, P, i64, P, i32, P, i32, P],
+        "pmg_tune_set": [ctypes.c_char_p, i32],
+        "pmg_tune_get": [ctypes.c_char_p, P],
     }
     for name, args in sig.items():
         if hasattr(L, name):

@@ -1136,11 +1136,12 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                 constexpr int kPairW = 12, kAhead = 5;
                 if (!contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
                     // line pairs along the contiguous axis (float2 aligned)
-                    constexpr int kSeg = 256;
-                    const long long work = (nc >> 1) * ((n + kSeg - 1) / kSeg);
+                    const int seg = tune_value(kTuneEdtPairSeg);
+                    const long long work = (nc >> 1) * ((n + seg - 1) / seg);
                     const int ps__ = prof_begin("k_env_pair", st);
-                    k_env_pair<kPairW, kAhead><<<grid_for(work, 256, 152LL * 32), 256, 0, st>>>(
-                        fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, kSeg);
+                    k_env_pair<kPairW, kAhead><<<grid_for(work, 256, 152LL * tune_value(kTuneEdtPairCtas)), 256, 0,
+                                                 st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag,
+                                                       seg);
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else if (contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
                     // row pairs through shared-memory tiles
@@ -1150,7 +1151,9 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                                              (int)sm) == cudaSuccess ? PMG_OK : PMG_ECUDA;
                     const int ps__ = prof_begin("k_env_pair_rows", st);
                     if (s == PMG_OK)
-                        k_env_pair_rows<kPairW><<<(unsigned)std::min<long long>(tiles, 152LL * 16), 256, sm, st>>>(
+                        k_env_pair_rows<kPairW><<<(unsigned)std::min<long long>(
+                                                       tiles, 152LL * tune_value(kTuneEdtRowsCtas)),
+                                                   256, sm, st>>>(
                             fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else {

@@ -57,6 +57,11 @@ constexpr int kUnitsGrowUniteA = 4, kUnitsGrowUniteB = 5, kUnitsCrossUnite = 6, 
 unsigned long long *prof_units(int id);
 void prof_end_units(int slot, int id, double bytes_per_unit, cudaStream_t st);
 
+// Launch parameters an autotuner may change at run time (pmg_tune_set):
+// results never depend on them, only speed.  Read once per launch.
+enum TuneKnob { kTuneEdtPairSeg = 0, kTuneEdtPairCtas, kTuneEdtRowsCtas, kTuneKnobs };
+int tune_value(int knob);
+
 // Validate a padded single-rank geometry: positive shape, boundary codes in
 // range, non-negative pads that leave a non-empty own region on every axis.
 inline int check_geometry(const int64_t *shape, const int32_t *bc, const int32_t *pad)

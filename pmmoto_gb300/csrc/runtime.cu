@@ -73,6 +73,28 @@ int scratch_free(void *p, cudaStream_t st)
     return PMG_OK;
 }
 
+// ---- tunable launch parameters ------------------------------------------------
+struct TuneSpec {
+    const char *name;
+    int def, lo, hi;
+};
+static const TuneSpec g_tune_spec[kTuneKnobs] = {
+    {"edt.pair_seg", 256, 32, 8192},    // positions per thread of the strided line-pair pass
+    {"edt.pair_ctas", 32, 1, 256},      // CTAs per SM of that pass (grid cap)
+    {"edt.rows_ctas", 16, 1, 256},      // CTAs per SM of the contiguous line-pair pass
+};
+static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}};
+
+int tune_value(int knob) { return knob >= 0 && knob < kTuneKnobs ? g_tune[knob].load() : 0; }
+
+static int tune_index(const char *name)
+{
+    for (int i = 0; name && i < kTuneKnobs; i++)
+        if (strcmp(name, g_tune_spec[i].name) == 0)
+            return i;
+    return -1;
+}
+
 static std::atomic<long long> g_launches{0};
 static std::atomic<int> g_prof_on{0};
 struct ProfRec {
@@ -248,4 +270,33 @@ extern "C" int pmg_last_error(char *buf, size_t len)
 extern "C" const char *pmg_version(void)
 {
     return "pmmoto_gb300 0.1 (sm_103a)";
+}
+
+extern "C" int pmg_tune_set(const char *name, int32_t value)
+{
+    const int i = pmg::tune_index(name);
+    if (i < 0) {
+        pmg::set_error("pmg_tune_set: unknown parameter '%s'", name ? name : "(null)");
+        return PMG_EINVAL;
+    }
+    const pmg::TuneSpec &t = pmg::g_tune_spec[i];
+    if (value == 0)
+        value = t.def;
+    if (value < t.lo || value > t.hi) {
+        pmg::set_error("pmg_tune_set: %s = %d outside [%d, %d]", name, value, t.lo, t.hi);
+        return PMG_ERANGE;
+    }
+    pmg::g_tune[i].store(value);
+    return PMG_OK;
+}
+
+extern "C" int pmg_tune_get(const char *name, int32_t *value)
+{
+    const int i = pmg::tune_index(name);
+    if (i < 0 || !value) {
+        pmg::set_error("pmg_tune_get: unknown parameter '%s'", name ? name : "(null)");
+        return PMG_EINVAL;
+    }
+    *value = pmg::g_tune[i].load();
+    return PMG_OK;
 }

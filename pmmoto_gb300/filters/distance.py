@@ -12,7 +12,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from .. import _dev
+from .. import _dev, tune
 from .._lib import AxisCfg, EDT_DIST, EDT_SQUARED, check, i64_array, lib, host_ptr
 
 __all__ = ["edt", "edt2d", "edt3d"]
@@ -48,6 +48,7 @@ def edt3d_device(t: torch.Tensor, res32: np.ndarray, cfg, squared: bool, out: to
         raise ValueError(f"Wrong img dimension {tuple(t.shape)}")
     if out is None:
         out = torch.empty(t.shape, dtype=torch.float32, device=t.device)
+    tune.apply("edt", t.shape)  # tuned launch parameters of this shape class, if any
     shape = i64_array(t.shape)
     st = lib().pmg_edt3d(_dev.ptr(t), _dev.ptr(out), host_ptr(shape), host_ptr(res32), cfg, NUM_HULL,
                          EDT_SQUARED if squared else EDT_DIST, _dev.stream_ptr(t.device))

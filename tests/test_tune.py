@@ -1,0 +1,46 @@
+"""Host logic of the autotuner: shape classes, cache keys and round trips,
+the PMG_TUNE override, and the library's tunable-parameter table (names,
+ranges, defaults) -- no GPU needed."""
+
+import ctypes
+import json
+
+import pytest
+
+from pmmoto_gb300 import tune
+
+
+def test_shape_class_and_key():
+    assert tune.shape_class((1024, 1026, 3)) == "1024x2048x4"
+    assert tune.key("edt", (96, 128, 130), gpu="G") == "G|edt|128x128x256"
+
+
+def test_cache_round_trip_and_override(tmp_path, monkeypatch):
+    monkeypatch.setenv("PMG_TUNE_CACHE", str(tmp_path / "c.json"))
+    monkeypatch.delenv("PMG_TUNE", raising=False)
+    k = tune.key("edt", (64, 64, 64), gpu="cpu")
+    tune.save_entry(k, {"edt.pair_seg": 512}, {"edt.pair_seg": {"512": 1.0}})
+    assert json.load(open(tmp_path / "c.json"))[k]["settings"] == {"edt.pair_seg": 512}
+    monkeypatch.setattr(tune, "gpu_name", lambda: "cpu")
+    assert tune.settings_for("edt", (60, 64, 33)) == {"edt.pair_seg": 512}
+    monkeypatch.setenv("PMG_TUNE", "edt.pair_seg=128, edt.rows_ctas=8")
+    assert tune.settings_for("edt", (64, 64, 64)) == {"edt.pair_seg": 128, "edt.rows_ctas": 8}
+    monkeypatch.setenv("PMG_TUNE", "edt.pair_seg")
+    with pytest.raises(ValueError):
+        tune.overrides()
+
+
+def test_library_knob_table():
+    from pmmoto_gb300 import _lib
+
+    L = _lib.lib()
+    v = ctypes.c_int32(0)
+    for name, cands in tune.KNOBS["edt"].items():
+        assert L.pmg_tune_get(name.encode(), ctypes.byref(v)) == 0
+        default = v.value
+        for c in cands:
+            assert L.pmg_tune_set(name.encode(), c) == 0
+        assert L.pmg_tune_set(name.encode(), 0) == 0  # back to the default
+        assert L.pmg_tune_get(name.encode(), ctypes.byref(v)) == 0 and v.value == default
+    assert L.pmg_tune_set(b"edt.pair_seg", 1) == _lib.PMG_ERANGE
+    assert L.pmg_tune_set(b"no.such", 4) == _lib.PMG_EINVAL
