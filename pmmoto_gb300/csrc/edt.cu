@@ -105,6 +105,105 @@ __global__ void k_pass0(const uint8_t *__restrict__ img, float *__restrict__ out
     }
 }
 
+// k_pass0 on four adjacent strided lines per thread (their voxels are
+// adjacent along the contiguous axis): uchar4 loads of the image and float4
+// loads and stores of the distances, each of the four lines with the same
+// state and the same float operations as k_pass0.
+__global__ void __launch_bounds__(256) k_pass0_x4(const uint8_t *__restrict__ img, float *__restrict__ out, Lines Ls,
+                                                  float res, pmg_axis_cfg cfg)
+{
+    const long long nquads = Ls.count() >> 2;
+    for (long long qi = blockIdx.x * (long long)blockDim.x + threadIdx.x; qi < nquads;
+         qi += (long long)gridDim.x * blockDim.x) {
+        const LineGeo g = line_addr(Ls, qi * 4);
+        const uint8_t *in = img + g.base;
+        float *d = out + g.base;
+        const long long st = g.stride;
+        const int n = g.n;
+        float lc[4] = {INFINITY, INFINITY, INFINITY, INFINITY}, uc[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
+        if (cfg.periodic) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                int F = -1, L = -1;
+                for (int i = cfg.f_lo; i < n; i++)
+                    if (in[i * st + q] == 0) {
+                        F = i;
+                        break;
+                    }
+                for (int i = n - cfg.l_hi - 1; i >= cfg.l_lo; i--)
+                    if (in[i * st + q] == 0) {
+                        L = i;
+                        break;
+                    }
+                if (F != -1)
+                    uc[q] = (float)(F + cfg.a_u);
+                if (L != -1)
+                    lc[q] = (float)(n - L + cfg.a_l);
+            }
+        }
+        // forward sweep (reset at zeros, restart at a change of nonzero value)
+        const uchar4 v0 = *reinterpret_cast<const uchar4 *>(in);
+        uint8_t seg[4] = {v0.x, v0.y, v0.z, v0.w};
+        uint8_t prev_v[4] = {v0.x, v0.y, v0.z, v0.w};
+        float prev[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            prev[q] = seg[q] == 0 ? 0.0f : fmul(lc[q], res);
+        *reinterpret_cast<float4 *>(d) = make_float4(prev[0], prev[1], prev[2], prev[3]);
+#pragma unroll 4
+        for (int i = 1; i < n; i++) {
+            const uchar4 vv = *reinterpret_cast<const uchar4 *>(in + i * st);
+            const uint8_t v[4] = {vv.x, vv.y, vv.z, vv.w};
+            float cur[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (v[q] == 0) {
+                    cur[q] = 0.0f;
+                } else if (v[q] == seg[q]) {
+                    cur[q] = fadd(prev[q], res);
+                } else {
+                    cur[q] = res;
+                    d[(i - 1) * st + q] = prev_v[q] != 0 ? res : 0.0f;
+                    seg[q] = v[q];
+                }
+                prev[q] = cur[q];
+                prev_v[q] = v[q];
+            }
+            *reinterpret_cast<float4 *>(d + i * st) = make_float4(cur[0], cur[1], cur[2], cur[3]);
+        }
+        // clamp the last voxel, backward sweep, square, inf -> FLT_MAX
+        float b[4];
+        {
+            const float4 t = *reinterpret_cast<const float4 *>(d + (n - 1) * st);
+            const float tv[4] = {t.x, t.y, t.z, t.w};
+            float q4[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                b[q] = tv[q];
+                const float ucr = fmul(uc[q], res);
+                if (b[q] > ucr)
+                    b[q] = ucr;
+                const float sq = fmul(b[q], b[q]);
+                q4[q] = sq == INFINITY ? FLT_MAX : sq;
+            }
+            *reinterpret_cast<float4 *>(d + (n - 1) * st) = make_float4(q4[0], q4[1], q4[2], q4[3]);
+        }
+#pragma unroll 4
+        for (int i = n - 2; i >= 0; i--) {
+            const float4 t = *reinterpret_cast<const float4 *>(d + i * st);
+            const float tv[4] = {t.x, t.y, t.z, t.w};
+            float q4[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                b[q] = fminf(tv[q], fadd(b[q], res));
+                const float sq = fmul(b[q], b[q]);
+                q4[q] = sq == INFINITY ? FLT_MAX : sq;
+            }
+            *reinterpret_cast<float4 *>(d + i * st) = make_float4(q4[0], q4[1], q4[2], q4[3]);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // envelope stack kept as a bitmask in shared memory
 // ---------------------------------------------------------------------------
@@ -1069,7 +1168,14 @@ int launch_pass0(const uint8_t *img, float *out, const Lines &Ls, float res,
     const int block = 256;
     {
         const int ps__ = prof_begin("k_pass0", st);
-        k_pass0<<<grid_for(Ls.count(), block, 1LL << 30), block, 0, st>>>(img, out, Ls, res, cfg);
+        // four adjacent strided lines per thread where the quads align to 16
+        // bytes (float4) and 4 bytes (uchar4)
+        const bool quads = Ls.ax != 2 && !(Ls.nb2 & 3) && !(Ls.b2lo & 3) && !(Ls.s2 & 3) &&
+                           !(reinterpret_cast<uintptr_t>(out) & 15) && !(reinterpret_cast<uintptr_t>(img) & 3);
+        if (quads)
+            k_pass0_x4<<<grid_for(Ls.count() >> 2, block, 1LL << 30), block, 0, st>>>(img, out, Ls, res, cfg);
+        else
+            k_pass0<<<grid_for(Ls.count(), block, 1LL << 30), block, 0, st>>>(img, out, Ls, res, cfg);
         prof_end(ps__, (double)Ls.count() * (Ls.ax == 0 ? Ls.s0 : Ls.ax == 1 ? Ls.s1 : Ls.s2) * 5, st);
     }
     PMG_CHECK_LAUNCH();
