@@ -2,11 +2,12 @@
 
     python -m pmmoto_gb300.learned.evaluate --packs 50 --out eval.json
 
-For each held-out medium, three curves over the same 64 radii:
+For each held-out medium, four curves over the same 64 radii:
 
 * dense   -- all 64 radii evaluated exactly (the judge of curve error);
 * learned -- ``LearnedSchedule`` (at most 12 exact radii, dense fallback);
-* uniform -- 12 evenly spaced exact radii, linear fill (no network).
+* uniform -- 12 evenly spaced exact radii, linear fill (no network);
+* predicted -- the network's curve alone, no exact radius.
 
 Media: 512^3 sphere packs of the plain-drainage configuration (3,000
 spheres, radii U[0.02, 0.05], walls y/z, inlet x-, outlet x+) with seeds the
@@ -75,7 +76,12 @@ def evaluate_medium(sd, img, sched):
         pm = _fresh(sd, img)
         return schedule.uniform_curve(sd, pm, sched.budget)
 
+    def predicted():
+        pm = _fresh(sd, img)
+        return sched.predicted_curve(sd, pm)
+
     sd_curve, t_dense = _timed(dense)
+    pcurve, t_pred = _timed(predicted)
     (lc, linfo), t_learned = _timed(learned)
     (uc, uinfo), t_uniform = _timed(uniform)
     # the same pipeline with a perfect prediction (the dense curve itself):
@@ -84,7 +90,8 @@ def evaluate_medium(sd, img, sched):
     k_min = schedule.active_from(float(pm.max_distance), min(sd.domain.resolution))
     plan = schedule.plan_radii(sd_curve, k_min, sched.budget)
     pc = schedule.fill(data.curve_at(sd, pm, plan, float(pm.max_distance)), sd_curve, k_min)
-    return {"dense_s": t_dense, "learned_s": t_learned, "uniform_s": t_uniform,
+    return {"dense_s": t_dense, "learned_s": t_learned, "uniform_s": t_uniform, "predict_s": t_pred,
+            "predict_only_max_abs": float(np.abs(pcurve - sd_curve).max()),
             "perfect_plan_max_abs": float(np.abs(pc - sd_curve).max()),
             "learned_max_abs": float(np.abs(lc - sd_curve).max()),
             "uniform_max_abs": float(np.abs(uc - sd_curve).max()),
@@ -113,7 +120,10 @@ def summarise(rows):
             "exact_vs_dense_at_plan_max": float(max(r["exact_vs_dense_at_plan"] for r in rows)),
             "perfect_plan_max_abs_dS": float(max(r["perfect_plan_max_abs"] for r in rows)),
             "perfect_plan_mean_max_abs_dS": float(np.mean([r["perfect_plan_max_abs"] for r in rows])),
-            "pred_max_abs_mean": float(np.mean([r["pred_max_abs"] for r in rows]))}
+            "pred_max_abs_mean": float(np.mean([r["pred_max_abs"] for r in rows])),
+            "predict_only_curves_s": len(rows) / sum(r["predict_s"] for r in rows),
+            "predict_only_max_abs_dS": float(max(r["predict_only_max_abs"] for r in rows)),
+            "predict_only_mean_max_abs_dS": float(np.mean([r["predict_only_max_abs"] for r in rows]))}
 
 
 def run(packs=50, grfs=50, seed0=5000, sched=None, warm=True, keep_curves=False):

@@ -127,6 +127,14 @@ class LearnedSchedule:
         x = data.features(sd, pm).reshape(1, -1)
         return self.net.predict(x)[0].double().cpu().numpy()
 
+    def predicted_curve(self, sd, pm) -> np.ndarray:
+        """The network's curve alone (no exact radius): monotone prediction,
+        radii below the voxel size holding the smallest active radius's value."""
+        k_min = active_from(float(pm.max_distance), min(sd.domain.resolution))
+        c = monotone(self.predict(sd, pm))
+        c[:k_min] = c[k_min]
+        return c
+
     def curve(self, sd, pm):
         """(curve [64], info): info has the planned indices, the exact values,
         whether the dense fallback ran, and the number of exact radii."""
