@@ -1407,6 +1407,12 @@ __global__ void __launch_bounds__(512) k_bcc_cross(const uint8_t *__restrict__ M
 
 // Phase 2b: the listed border blocks unite with touching earlier neighbours in
 // other tiles; neighbours reached through an in-tile neighbour are skipped.
+// Each lane first collects its block's union targets, then the warp issues
+// them in rounds: lanes whose (block parent, neighbour parent) pairs are
+// equal would unite the same two components, so one lane per distinct pair
+// unites (parents only ever move towards roots, so equal parents read at
+// any time mean equal roots).  Consecutive listed blocks mostly come from one
+// tile and reach the same neighbouring components.
 __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G, int *err, const int *hard,
                                   const int *nhard, unsigned long long *units)
 {
@@ -1416,32 +1422,54 @@ __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G
     const int cnt = *nhard;
     if (units && blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0)
         atomicAdd(units, (unsigned long long)cnt);
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < cnt; h += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int h0 = warp * 32; h0 < cnt; h0 += nwarps * 32) {
         // listed border blocks (block indices) and their offsets in their tile
-        const int bi = hard[h];
-        const int r = bi / G.b2;
-        const int c2 = bi - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
-        const int a = c0 % kT0, b = c1 % kT1, c = c2 % kT2;
-        const unsigned m = M[bi];
-        unsigned conn, local;
-        bool full;
-        uint64_t mlo, mhi;
-        if (nb_interior(G, c0, c1, c2))
-            border_conn<true, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
-        else
-            border_conn<false, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
-        unsigned covered = 0;
-        if (full && ((conn >> kCentre) & 1u))
-            covered = conn & ~(1u << kCentre); // the centre links all of them
-        while (local & ~covered) {
-            const int q = next_cover(local & ~covered);
-            covered |= bcover(q, conn & ~covered, mlo, mhi, tb);
+        const int h = h0 + lane;
+        unsigned todo = 0;
+        int bi = 0, pb = 0;
+        if (h < cnt) {
+            bi = hard[h];
+            const int r = bi / G.b2;
+            const int c2 = bi - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+            const int a = c0 % kT0, b = c1 % kT1, c = c2 % kT2;
+            const unsigned m = M[bi];
+            unsigned conn, local;
+            bool full;
+            uint64_t mlo, mhi;
+            if (nb_interior(G, c0, c1, c2))
+                border_conn<true, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+            else
+                border_conn<false, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+            unsigned covered = 0;
+            if (full && ((conn >> kCentre) & 1u))
+                covered = conn & ~(1u << kCentre); // the centre links all of them
+            while (local & ~covered) {
+                const int q = next_cover(local & ~covered);
+                covered |= bcover(q, conn & ~covered, mlo, mhi, tb);
+            }
+            while (conn & ~covered) {
+                const unsigned rest = conn & ~covered;
+                const int q = next_cover(rest);
+                todo |= 1u << q;
+                covered |= bcover(q, rest, mlo, mhi, tb);
+            }
+            pb = ld(P + bi);
         }
-        while (conn & ~covered) {
-            const unsigned rest = conn & ~covered;
-            const int q = next_cover(rest);
-            unite(P, bi, bi + nb_d0(q) * G.b1 * G.b2 + nb_d1(q) * G.b2 + nb_d2(q), err);
-            covered |= bcover(q, rest, mlo, mhi, tb);
+        while (__any_sync(0xffffffffu, todo != 0)) {
+            int o = -1;
+            unsigned long long key = ~0ull - (unsigned)lane; // unique for lanes without a target
+            if (todo) {
+                const int q = __ffs(todo) - 1;
+                todo &= todo - 1;
+                o = bi + nb_d0(q) * G.b1 * G.b2 + nb_d1(q) * G.b2 + nb_d2(q);
+                key = ((unsigned long long)(unsigned)pb << 32) | (unsigned)ld(P + o);
+            }
+            const unsigned same = __match_any_sync(0xffffffffu, key);
+            if (o >= 0 && (__ffs(same) - 1) == lane)
+                unite(P, bi, o, err);
         }
     }
 }
