@@ -863,9 +863,20 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
                     for (int h = 0; h < 2; h++) {
                         const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
                         bool fin_ok = mh <= kFinal && x > (h ? big_until1 : big_until0);
-                        if (fin_ok && periodic &&
-                            ((unsigned)((x + 1) * (x + 1)) <= mh || (unsigned)((n - x) * (n - x)) <= mh))
-                            fin_ok = false;
+                        if (fin_ok && periodic) {
+                            const unsigned el = (unsigned)((x + 1) * (x + 1)), er = (unsigned)((n - x) * (n - x));
+                            if (el < mh || er < mh) {
+                                // no solid voxel between x and that line end (it would
+                                // bound the minimum below): the scan runs off the line
+                                if (h)
+                                    need1 |= 1;
+                                else
+                                    need0 |= 1;
+                                continue;
+                            }
+                            if (el == mh || er == mh)
+                                fin_ok = false;
+                        }
                         float val;
                         if (fin_ok) {
                             val = fmul((float)mh, a);
@@ -1018,9 +1029,21 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
                         for (int h = 0; h < 2; h++) {
                             const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
                             bool fin_ok = mh <= kFinal && !sbig[2 * pr + h];
-                            if (fin_ok && periodic &&
-                                ((unsigned)((x + 1) * (x + 1)) <= mh || (unsigned)((n - x) * (n - x)) <= mh))
-                                fin_ok = false;
+                            if (fin_ok && periodic) {
+                                const unsigned el = (unsigned)((x + 1) * (x + 1)),
+                                               er = (unsigned)((n - x) * (n - x));
+                                if (el < mh || er < mh) {
+                                    // the scan would run off the line: flag it directly
+                                    if (h)
+                                        need1 |= 1;
+                                    else
+                                        need0 |= 1;
+                                    sout[(2 * pr + h) * (kRowsTX + 1) + (x - c0)] = kSkip;
+                                    continue;
+                                }
+                                if (el == mh || er == mh)
+                                    fin_ok = false;
+                            }
                             float val;
                             if (fin_ok) {
                                 val = fmul((float)mh, a);
