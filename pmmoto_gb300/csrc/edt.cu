@@ -793,7 +793,6 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
                                                   int seglen)
 {
     constexpr int R = 2 * W + 1; // the window of packed heights
-    static_assert(R % A == 0, "the raw ring's slots must repeat with the window's");
     constexpr unsigned kClamp = 65535u - (unsigned)(W * W) - 1u;
     constexpr unsigned kFinal = (unsigned)((W + 1) * (W + 1));
     const long long nlines = Ls.count();
@@ -838,6 +837,9 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
                 big_until1 = y + W;
             return u0 | (u1 << 16);
         };
+        // win[s] holds position x - W + s; ahead[q] the raw load of position
+        // x + W + 1 + q.  The loop is rolled and the window shifts by register
+        // moves, so the loop body stays small enough for the instruction cache.
         uint32_t win[R];
         float2 ahead[A];
 #pragma unroll
@@ -847,61 +849,60 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
         for (int q = 0; q < A; q++)
             ahead[q] = raw(x0 + W + 1 + q);
         int need0 = 0, need1 = 0;
-        for (int y0 = x0; y0 < x1; y0 += R) {
+#pragma unroll 1
+        for (int x = x0; x < x1; x++) {
+            uint32_t m = win[W];
 #pragma unroll
-            for (int u = 0; u < R; u++) {
-                const int x = y0 + u;
-                if (x < x1) {
-                    uint32_t m = win[(u + W) % R];
-#pragma unroll
-                    for (int d = 1; d <= W; d++) {
-                        const uint32_t dd = (uint32_t)(d * d) * 0x10001u;
-                        m = __viaddmin_u16x2(win[(u + W - d) % R], dd, m);
-                        m = __viaddmin_u16x2(win[(u + W + d) % R], dd, m);
-                    }
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
-                        bool fin_ok = mh <= kFinal && x > (h ? big_until1 : big_until0);
-                        if (fin_ok && periodic) {
-                            const unsigned el = (unsigned)((x + 1) * (x + 1)), er = (unsigned)((n - x) * (n - x));
-                            if (el < mh || er < mh) {
-                                // no solid voxel between x and that line end (it would
-                                // bound the minimum below): the scan runs off the line
-                                if (h)
-                                    need1 |= 1;
-                                else
-                                    need0 |= 1;
-                                continue;
-                            }
-                            if (el == mh || er == mh)
-                                fin_ok = false;
-                        }
-                        float val;
-                        if (fin_ok) {
-                            val = fmul((float)mh, a);
-                        } else {
-                            float best = 0.0f;
-                            int nd = 0;
-                            if (!window_voxel_call(line + h, st, n, x, inv_a, kmax, periodic, &best, &nd)) {
-                                if (h)
-                                    need1 |= nd;
-                                else
-                                    need0 |= nd;
-                                continue;
-                            }
-                            val = fmul(best, a);
-                        }
-                        if (form == PMG_EDT_DIST)
-                            val = __fsqrt_rn(val);
-                        o[x * st + h] = val;
-                    }
-                }
-                // position x + W + 1 enters the window (loaded A outputs ago),
-                // position x + W + 1 + A is loaded
-                win[u] = pack(ahead[u % A], x + W + 1);
-                ahead[u % A] = raw(x + W + 1 + A);
+            for (int d = 1; d <= W; d++) {
+                const uint32_t dd = (uint32_t)(d * d) * 0x10001u;
+                m = __viaddmin_u16x2(win[W - d], dd, m);
+                m = __viaddmin_u16x2(win[W + d], dd, m);
             }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
+                bool fin_ok = mh <= kFinal && x > (h ? big_until1 : big_until0);
+                if (fin_ok && periodic) {
+                    const unsigned el = (unsigned)((x + 1) * (x + 1)), er = (unsigned)((n - x) * (n - x));
+                    if (el < mh || er < mh) {
+                        // no solid voxel between x and that line end (it would
+                        // bound the minimum below): the scan runs off the line
+                        if (h)
+                            need1 |= 1;
+                        else
+                            need0 |= 1;
+                        continue;
+                    }
+                    if (el == mh || er == mh)
+                        fin_ok = false;
+                }
+                float val;
+                if (fin_ok) {
+                    val = fmul((float)mh, a);
+                } else {
+                    float best = 0.0f;
+                    int nd = 0;
+                    if (!window_voxel_call(line + h, st, n, x, inv_a, kmax, periodic, &best, &nd)) {
+                        if (h)
+                            need1 |= nd;
+                        else
+                            need0 |= nd;
+                        continue;
+                    }
+                    val = fmul(best, a);
+                }
+                if (form == PMG_EDT_DIST)
+                    val = __fsqrt_rn(val);
+                o[x * st + h] = val;
+            }
+#pragma unroll
+            for (int s2 = 0; s2 < R - 1; s2++)
+                win[s2] = win[s2 + 1];
+            win[R - 1] = pack(ahead[0], x + W + 1);
+#pragma unroll
+            for (int q = 0; q < A - 1; q++)
+                ahead[q] = ahead[q + 1];
+            ahead[A - 1] = raw(x + W + 1 + A);
         }
         if (need0)
             atomicOr(flag + li, need0);
