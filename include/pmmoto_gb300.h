@@ -350,9 +350,12 @@ int pmg_set_iteration_cap(int32_t cap);
  * depend on them, only speed.  Names: "edt.pair_seg" (positions per thread
  * of the strided line-pair envelope pass, default 256), "edt.pair_ctas" and
  * "edt.rows_ctas" (CTAs per SM of the strided and contiguous line-pair
- * passes, defaults 32 and 16).  value 0 restores the default; values are
- * process-wide and apply to launches that follow.  pmmoto_gb300.tune sets
- * them from its cached measurements.
+ * passes, defaults 32 and 16), "cc.cross_fused" (block labelling's
+ * cross-tile phase as one fused pass, 1, or as a classification pass and a
+ * union pass, 0; default 0).  A negative value restores the default, and so
+ * does 0 for the knobs whose smallest value is 1; values are process-wide
+ * and apply to launches that follow.  pmmoto_gb300.tune sets them from its
+ * cached measurements.
  */
 int pmg_tune_set(const char *name, int32_t value);
 int pmg_tune_get(const char *name, int32_t *value);

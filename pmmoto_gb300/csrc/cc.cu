@@ -1474,6 +1474,77 @@ __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G
     }
 }
 
+// Phases 2a and 2b in one pass: one thread block per tile, border item t on
+// thread t; a border block that needs cross-tile unions collects its targets
+// (as k_bcc_cross_unite does) and its warp unites in rounds, one lane per
+// distinct (block parent, neighbour parent) pair.  Each border block and its
+// neighbours' masks are read once, and no list is written.
+__global__ void __launch_bounds__(512) k_bcc_cross_fused(int *P, const uint8_t *__restrict__ M, BGrid G, int *err,
+                                                         unsigned long long *units)
+{
+    __shared__ BTabs tb;
+    load_btabs(tb);
+    __syncthreads();
+    const int nt1 = (G.b1 + kT1 - 1) / kT1, nt2 = (G.b2 + kT2 - 1) / kT2;
+    const int tile = blockIdx.x;
+    const int ti = tile / (nt1 * nt2), tj = (tile / nt2) % nt1, tk = tile % nt2;
+    const int t = threadIdx.x;
+    if (t >= (kBorder + 31) / 32 * 32)
+        return; // warps without border items
+    const int lane = t & 31;
+    unsigned todo = 0;
+    int bi = 0, pb = 0;
+    if (t < kBorder) {
+        int a, b, c;
+        border_block(t, a, b, c);
+        const int c0 = ti * kT0 + a, c1 = tj * kT1 + b, c2 = tk * kT2 + c;
+        const unsigned m = c0 < G.b0 && c1 < G.b1 && c2 < G.b2 ? M[(c0 * G.b1 + c1) * G.b2 + c2] : 0u;
+        bi = (c0 * G.b1 + c1) * G.b2 + c2;
+        if (m) {
+            unsigned conn, local;
+            bool full;
+            uint64_t mlo, mhi;
+            if (nb_interior(G, c0, c1, c2))
+                border_conn<true, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+            else
+                border_conn<false, false, true>(M, G, bi, c0, c1, c2, a, b, c, m, conn, local, full, mlo, mhi);
+            // in-tile neighbours were united in phase 1, and so was
+            // everything touching them
+            if ((conn & ~local) != 0 && !(full && ((conn >> kCentre) & 1u) && local)) {
+                unsigned covered = 0;
+                if (full && ((conn >> kCentre) & 1u))
+                    covered = conn & ~(1u << kCentre); // the centre links all of them
+                while (local & ~covered) {
+                    const int q = next_cover(local & ~covered);
+                    covered |= bcover(q, conn & ~covered, mlo, mhi, tb);
+                }
+                while (conn & ~covered) {
+                    const unsigned rest = conn & ~covered;
+                    const int q = next_cover(rest);
+                    todo |= 1u << q;
+                    covered |= bcover(q, rest, mlo, mhi, tb);
+                }
+                pb = ld(P + bi);
+            }
+        }
+    }
+    if (units && todo)
+        atomicAdd(units, 1ull);
+    while (__any_sync(0xffffffffu, todo != 0)) {
+        int o = -1;
+        unsigned long long key = ~0ull - (unsigned)lane; // unique for lanes without a target
+        if (todo) {
+            const int q = __ffs(todo) - 1;
+            todo &= todo - 1;
+            o = bi + nb_d0(q) * G.b1 * G.b2 + nb_d1(q) * G.b2 + nb_d2(q);
+            key = ((unsigned long long)(unsigned)pb << 32) | (unsigned)ld(P + o);
+        }
+        const unsigned same = __match_any_sync(0xffffffffu, key);
+        if (o >= 0 && (__ffs(same) - 1) == lane)
+            unite(P, bi, o, err);
+    }
+}
+
 static bool g_btables_ready[64] = {false};
 
 static int ensure_block_tables()
@@ -1725,7 +1796,15 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
         prof_end(ps__, src_bytes(src, n, nb) + (double)nb * 5, st);
     }
     PMG_CHECK_LAUNCH();
-    {
+    if (tune_value(kTuneCcCrossFused)) {
+        const int nt = ((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
+        const int ps__ = prof_begin("k_bcc_cross_fused", st);
+        k_bcc_cross_fused<<<nt, 512, 0, st>>>(P, M, G, err, prof_units(kUnitsCrossUnite));
+        // per border block: its mask and the masks of its 13 earlier
+        // neighbours; two parents per union
+        prof_end(ps__, (double)nt * kBorder * 14, st);
+        PMG_CHECK_LAUNCH();
+    } else {
         const long long border = (long long)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) *
                                  ((G.b2 + kT2 - 1) / kT2) * kBorder;
         // list of the border blocks that need unions, and its length

@@ -82,8 +82,9 @@ static const TuneSpec g_tune_spec[kTuneKnobs] = {
     {"edt.pair_seg", 256, 32, 8192},    // positions per thread of the strided line-pair pass
     {"edt.pair_ctas", 32, 1, 256},      // CTAs per SM of that pass (grid cap)
     {"edt.rows_ctas", 16, 1, 256},      // CTAs per SM of the contiguous line-pair pass
+    {"cc.cross_fused", 0, 0, 1},        // block labelling: one fused cross-tile pass (1) or two (0)
 };
-static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}};
+static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}, {0}};
 
 int tune_value(int knob) { return knob >= 0 && knob < kTuneKnobs ? g_tune[knob].load() : 0; }
 
@@ -280,7 +281,9 @@ extern "C" int pmg_tune_set(const char *name, int32_t value)
         return PMG_EINVAL;
     }
     const pmg::TuneSpec &t = pmg::g_tune_spec[i];
-    if (value == 0)
+    if (value == 0 && t.lo > 0)
+        value = t.def;
+    if (value < 0)
         value = t.def;
     if (value < t.lo || value > t.hi) {
         pmg::set_error("pmg_tune_set: %s = %d outside [%d, %d]", name, value, t.lo, t.hi);

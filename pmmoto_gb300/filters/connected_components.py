@@ -16,7 +16,7 @@ from collections import defaultdict
 import numpy as np
 import torch
 
-from .. import _dev
+from .. import _dev, tune
 from .._lib import check, host_ptr, i64_array, lib
 from ..core.geometry import geo_of
 
@@ -52,6 +52,7 @@ def _img_device(img):
 
 
 def connect_components_device(t: torch.Tensor, g):
+    tune.apply("cc", t.shape)  # tuned launch parameters of this shape class, if any
     labels = torch.empty(t.shape, dtype=torch.int64, device=t.device)
     count = np.zeros(1, dtype=np.int64)
     st = lib().pmg_cc_label(_dev.ptr(t), t.element_size(), _dev.ptr(labels), host_ptr(i64_array(t.shape)),

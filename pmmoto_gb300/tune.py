@@ -28,6 +28,7 @@ import numpy as np
 KNOBS = {
     "edt": {"edt.pair_seg": [128, 256, 512, 1024], "edt.pair_ctas": [8, 16, 32, 64],
             "edt.rows_ctas": [4, 8, 16, 32]},
+    "cc": {"cc.cross_fused": [0, 1]},
     "batch": {"batch.workers": [2, 4, 8, 16]},
 }
 HOST_KNOBS = {"batch.workers": 8}
@@ -92,6 +93,13 @@ def _set_lib(name: str, value: int) -> None:
     from ._lib import check, lib
 
     check(lib().pmg_tune_set(name.encode(), int(value)), "tune")
+
+
+def reset_lib(kernel: str) -> None:
+    """Defaults for every library knob of `kernel`."""
+    for name in KNOBS.get(kernel, {}):
+        if name not in HOST_KNOBS:
+            _set_lib(name, -1)
 
 
 def get_lib(name: str) -> int:
@@ -179,6 +187,32 @@ def tune_edt(shape, periodic=(True, True, True), steps: int = 3, force: bool = F
     cfg = D.edt3d_cfg(periodic)
     res = np.ones(3, np.float32)
     best, timings = _descend("edt", shape, lambda: D.edt3d_device(img, res, cfg, True, out), steps, _set_lib)
+    save_entry(k, best, timings)
+    _applied[k] = best
+    return best
+
+
+def tune_cc(shape, steps: int = 3, force: bool = False) -> dict:
+    """Tune the block labelling for padded periodic volumes of `shape` on a GRF
+    medium (porosity 0.35, sigma 4 voxels); cached per shape class."""
+    import pmmoto_gb300 as P
+
+    from .core.geometry import geo_of
+    from .domain_generation import grf
+    from .filters import connected_components as CC
+
+    k = key("cc", shape)
+    if not force and load_cache().get(k):
+        _applied.pop(k, None)
+        return apply("cc", shape)
+    own = grf.gen_grf_medium(tuple(int(s) - 2 for s in shape))
+    import torch
+
+    idx = [torch.arange(-1, n + 1, device=own.device) % n for n in own.shape]
+    img = own[idx[0]][:, idx[1]][:, :, idx[2]].contiguous()
+    sd = P.initialize(tuple(own.shape), boundary_types=(("periodic", "periodic"),) * 3)
+    geo = geo_of(sd)
+    best, timings = _descend("cc", shape, lambda: CC.connect_components_device(img, geo), steps, _set_lib)
     save_entry(k, best, timings)
     _applied[k] = best
     return best

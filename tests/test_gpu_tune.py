@@ -30,6 +30,30 @@ def test_every_candidate_gives_the_same_bits():
             tune._set_lib(name, 0)
 
 
+@pytest.mark.parametrize("kinds,p", [(("periodic",) * 3, 0.35), (("end", "wall", "periodic"), 0.6),
+                                     (("end",) * 3, 0.8)])
+def test_cross_tile_variants_give_the_same_labels(kinds, p):
+    from pmmoto_gb300 import tune
+    from pmmoto_gb300.core import initialize
+    from pmmoto_gb300.filters import connected_components as C
+
+    vox = (70, 40, 130)
+    bts = tuple((k, k) for k in kinds)
+    sd = initialize(vox, box=tuple((0.0, v / 64) for v in vox), boundary_types=bts)
+    g = O.Geom(vox, boundary_types=bts, box=tuple((0.0, v / 64) for v in vox))
+    rng = np.random.default_rng(7)
+    img = O.update_buffer(g, (rng.random(sd.voxels) < p).astype(np.uint8))
+    want, wn = O.connect_components(img, g)
+    try:
+        for fused in (0, 1):
+            tune._set_lib("cc.cross_fused", fused)
+            lbl, n = C.connect_components(img, sd)
+            np.testing.assert_array_equal(lbl, want)
+            assert n == wn
+    finally:
+        tune.reset_lib("cc")
+
+
 def test_tune_cache_apply_and_override(tmp_path, monkeypatch):
     from pmmoto_gb300 import tune
 

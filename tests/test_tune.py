@@ -42,5 +42,11 @@ def test_library_knob_table():
             assert L.pmg_tune_set(name.encode(), c) == 0
         assert L.pmg_tune_set(name.encode(), 0) == 0  # back to the default
         assert L.pmg_tune_get(name.encode(), ctypes.byref(v)) == 0 and v.value == default
+    assert L.pmg_tune_set(b"cc.cross_fused", 1) == 0
+    assert L.pmg_tune_set(b"cc.cross_fused", 0) == 0
+    assert L.pmg_tune_get(b"cc.cross_fused", ctypes.byref(v)) == 0 and v.value == 0  # 0 is a value here
+    assert L.pmg_tune_set(b"cc.cross_fused", 1) == 0
+    assert L.pmg_tune_set(b"cc.cross_fused", -1) == 0
+    assert L.pmg_tune_get(b"cc.cross_fused", ctypes.byref(v)) == 0 and v.value == 0
     assert L.pmg_tune_set(b"edt.pair_seg", 1) == _lib.PMG_ERANGE
     assert L.pmg_tune_set(b"no.such", 4) == _lib.PMG_EINVAL
