@@ -1090,18 +1090,45 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
     }
 }
 
-__global__ void k_envelope_ends(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
-                                pmg_axis_cfg cfg, int num_hull, int form, const int *__restrict__ flag)
+// Flagged lines, compacted: list[0 .. *count) gets the indices of the lines
+// whose flag is set (in no particular order), so the replay's warps only hold
+// lines with work.
+__global__ void k_flag_list(const int *__restrict__ flag, long long nlines, int *__restrict__ list,
+                            int *__restrict__ count)
 {
-    const long long nlines = Ls.count();
+    const int lane = threadIdx.x & 31;
+    for (long long base = (blockIdx.x * (long long)blockDim.x + threadIdx.x) - lane; base < nlines;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long li = base + lane;
+        const bool f = li < nlines && flag[li] != 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, f);
+        if (!bal)
+            continue;
+        int pos = 0;
+        if (lane == 0)
+            pos = atomicAdd(count, __popc(bal));
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (f)
+            list[pos + __popc(bal & ((1u << lane) - 1u))] = (int)li;
+    }
+}
+
+// list (optional): the flagged lines' indices and their number (*count);
+// without it every line is visited and unflagged ones are skipped.
+__global__ void k_envelope_ends(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
+                                pmg_axis_cfg cfg, int num_hull, int form, const int *__restrict__ flag,
+                                const int *__restrict__ list, const int *__restrict__ count)
+{
+    const long long nlines = list ? (long long)*count : Ls.count();
     extern __shared__ uint32_t smem_bm[];
     const float aniso = fmul(res, res);
     const MorphEpi none{};
     Stack S;
     S.bm = smem_bm + threadIdx.x;
     S.nthr = blockDim.x;
-    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < nlines;
-         li += (long long)gridDim.x * blockDim.x) {
+    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < nlines;
+         it += (long long)gridDim.x * blockDim.x) {
+        const long long li = list ? (long long)list[it] : it;
         const int fl = flag[li];
         if (!fl)
             continue;
@@ -1243,8 +1270,8 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
         // segments of periodic lines (or whole lines) the window kernel flags
         const long long nl = Ls.count();
         int *flag = flag_buf;
-        if (!flag)
-            PMG_TRY(scratch_alloc((void **)&flag, sizeof(int) * (size_t)nl, st));
+        if (!flag) // flags, then room for the compacted list and its count
+            PMG_TRY(scratch_alloc((void **)&flag, sizeof(int) * (size_t)(2 * nl + 1), st));
         // a caller-supplied flag buffer smaller than the line count is used
         // for one block of rows (lines along the first other axis) at a time
         const int rows = flag_buf ? (int)std::min<long long>(Ls.nb1, std::max<long long>(1, flag_cap / Ls.nb2))
@@ -1296,11 +1323,24 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                     s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
             }
             if (s == PMG_OK) {
+                // the library's own flag buffer has room for the compacted list
+                // of flagged lines after the flags; a caller's buffer is used
+                // as it is (every line visited)
+                int *list = flag_buf ? nullptr : flag + nl, *cnt = flag_buf ? nullptr : flag + 2 * nl;
+                if (list) {
+                    s = cudaMemsetAsync(cnt, 0, sizeof(int), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+                    const int ps__ = prof_begin("k_flag_list", st);
+                    if (s == PMG_OK)
+                        k_flag_list<<<grid_for(nc, 256, 152LL * 16), 256, 0, st>>>(flag, nc, list, cnt);
+                    prof_end(ps__, (double)nc * 4, st);
+                }
                 const int ps__ = prof_begin("k_envelope_ends", st);
-                k_envelope_ends<<<grid_for(nc, block, 1LL << 30), block, smem, st>>>(fin, fout, C, res, cfg, num_hull,
-                                                                                    form, flag);
+                if (s == PMG_OK)
+                    k_envelope_ends<<<grid_for(nc, block, 1LL << 30), block, smem, st>>>(
+                        fin, fout, C, res, cfg, num_hull, form, flag, list, cnt);
                 prof_end(ps__, 0.0, st);
-                s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+                if (s == PMG_OK)
+                    s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
             }
         }
         const int s2 = flag_buf ? PMG_OK : scratch_free(flag, st);
