@@ -411,7 +411,7 @@ def run_reference(args):
 
 
 def measure_learned(args):
-    """Learned radius schedule against the dense exact sweep: held-out 512^3
+    """Learned radius schedule against the dense exact sweep: 12 held-out 512^3
     sphere packs of this configuration's generator (seeds the timed curve does
     not use), 64 radii r_max (k + 1) / 64; per pack the dense curve (64 exact
     radii) and the learned curve (schedule network + at most 12 exact radii,
@@ -717,7 +717,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-large", action="store_true", help="skip the 1024^3 EDT + CC measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-schedule measurement")
-    ap.add_argument("--learned-packs", type=int, default=6, help="held-out packs of the learned-schedule leg")
+    ap.add_argument("--learned-packs", type=int, default=12, help="held-out packs of the learned-schedule leg")
     ap.add_argument("--case", default="drainage",
                     choices=["drainage", "edt", "cc", "morph", "select", "batch", "cnn"])
     ap.add_argument("--batch", type=int, default=64, help="samples per training step of the cnn case")
