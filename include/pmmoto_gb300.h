@@ -82,7 +82,9 @@ int pmg_edt3d(const uint8_t *img, float *out, const int64_t shape[3],
  * pool or budget, or a latency-critical loop where a pool allocation could
  * block or fail mid-run.  Same arguments and results as pmg_edt3d; the
  * intermediate volume lives in a fixed 64 MiB array and the per-line flags
- * of the envelope passes in a fixed 4 MiB array, both reserved by the
+ * and deferred voxels of the envelope passes in a fixed 4 MiB array (a line
+ * whose deferred voxels find the array full takes the float envelope
+ * instead: same results, slower), both reserved by the
  * library on every device that loads it (held until the process exits), so
  * volumes are limited to 16,777,216 voxels (256^3); larger ones return
  * PMG_ERANGE with a message.  The first call on a device looks up that
@@ -352,7 +354,12 @@ int pmg_set_iteration_cap(int32_t cap);
  * "edt.rows_ctas" (CTAs per SM of the strided and contiguous line-pair
  * passes, defaults 32 and 16), "cc.cross_fused" (block labelling's
  * cross-tile phase as one fused pass, 1, or as a classification pass and a
- * union pass, 0; default 0).  A negative value restores the default, and so
+ * union pass, 0; default 0), "edt.path" (envelope passes with power-of-two
+ * voxels: windowed with the probed fallback, 0, the exact integer stream, 1,
+ * or the float envelope, 2; default 0), "edt.fallback" and
+ * "edt.fallback_rows" (probe samples, of 8192, that the +-12 window does not
+ * finish, from which a strided or a contiguous windowed pass hands the whole
+ * pass to the float envelope; 0 always, 8193 never; defaults 96 and 2048).  A negative value restores the default, and so
  * does 0 for the knobs whose smallest value is 1; values are process-wide
  * and apply to launches that follow.  pmmoto_gb300.tune sets them from its
  * cached measurements.

@@ -28,6 +28,7 @@
 #include <cmath>
 #include <algorithm>
 #include <cstring>
+#include <cooperative_groups.h>
 
 #include "edt_internal.cuh"
 
@@ -571,9 +572,21 @@ __device__ __forceinline__ void evaluate(Stack &S, const float *line, long long 
     }
 }
 
-__global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
-                           pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me, int redo)
+// A pass whose probe (k_env_probe, below) counted at least `thr` samples the
+// windowed kernels would not finish goes to the float envelope: the windowed
+// kernels return at once and k_envelope takes every line.
+__device__ __forceinline__ bool probe_says_envelope(const int *probe, int thr)
 {
+    return probe && *probe >= thr;
+}
+
+__global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
+                           pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me, int redo,
+                           const int *__restrict__ probe = nullptr, int probe_thr = 0)
+{
+    // behind the windowed kernels: every line, when the probe chose the envelope
+    if (probe && !probe_says_envelope(probe, probe_thr))
+        return;
     const long long nlines = Ls.count();
     extern __shared__ uint32_t smem_bm[];
     const float aniso = fmul(res, res);
@@ -721,8 +734,11 @@ __device__ __forceinline__ bool window_voxel(const float *line, long long st, in
 constexpr int kWinChunk = 64;
 
 __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float a,
-                             float inv_a, int periodic, int form, int *__restrict__ flag)
+                             float inv_a, int periodic, int form, int *__restrict__ flag,
+                             const int *__restrict__ probe, int probe_thr)
 {
+    if (probe_says_envelope(probe, probe_thr))
+        return;
     const long long nlines = Ls.count();
     const LineGeo g0 = line_addr(Ls, 0);
     const int n = g0.n;
@@ -762,18 +778,211 @@ __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ 
     }
 }
 
-// The per-voxel scan as an out-of-line call (the rare slow path of the
-// line-pair kernels: inlining it at every unrolled position would bloat the
-// ring loop).
-__device__ __noinline__ bool window_voxel_call(const float *line, long long st, int n, int x, float inv_a, float kmax,
-                                               int periodic, float *best, int *need)
+// The line-pair kernels' slow path, out of line: window_voxel from the start
+// (t0 = 1), or continued past a window of +-W = t0 - 1 whose exact minimum m0
+// (units of res^2, every height in the window an exact integer) is above
+// (W + 1)^2.  In the second case no solid voxel lies within the window (one
+// would give at most W^2), so the scan from the start would cover the whole
+// window: it runs off a periodic line end there (flag 1), or closes the side
+// of a non-periodic end there, and otherwise continues at distance W + 1 with
+// the best value m0.  Either way the result and the flags are those of
+// window_voxel.  Four distances are loaded per side at a time so that the
+// loads overlap.
+__device__ __forceinline__ bool window_voxel_from(const float *line, long long st, int n, int x, float inv_a,
+                                               float kmax, int periodic, int t0, float m0, float *best_out,
+                                               int *need)
 {
-    float b = 0.0f;
-    int nd = 0;
-    const bool ok = window_voxel(line, st, n, x, inv_a, kmax, periodic, b, nd);
-    *best = b;
-    *need = nd;
-    return ok;
+    float best;
+    bool ldone, rdone;
+    if (t0 <= 1) {
+        const float f = line[x * st];
+        if (f == 0.0f) {
+            *best_out = 0.0f;
+            return true;
+        }
+        best = fmul(f, inv_a);
+        if (best >= kmax) {
+            *need = 2;
+            return false;
+        }
+        t0 = 1;
+        ldone = rdone = false;
+    } else {
+        const int W = t0 - 1;
+        if (periodic && (x + 1 <= W || n - x <= W)) {
+            *need = 1;
+            return false;
+        }
+        best = m0;
+        ldone = !periodic && x + 1 <= W;
+        rdone = !periodic && n - x <= W;
+    }
+    for (int t = t0; (float)(t * t) < best && !(ldone && rdone); t += 4) {
+        float kl[4], kr[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int vl = x - t - q, vr = x + t + q;
+            kl[q] = (!ldone && vl >= 0) ? __ldg(line + vl * st) : 0.0f;
+            kr[q] = (!rdone && vr < n) ? __ldg(line + vr * st) : 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int tq = t + q;
+            const float tt = (float)(tq * tq);
+            if (tt >= best)
+                break;
+            if (tq > kWinMax) {
+                *need = 2;
+                return false;
+            }
+            if (!ldone) {
+                if (x - tq < 0) {
+                    if (periodic) {
+                        *need = 1;
+                        return false;
+                    }
+                    ldone = true;
+                } else {
+                    const float kv = fmul(kl[q], inv_a);
+                    if (kv >= kmax) {
+                        *need = 2;
+                        return false;
+                    }
+                    best = fminf(best, fadd(kv, tt));
+                    ldone = kv == 0.0f;
+                }
+            }
+            if (!rdone) {
+                if (x + tq >= n) {
+                    if (periodic) {
+                        *need = 1;
+                        return false;
+                    }
+                    rdone = true;
+                } else {
+                    const float kv = fmul(kr[q], inv_a);
+                    if (kv >= kmax) {
+                        *need = 2;
+                        return false;
+                    }
+                    best = fminf(best, fadd(kv, tt));
+                    rdone = kv == 0.0f;
+                }
+            }
+            if (ldone && rdone)
+                break;
+        }
+    }
+    *best_out = best;
+    return true;
+}
+
+// Voxels the line-pair kernels do not finish in their window are deferred to
+// k_env_slow: one 64-bit entry each, the line index (<< 32), the position
+// (<< 17), whether the scan continues past the window (<< 16) and the window
+// minimum (low 16 bits).  Appends are aggregated over the lanes that defer at
+// the same step; when the list is full the line is flagged for the whole float
+// envelope instead (a correct, slower result).
+__device__ __forceinline__ unsigned long long slow_entry(long long li, int x, bool resume, unsigned m)
+{
+    return ((unsigned long long)li << 32) | ((unsigned long long)(unsigned)x << 17) |
+           ((unsigned long long)(resume ? 1u : 0u) << 16) | (unsigned long long)(resume ? (m & 0xFFFFu) : 0u);
+}
+
+__device__ __forceinline__ bool slow_push(unsigned long long *list, int *count, int cap, unsigned long long e)
+{
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0)
+        base = atomicAdd(count, (int)g.size());
+    base = g.shfl(base, 0);
+    const int pos = base + (int)g.thread_rank();
+    if (pos >= cap)
+        return false;
+    list[pos] = e;
+    return true;
+}
+
+// The deferred voxels, one thread each: window_voxel_from, then the output or
+// the line's flags (before the flagged lines are listed and replayed).
+template <int W>
+__global__ void __launch_bounds__(256) k_env_slow(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
+                                                  float a, float inv_a, int periodic, int form,
+                                                  int *__restrict__ flag, const unsigned long long *__restrict__ list,
+                                                  const int *__restrict__ count, int cap)
+{
+    const int cnt = min(*count, cap);
+    const int n = line_addr(Ls, 0).n;
+    const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
+        const unsigned long long e = list[it];
+        const long long li = (long long)(e >> 32);
+        const int x = (int)((e >> 17) & 0x7FFFu);
+        const bool resume = (e >> 16) & 1u;
+        const LineGeo g = line_addr(Ls, li);
+        float best = 0.0f;
+        int nd = 0;
+        if (!window_voxel_from(fin + g.base, g.stride, n, x, inv_a, kmax, periodic, resume ? W + 1 : 1,
+                               (float)(unsigned)(e & 0xFFFFu), &best, &nd)) {
+            atomicOr(flag + li, nd);
+            continue;
+        }
+        float val = fmul(best, a);
+        if (form == PMG_EDT_DIST)
+            val = __fsqrt_rn(val);
+        fout[g.base + (long long)x * g.stride] = val;
+    }
+}
+
+// How often the windowed passes would fall back, sampled before a pass:
+// kProbe (line, position) samples spread over the lines; a sample counts when
+// its minimum over the +-W window is above (W + 1)^2 (not final: the per-voxel
+// scan would take it) or the window holds a height that is not an integer
+// below 2^16.  Media with wide pores (sphere packs) fall back at most voxels,
+// and the per-voxel scans cost several times the float envelope's sweep; so
+// when the count reaches the threshold the windowed kernels return at once
+// and the float envelope takes every line of the pass.  The choice is made on
+// the device (no host round trip) and changes no output: both give the
+// reference's values.
+constexpr int kProbe = 8192;
+
+template <int W>
+__global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin, Lines Ls, float inv_a,
+                                                   int *__restrict__ count)
+{
+    const long long nl = Ls.count();
+    if (nl <= 0)
+        return;
+    const int n = line_addr(Ls, 0).n;
+    int c = 0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < kProbe; s += gridDim.x * blockDim.x) {
+        const long long li = (long long)(((unsigned long long)s * (unsigned long long)nl) / kProbe);
+        const int x = (int)(((unsigned)s * 2654435761u) % (unsigned)n);
+        const LineGeo g = line_addr(Ls, li);
+        const float *line = fin + g.base;
+        const long long st = g.stride;
+        float best = fmul(line[x * st], inv_a);
+        bool bad = !(best < 65000.0f && best == truncf(best));
+#pragma unroll
+        for (int d = 1; d <= W; d++) {
+            const float dd = (float)(d * d);
+            if (x - d >= 0) {
+                const float k = fmul(line[(x - d) * st], inv_a);
+                bad |= !(k < 65000.0f && k == truncf(k));
+                best = fminf(best, fadd(k, dd));
+            }
+            if (x + d < n) {
+                const float k = fmul(line[(x + d) * st], inv_a);
+                bad |= !(k < 65000.0f && k == truncf(k));
+                best = fminf(best, fadd(k, dd));
+            }
+        }
+        c += (bad || best > (float)((W + 1) * (W + 1))) ? 1 : 0;
+    }
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && c)
+        atomicAdd(count, c);
 }
 
 // Strided lines, two at a time (adjacent along the contiguous axis, packed
@@ -790,8 +999,12 @@ __device__ __noinline__ bool window_voxel_call(const float *line, long long st, 
 template <int W, int A>
 __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
                                                   float a, float inv_a, int periodic, int form, int *__restrict__ flag,
-                                                  int seglen)
+                                                  int seglen, const int *__restrict__ probe, int probe_thr,
+                                                  unsigned long long *__restrict__ slow, int *__restrict__ slow_count,
+                                                  int slow_cap)
 {
+    if (probe_says_envelope(probe, probe_thr))
+        return;
     constexpr int R = 2 * W + 1; // the window of packed heights
     constexpr unsigned kClamp = 65535u - (unsigned)(W * W) - 1u;
     constexpr unsigned kFinal = (unsigned)((W + 1) * (W + 1));
@@ -861,7 +1074,10 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
-                bool fin_ok = mh <= kFinal && x > (h ? big_until1 : big_until0);
+                // clean: every height in the window is an exact integer below the clamp
+                const bool clean = x > (h ? big_until1 : big_until0);
+                bool fin_ok = mh <= kFinal && clean;
+                const bool resume = mh > kFinal && clean;
                 if (fin_ok && periodic) {
                     const unsigned el = (unsigned)((x + 1) * (x + 1)), er = (unsigned)((n - x) * (n - x));
                     if (el < mh || er < mh) {
@@ -876,21 +1092,17 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
                     if (el == mh || er == mh)
                         fin_ok = false;
                 }
-                float val;
-                if (fin_ok) {
-                    val = fmul((float)mh, a);
-                } else {
-                    float best = 0.0f;
-                    int nd = 0;
-                    if (!window_voxel_call(line + h, st, n, x, inv_a, kmax, periodic, &best, &nd)) {
+                if (!fin_ok) {
+                    // deferred to k_env_slow
+                    if (!slow_push(slow, slow_count, slow_cap, slow_entry(li + h, x, resume, mh))) {
                         if (h)
-                            need1 |= nd;
+                            need1 |= 2;
                         else
-                            need0 |= nd;
-                        continue;
+                            need0 |= 2;
                     }
-                    val = fmul(best, a);
+                    continue;
                 }
+                float val = fmul((float)mh, a);
                 if (form == PMG_EDT_DIST)
                     val = __fsqrt_rn(val);
                 o[x * st + h] = val;
@@ -930,14 +1142,18 @@ constexpr size_t rows_smem_bytes()
 template <int W>
 __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__ fin, float *__restrict__ fout,
                                                        Lines Ls, float a, float inv_a, int periodic, int form,
-                                                       int *__restrict__ flag)
+                                                       int *__restrict__ flag, const int *__restrict__ probe,
+                                                       int probe_thr, unsigned long long *__restrict__ slow,
+                                                       int *__restrict__ slow_count, int slow_cap)
 {
+    if (probe_says_envelope(probe, probe_thr))
+        return;
     constexpr int R = 2 * W + 1;
     constexpr int SPAN = kRowsTX + 2 * W;
     constexpr int SROW = SPAN + 1; // padded word stride of a pair row
     constexpr unsigned kClamp = 65535u - (unsigned)(W * W) - 1u;
     constexpr unsigned kFinal = (unsigned)((W + 1) * (W + 1));
-    constexpr float kSkip = -1.0f; // "left to the end-segment replay"
+    constexpr float kSkip = -1.0f; // "left to k_env_slow or the end-segment replay"
     extern __shared__ uint32_t rows_smem[];
     uint32_t *sin = rows_smem;                                // [32][SROW]
     float *sout = reinterpret_cast<float *>(sin + 32 * SROW); // [64][kRowsTX + 1]
@@ -1029,7 +1245,9 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
 #pragma unroll
                         for (int h = 0; h < 2; h++) {
                             const unsigned mh = h ? (m >> 16) : (m & 0xFFFFu);
-                            bool fin_ok = mh <= kFinal && !sbig[2 * pr + h];
+                            const bool clean = !sbig[2 * pr + h];
+                            bool fin_ok = mh <= kFinal && clean;
+                            const bool resume = mh > kFinal && clean;
                             if (fin_ok && periodic) {
                                 const unsigned el = (unsigned)((x + 1) * (x + 1)),
                                                er = (unsigned)((n - x) * (n - x));
@@ -1045,23 +1263,18 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
                                 if (el == mh || er == mh)
                                     fin_ok = false;
                             }
-                            float val;
-                            if (fin_ok) {
-                                val = fmul((float)mh, a);
-                            } else {
-                                float best = 0.0f;
-                                int nd = 0;
-                                if (!window_voxel_call(fin + rbase + (h ? (long long)n : 0), 1, n, x, inv_a, kmax,
-                                                       periodic, &best, &nd)) {
+                            if (!fin_ok) {
+                                // deferred to k_env_slow
+                                if (!slow_push(slow, slow_count, slow_cap, slow_entry(lia + h, x, resume, mh))) {
                                     if (h)
-                                        need1 |= nd;
+                                        need1 |= 2;
                                     else
-                                        need0 |= nd;
-                                    sout[(2 * pr + h) * (kRowsTX + 1) + (x - c0)] = kSkip;
-                                    continue;
+                                        need0 |= 2;
                                 }
-                                val = fmul(best, a);
+                                sout[(2 * pr + h) * (kRowsTX + 1) + (x - c0)] = kSkip;
+                                continue;
                             }
+                            float val = fmul((float)mh, a);
                             if (form == PMG_EDT_DIST)
                                 val = __fsqrt_rn(val);
                             sout[(2 * pr + h) * (kRowsTX + 1) + (x - c0)] = val;
@@ -1265,20 +1478,43 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     if (smem > 48 * 1024)
         PMG_CUDA(cudaFuncSetAttribute(k_envelope, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    if (form != PMG_EDT_MORPH && window_path_ok(res, n)) {
+    const int path = tune_value(kTuneEdtPath);
+    if (form != PMG_EDT_MORPH && window_path_ok(res, n) && path == 0) {
         // windowed exact minimum everywhere, the float envelope on the end
         // segments of periodic lines (or whole lines) the window kernel flags
         const long long nl = Ls.count();
-        int *flag = flag_buf;
-        if (!flag) // flags, then room for the compacted list and its count
-            PMG_TRY(scratch_alloc((void **)&flag, sizeof(int) * (size_t)(2 * nl + 1), st));
+        // The library's own buffer (ints): flags [0, nl) | the flagged-line
+        // list [nl, 2nl) | its count | the probe's count | the deferred count |
+        // the deferred voxels (8-byte entries).  A caller's buffer of flag_cap
+        // ints: flags in its first half (one block of rows at a time), then
+        // the two counts and the deferred voxels; no flagged-line list.
+        int *flag = flag_buf, *probe = nullptr, *slow_cnt = nullptr;
+        unsigned long long *slow = nullptr;
+        long long fcap = nl, slow_cap = 0;
+        if (!flag_buf) {
+            slow_cap = std::min<long long>(nl * n / 16 + 1024, 1LL << 27);
+            const size_t head = ((sizeof(int) * (size_t)(2 * nl + 3)) + 15) & ~(size_t)15;
+            void *mem = nullptr;
+            PMG_TRY(scratch_alloc(&mem, head + sizeof(unsigned long long) * (size_t)slow_cap, st));
+            flag = (int *)mem;
+            probe = flag + 2 * nl + 1;
+            slow = (unsigned long long *)((char *)mem + head);
+        } else {
+            fcap = flag_cap / 2;
+            probe = flag_buf + fcap;
+            const uintptr_t lo = ((uintptr_t)(probe + 2) + 15) & ~(uintptr_t)15, hi = (uintptr_t)(flag_buf + flag_cap);
+            slow = (unsigned long long *)lo;
+            slow_cap = hi > lo ? (long long)((hi - lo) / sizeof(unsigned long long)) : 0;
+        }
+        slow_cnt = probe + 1;
+        const int probe_thr = tune_value(Ls.ax == 2 ? kTuneEdtFallbackRows : kTuneEdtFallback);
         // a caller-supplied flag buffer smaller than the line count is used
         // for one block of rows (lines along the first other axis) at a time
-        const int rows = flag_buf ? (int)std::min<long long>(Ls.nb1, std::max<long long>(1, flag_cap / Ls.nb2))
+        const int rows = flag_buf ? (int)std::min<long long>(Ls.nb1, std::max<long long>(1, fcap / Ls.nb2))
                                   : Ls.nb1;
         int s = PMG_OK;
-        if (flag_buf && (long long)Ls.nb2 > flag_cap) {
-            set_error("envelope: flag buffer of %lld lines holds less than one row of %d lines", flag_cap, Ls.nb2);
+        if (flag_buf && (long long)Ls.nb2 > fcap) {
+            set_error("envelope: flag buffer of %lld lines holds less than one row of %d lines", fcap, Ls.nb2);
             s = PMG_EINVAL;
         }
         for (int r0 = 0; s == PMG_OK && r0 < Ls.nb1; r0 += rows) {
@@ -1287,6 +1523,13 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
             C.nb1 = std::min(rows, Ls.nb1 - r0);
             const long long nc = C.count();
             s = cudaMemsetAsync(flag, 0, sizeof(int) * (size_t)nc, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            if (s == PMG_OK) // the probe's and the deferred count
+                s = cudaMemsetAsync(probe, 0, 2 * sizeof(int), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            if (s == PMG_OK) {
+                const int ps__ = prof_begin("k_env_probe", st);
+                k_env_probe<12><<<kProbe / 256, 256, 0, st>>>(fin, C, 1.0f / (res * res), probe);
+                prof_end(ps__, 0.0, st);
+            }
             if (s == PMG_OK) {
                 const float a = res * res;
                 const bool contiguous = C.ax == 2;
@@ -1298,7 +1541,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                     const int ps__ = prof_begin("k_env_pair", st);
                     k_env_pair<kPairW, kAhead><<<grid_for(work, 256, 152LL * tune_value(kTuneEdtPairCtas)), 256, 0,
                                                  st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag,
-                                                       seg);
+                                                       seg, probe, probe_thr, slow, slow_cnt, (int)slow_cap);
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else if (contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
                     // row pairs through shared-memory tiles
@@ -1311,16 +1554,26 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                         k_env_pair_rows<kPairW><<<(unsigned)std::min<long long>(
                                                        tiles, 152LL * tune_value(kTuneEdtRowsCtas)),
                                                    256, sm, st>>>(
-                            fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
+                            fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, probe, probe_thr, slow,
+                            slow_cnt, (int)slow_cap);
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else {
                     const int ps__ = prof_begin("k_env_window", st);
                     k_env_window<<<grid_for(contiguous ? nc * 32 : nc * ((n + 63) / 64), 256, 152LL * 32), 256, 0,
-                                   st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag);
+                                   st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, probe,
+                                         probe_thr);
                     prof_end(ps__, (double)nc * n * 8, st);
                 }
                 if (s == PMG_OK)
                     s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+                if (s == PMG_OK && !(C.nb2 & 1) && !(C.b2lo & 1)) {
+                    // the voxels the line-pair kernels deferred
+                    const int ps__ = prof_begin("k_env_slow", st);
+                    k_env_slow<kPairW><<<152 * 8, 256, 0, st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form,
+                                                                 flag, slow, slow_cnt, (int)slow_cap);
+                    prof_end(ps__, 0.0, st);
+                    s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+                }
             }
             if (s == PMG_OK) {
                 // the library's own flag buffer has room for the compacted list
@@ -1342,12 +1595,20 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                 if (s == PMG_OK)
                     s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
             }
+            if (s == PMG_OK) {
+                // the whole pass on the float envelope when the probe chose it
+                const int ps__ = prof_begin("k_envelope[probed]", st);
+                k_envelope<<<grid_for(nc, block, 1LL << 30), block, smem, st>>>(
+                    fin, fout, C, res, cfg, num_hull, form, MorphEpi{}, 0, probe, probe_thr);
+                prof_end(ps__, 0.0, st);
+                s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            }
         }
         const int s2 = flag_buf ? PMG_OK : scratch_free(flag, st);
         return s != PMG_OK ? s : s2;
     }
     int redo = 0;
-    if (exact_path_ok(res, cfg, n)) {
+    if (path != 2 && exact_path_ok(res, cfg, n)) {
         // exact integer streaming pass; lines it cannot finish are redone below
         PMG_TRY(launch_envelope_exact(fin, fout, Ls, res, form, me, st, cap));
         redo = 1;
@@ -1355,7 +1616,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     {
         const int ps__ = prof_begin(redo ? "k_envelope_redo" : "k_envelope", st);
         k_envelope<<<grid_for(Ls.count(), block, redo ? 152LL * 8 : 1LL << 30), block, smem, st>>>(
-            fin, fout, Ls, res, cfg, num_hull, form, me, redo);
+            fin, fout, Ls, res, cfg, num_hull, form, me, redo, nullptr, 0);
         prof_end(ps__, redo ? 0.0 : (double)Ls.count() * n * 4 + (form == PMG_EDT_MORPH ? (double)Ls.count() * me.o2 : (double)Ls.count() * n * 4), st);
     }
     PMG_CHECK_LAUNCH();

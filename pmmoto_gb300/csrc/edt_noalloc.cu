@@ -11,7 +11,8 @@
 //
 // The arrays are file-scope __device__ variables: every GPU that loads this
 // library holds them (64 MiB for the intermediate volume, 4 MiB for the
-// per-line flags of the windowed envelope path) until the process exits.
+// per-line flags and the deferred voxels of the windowed envelope path) until
+// the process exits.
 // Host code may not use an array's name as a device address, so the first
 // call on each device resolves both addresses with cudaGetSymbolAddress
 // while that device is current and caches them.  The cache is not
@@ -26,10 +27,12 @@ namespace pmg {
 // 16 Mi float32 = 64 MiB: volumes of up to 16,777,216 voxels (e.g. 256^3).
 constexpr long long kNoAllocMaxVoxels = 16LL * 1024 * 1024;
 
-// 1 Mi int32 = 4 MiB of per-line flags; an envelope pass with more lines
-// runs in blocks of rows that fit (one row is at most PMG_MAX_LINE lines).
+// 1 Mi int32 = 4 MiB: the first half per-line flags (an envelope pass with
+// more lines runs in blocks of rows that fit; one row is at most PMG_MAX_LINE
+// lines), the second half the voxels the line-pair kernels defer (about 262 K;
+// beyond that a line takes the whole float envelope).
 constexpr long long kNoAllocMaxFlagLines = 1LL << 20;
-static_assert(kNoAllocMaxFlagLines >= PMG_MAX_LINE, "a row of lines must fit the flag array");
+static_assert(kNoAllocMaxFlagLines / 2 >= PMG_MAX_LINE, "a row of lines must fit the flag half");
 
 static __device__ __align__(256) float g_edt_noalloc_scratch[kNoAllocMaxVoxels];
 static __device__ __align__(256) int g_edt_noalloc_flags[kNoAllocMaxFlagLines];

@@ -83,8 +83,11 @@ static const TuneSpec g_tune_spec[kTuneKnobs] = {
     {"edt.pair_ctas", 32, 1, 256},      // CTAs per SM of that pass (grid cap)
     {"edt.rows_ctas", 16, 1, 256},      // CTAs per SM of the contiguous line-pair pass
     {"cc.cross_fused", 0, 0, 1},        // block labelling: one fused cross-tile pass (1) or two (0)
+    {"edt.path", 0, 0, 2},              // envelope passes: windowed (0), exact stream (1), float envelope (2)
+    {"edt.fallback", 96, 0, 8193},      // probe samples (of 8192) from which a strided windowed pass goes to the envelope
+    {"edt.fallback_rows", 2048, 0, 8193}, // the same for the contiguous (row) pass
 };
-static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}, {0}};
+static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}, {0}, {0}, {96}, {2048}};
 
 int tune_value(int knob) { return knob >= 0 && knob < kTuneKnobs ? g_tune[knob].load() : 0; }
 

@@ -30,6 +30,44 @@ def test_every_candidate_gives_the_same_bits():
             tune._set_lib(name, 0)
 
 
+def _wide_pore_media():
+    """Media whose distances run past the windowed passes' +-12 window: a few
+    scattered solid voxels, and solid balls of radius 4-9 at porosity ~0.8."""
+    rng = np.random.default_rng(43)
+    shape = (96, 80, 128)
+    sparse = (rng.random(shape) >= 2e-4).astype(np.uint8)
+    balls = np.ones(shape, np.uint8)
+    idx = np.indices(shape)
+    for _ in range(40):
+        c = rng.random(3) * shape
+        r = rng.uniform(4, 9)
+        balls[((idx - c[:, None, None, None]) ** 2).sum(0) <= r * r] = 0
+    return [sparse, balls]
+
+
+@pytest.mark.parametrize("per", [(True, True, True), (True, False, True), (False, False, False)])
+def test_envelope_paths_agree_on_wide_pores(per):
+    """The windowed passes (with the resumed scan past the window), the same
+    passes handed to the float envelope by the probe, the exact integer
+    stream and the float envelope give the oracle's bits."""
+    from pmmoto_gb300 import tune
+    from pmmoto_gb300.filters import distance as D
+
+    try:
+        for img in _wide_pore_media():
+            want = O.edt3d(img, periodic=per, squared=True)
+            assert want.max() > 14 ** 2  # the scans pass the window
+            for path, thr in ((0, 8193), (0, 0), (1, 8193), (2, 8193)):
+                tune._set_lib("edt.path", path)
+                tune._set_lib("edt.fallback", thr)
+                tune._set_lib("edt.fallback_rows", thr)
+                np.testing.assert_array_equal(D.edt3d(img, periodic=per, squared=True), want,
+                                              err_msg=f"path {path} fallback {thr}")
+    finally:
+        for name in ("edt.path", "edt.fallback", "edt.fallback_rows"):
+            tune._set_lib(name, -1)
+
+
 @pytest.mark.parametrize("kinds,p", [(("periodic",) * 3, 0.35), (("end", "wall", "periodic"), 0.6),
                                      (("end",) * 3, 0.8)])
 def test_cross_tile_variants_give_the_same_labels(kinds, p):
