@@ -359,7 +359,10 @@ int pmg_set_iteration_cap(int32_t cap);
  * or the float envelope, 2; default 0), "edt.fallback" and
  * "edt.fallback_rows" (probe samples, of 8192, that the +-12 window does not
  * finish, from which a strided or a contiguous windowed pass hands the whole
- * pass to the float envelope; 0 always, 8193 never; defaults 96 and 2048).  A negative value restores the default, and so
+ * pass to the float envelope; 0 always, 8193 never; defaults 96 and 2048),
+ * "edt.narrow" and "edt.narrow_rows" (probe samples the +-8 window does not
+ * finish, below which the pass runs the +-8 window instead of the +-12 one;
+ * 0 never; defaults 64 and 32).  A negative value restores the default, and so
  * does 0 for the knobs whose smallest value is 1; values are process-wide
  * and apply to launches that follow.  pmmoto_gb300.tune sets them from its
  * cached measurements.

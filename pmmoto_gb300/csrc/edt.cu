@@ -572,20 +572,34 @@ __device__ __forceinline__ void evaluate(Stack &S, const float *line, long long 
     }
 }
 
-// A pass whose probe (k_env_probe, below) counted at least `thr` samples the
-// windowed kernels would not finish goes to the float envelope: the windowed
-// kernels return at once and k_envelope takes every line.
-__device__ __forceinline__ bool probe_says_envelope(const int *probe, int thr)
+// The choice a windowed pass makes from its probe (k_env_probe, below):
+// count[0] and count[1] are the samples the +-8 and the +-12 windows do not
+// finish.  Choice 0 runs the +-8 line-pair kernels, 1 the +-12 ones, 2 the
+// float envelope on every line; the kernels of the other choices return at
+// once.  Without a probe the +-12 window runs.
+struct Probe {
+    const int *count;
+    int thr8, thr12;
+    __device__ __forceinline__ int choice() const
+    {
+        if (!count)
+            return 1;
+        return count[0] < thr8 ? 0 : (count[1] < thr12 ? 1 : 2);
+    }
+};
+
+template <int W>
+__host__ __device__ constexpr int window_choice()
 {
-    return probe && *probe >= thr;
+    static_assert(W == 8 || W == 12, "windows of +-8 and +-12");
+    return W == 8 ? 0 : 1;
 }
 
 __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
-                           pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me, int redo,
-                           const int *__restrict__ probe = nullptr, int probe_thr = 0)
+                           pmg_axis_cfg cfg, int num_hull, int form, MorphEpi me, int redo, Probe probe)
 {
     // behind the windowed kernels: every line, when the probe chose the envelope
-    if (probe && !probe_says_envelope(probe, probe_thr))
+    if (probe.count && probe.choice() != 2)
         return;
     const long long nlines = Ls.count();
     extern __shared__ uint32_t smem_bm[];
@@ -735,9 +749,9 @@ constexpr int kWinChunk = 64;
 
 __global__ void k_env_window(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float a,
                              float inv_a, int periodic, int form, int *__restrict__ flag,
-                             const int *__restrict__ probe, int probe_thr)
+                             Probe probe)
 {
-    if (probe_says_envelope(probe, probe_thr))
+    if (probe.choice() == 2)
         return;
     const long long nlines = Ls.count();
     const LineGeo g0 = line_addr(Ls, 0);
@@ -906,12 +920,13 @@ __device__ __forceinline__ bool slow_push(unsigned long long *list, int *count, 
 
 // The deferred voxels, one thread each: window_voxel_from, then the output or
 // the line's flags (before the flagged lines are listed and replayed).
-template <int W>
 __global__ void __launch_bounds__(256) k_env_slow(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
                                                   float a, float inv_a, int periodic, int form,
                                                   int *__restrict__ flag, const unsigned long long *__restrict__ list,
-                                                  const int *__restrict__ count, int cap)
+                                                  const int *__restrict__ count, int cap, Probe probe)
 {
+    // the window of the kernel that deferred the voxels
+    const int W = probe.choice() == 0 ? 8 : 12;
     const int cnt = min(*count, cap);
     const int n = line_addr(Ls, 0).n;
     const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
@@ -936,10 +951,10 @@ __global__ void __launch_bounds__(256) k_env_slow(const float *__restrict__ fin,
 }
 
 // How often the windowed passes would fall back, sampled before a pass:
-// kProbe (line, position) samples spread over the lines; a sample counts when
-// its minimum over the +-W window is above (W + 1)^2 (not final: the per-voxel
-// scan would take it) or the window holds a height that is not an integer
-// below 2^16.  Media with wide pores (sphere packs) fall back at most voxels,
+// kProbe (line, position) samples spread over the lines; a sample counts for a
+// window of +-W when its minimum there is above (W + 1)^2 (not final: the
+// per-voxel scan would take it) or the window holds a height that is not an
+// integer below 2^16, for W = 8 and W = 12.  Media with wide pores (sphere packs) fall back at most voxels,
 // and the per-voxel scans cost several times the float envelope's sweep; so
 // when the count reaches the threshold the windowed kernels return at once
 // and the float envelope takes every line of the pass.  The choice is made on
@@ -947,7 +962,6 @@ __global__ void __launch_bounds__(256) k_env_slow(const float *__restrict__ fin,
 // reference's values.
 constexpr int kProbe = 8192;
 
-template <int W>
 __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin, Lines Ls, float inv_a,
                                                    int *__restrict__ count)
 {
@@ -955,7 +969,7 @@ __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin
     if (nl <= 0)
         return;
     const int n = line_addr(Ls, 0).n;
-    int c = 0;
+    int c8 = 0, c12 = 0;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < kProbe; s += gridDim.x * blockDim.x) {
         const long long li = (long long)(((unsigned long long)s * (unsigned long long)nl) / kProbe);
         const int x = (int)(((unsigned)s * 2654435761u) % (unsigned)n);
@@ -965,7 +979,7 @@ __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin
         float best = fmul(line[x * st], inv_a);
         bool bad = !(best < 65000.0f && best == truncf(best));
 #pragma unroll
-        for (int d = 1; d <= W; d++) {
+        for (int d = 1; d <= 12; d++) {
             const float dd = (float)(d * d);
             if (x - d >= 0) {
                 const float k = fmul(line[(x - d) * st], inv_a);
@@ -977,12 +991,19 @@ __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin
                 bad |= !(k < 65000.0f && k == truncf(k));
                 best = fminf(best, fadd(k, dd));
             }
+            if (d == 8)
+                c8 += (bad || best > 81.0f) ? 1 : 0;
         }
-        c += (bad || best > (float)((W + 1) * (W + 1))) ? 1 : 0;
+        c12 += (bad || best > 169.0f) ? 1 : 0;
     }
-    c = __reduce_add_sync(0xffffffffu, c);
-    if ((threadIdx.x & 31) == 0 && c)
-        atomicAdd(count, c);
+    c8 = __reduce_add_sync(0xffffffffu, c8);
+    c12 = __reduce_add_sync(0xffffffffu, c12);
+    if ((threadIdx.x & 31) == 0) {
+        if (c8)
+            atomicAdd(count, c8);
+        if (c12)
+            atomicAdd(count + 1, c12);
+    }
 }
 
 // Strided lines, two at a time (adjacent along the contiguous axis, packed
@@ -999,11 +1020,11 @@ __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin
 template <int W, int A>
 __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls,
                                                   float a, float inv_a, int periodic, int form, int *__restrict__ flag,
-                                                  int seglen, const int *__restrict__ probe, int probe_thr,
+                                                  int seglen, Probe probe,
                                                   unsigned long long *__restrict__ slow, int *__restrict__ slow_count,
                                                   int slow_cap)
 {
-    if (probe_says_envelope(probe, probe_thr))
+    if (probe.choice() != window_choice<W>())
         return;
     constexpr int R = 2 * W + 1; // the window of packed heights
     constexpr unsigned kClamp = 65535u - (unsigned)(W * W) - 1u;
@@ -1142,11 +1163,11 @@ constexpr size_t rows_smem_bytes()
 template <int W>
 __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__ fin, float *__restrict__ fout,
                                                        Lines Ls, float a, float inv_a, int periodic, int form,
-                                                       int *__restrict__ flag, const int *__restrict__ probe,
-                                                       int probe_thr, unsigned long long *__restrict__ slow,
+                                                       int *__restrict__ flag, Probe probe,
+                                                       unsigned long long *__restrict__ slow,
                                                        int *__restrict__ slow_count, int slow_cap)
 {
-    if (probe_says_envelope(probe, probe_thr))
+    if (probe.choice() != window_choice<W>())
         return;
     constexpr int R = 2 * W + 1;
     constexpr int SPAN = kRowsTX + 2 * W;
@@ -1493,7 +1514,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
         long long fcap = nl, slow_cap = 0;
         if (!flag_buf) {
             slow_cap = std::min<long long>(nl * n / 16 + 1024, 1LL << 27);
-            const size_t head = ((sizeof(int) * (size_t)(2 * nl + 3)) + 15) & ~(size_t)15;
+            const size_t head = ((sizeof(int) * (size_t)(2 * nl + 4)) + 15) & ~(size_t)15;
             void *mem = nullptr;
             PMG_TRY(scratch_alloc(&mem, head + sizeof(unsigned long long) * (size_t)slow_cap, st));
             flag = (int *)mem;
@@ -1502,12 +1523,14 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
         } else {
             fcap = flag_cap / 2;
             probe = flag_buf + fcap;
-            const uintptr_t lo = ((uintptr_t)(probe + 2) + 15) & ~(uintptr_t)15, hi = (uintptr_t)(flag_buf + flag_cap);
+            const uintptr_t lo = ((uintptr_t)(probe + 3) + 15) & ~(uintptr_t)15, hi = (uintptr_t)(flag_buf + flag_cap);
             slow = (unsigned long long *)lo;
             slow_cap = hi > lo ? (long long)((hi - lo) / sizeof(unsigned long long)) : 0;
         }
-        slow_cnt = probe + 1;
-        const int probe_thr = tune_value(Ls.ax == 2 ? kTuneEdtFallbackRows : kTuneEdtFallback);
+        slow_cnt = probe + 2;
+        const bool rows_pass = Ls.ax == 2;
+        const Probe pr{probe, tune_value(rows_pass ? kTuneEdtNarrowRows : kTuneEdtNarrow),
+                       tune_value(rows_pass ? kTuneEdtFallbackRows : kTuneEdtFallback)};
         // a caller-supplied flag buffer smaller than the line count is used
         // for one block of rows (lines along the first other axis) at a time
         const int rows = flag_buf ? (int)std::min<long long>(Ls.nb1, std::max<long long>(1, fcap / Ls.nb2))
@@ -1523,45 +1546,53 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
             C.nb1 = std::min(rows, Ls.nb1 - r0);
             const long long nc = C.count();
             s = cudaMemsetAsync(flag, 0, sizeof(int) * (size_t)nc, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-            if (s == PMG_OK) // the probe's and the deferred count
-                s = cudaMemsetAsync(probe, 0, 2 * sizeof(int), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            if (s == PMG_OK) // the probe's two counts and the deferred count
+                s = cudaMemsetAsync(probe, 0, 3 * sizeof(int), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
             if (s == PMG_OK) {
                 const int ps__ = prof_begin("k_env_probe", st);
-                k_env_probe<12><<<kProbe / 256, 256, 0, st>>>(fin, C, 1.0f / (res * res), probe);
+                k_env_probe<<<kProbe / 256, 256, 0, st>>>(fin, C, 1.0f / (res * res), probe);
                 prof_end(ps__, 0.0, st);
             }
             if (s == PMG_OK) {
                 const float a = res * res;
                 const bool contiguous = C.ax == 2;
-                constexpr int kPairW = 12, kAhead = 5;
+                constexpr int kAhead = 5;
                 if (!contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
-                    // line pairs along the contiguous axis (float2 aligned)
+                    // line pairs along the contiguous axis (float2 aligned);
+                    // the +-8 and +-12 kernels both launch, the probe runs one
                     const int seg = tune_value(kTuneEdtPairSeg);
                     const long long work = (nc >> 1) * ((n + seg - 1) / seg);
+                    const unsigned grid = (unsigned)grid_for(work, 256, 152LL * tune_value(kTuneEdtPairCtas));
                     const int ps__ = prof_begin("k_env_pair", st);
-                    k_env_pair<kPairW, kAhead><<<grid_for(work, 256, 152LL * tune_value(kTuneEdtPairCtas)), 256, 0,
-                                                 st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag,
-                                                       seg, probe, probe_thr, slow, slow_cnt, (int)slow_cap);
+                    k_env_pair<8, kAhead><<<grid, 256, 0, st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form,
+                                                                flag, seg, pr, slow, slow_cnt, (int)slow_cap);
+                    k_env_pair<12, kAhead><<<grid, 256, 0, st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0,
+                                                                 form, flag, seg, pr, slow, slow_cnt, (int)slow_cap);
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else if (contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
                     // row pairs through shared-memory tiles
                     const long long tiles = ((nc + 63) / 64) * ((n + kRowsTX - 1) / kRowsTX);
-                    const size_t sm = rows_smem_bytes<kPairW>();
-                    s = cudaFuncSetAttribute(k_env_pair_rows<kPairW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sm) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+                    const unsigned grid = (unsigned)std::min<long long>(tiles, 152LL * tune_value(kTuneEdtRowsCtas));
+                    const size_t sm8 = rows_smem_bytes<8>(), sm12 = rows_smem_bytes<12>();
+                    s = cudaFuncSetAttribute(k_env_pair_rows<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sm8) == cudaSuccess &&
+                                cudaFuncSetAttribute(k_env_pair_rows<12>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)sm12) == cudaSuccess
+                            ? PMG_OK
+                            : PMG_ECUDA;
                     const int ps__ = prof_begin("k_env_pair_rows", st);
-                    if (s == PMG_OK)
-                        k_env_pair_rows<kPairW><<<(unsigned)std::min<long long>(
-                                                       tiles, 152LL * tune_value(kTuneEdtRowsCtas)),
-                                                   256, sm, st>>>(
-                            fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, probe, probe_thr, slow,
-                            slow_cnt, (int)slow_cap);
+                    if (s == PMG_OK) {
+                        k_env_pair_rows<8><<<grid, 256, sm8, st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0,
+                                                                  form, flag, pr, slow, slow_cnt, (int)slow_cap);
+                        k_env_pair_rows<12><<<grid, 256, sm12, st>>>(fin, fout, C, a, 1.0f / a,
+                                                                    cfg.periodic ? 1 : 0, form, flag, pr, slow,
+                                                                    slow_cnt, (int)slow_cap);
+                    }
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else {
                     const int ps__ = prof_begin("k_env_window", st);
                     k_env_window<<<grid_for(contiguous ? nc * 32 : nc * ((n + 63) / 64), 256, 152LL * 32), 256, 0,
-                                   st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, probe,
-                                         probe_thr);
+                                   st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag, pr);
                     prof_end(ps__, (double)nc * n * 8, st);
                 }
                 if (s == PMG_OK)
@@ -1569,8 +1600,8 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                 if (s == PMG_OK && !(C.nb2 & 1) && !(C.b2lo & 1)) {
                     // the voxels the line-pair kernels deferred
                     const int ps__ = prof_begin("k_env_slow", st);
-                    k_env_slow<kPairW><<<152 * 8, 256, 0, st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form,
-                                                                 flag, slow, slow_cnt, (int)slow_cap);
+                    k_env_slow<<<152 * 8, 256, 0, st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0, form, flag,
+                                                        slow, slow_cnt, (int)slow_cap, pr);
                     prof_end(ps__, 0.0, st);
                     s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
                 }
@@ -1599,7 +1630,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                 // the whole pass on the float envelope when the probe chose it
                 const int ps__ = prof_begin("k_envelope[probed]", st);
                 k_envelope<<<grid_for(nc, block, 1LL << 30), block, smem, st>>>(
-                    fin, fout, C, res, cfg, num_hull, form, MorphEpi{}, 0, probe, probe_thr);
+                    fin, fout, C, res, cfg, num_hull, form, MorphEpi{}, 0, pr);
                 prof_end(ps__, 0.0, st);
                 s = cudaGetLastError() == cudaSuccess ? PMG_OK : PMG_ECUDA;
             }
@@ -1616,7 +1647,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     {
         const int ps__ = prof_begin(redo ? "k_envelope_redo" : "k_envelope", st);
         k_envelope<<<grid_for(Ls.count(), block, redo ? 152LL * 8 : 1LL << 30), block, smem, st>>>(
-            fin, fout, Ls, res, cfg, num_hull, form, me, redo, nullptr, 0);
+            fin, fout, Ls, res, cfg, num_hull, form, me, redo, Probe{nullptr, 0, 0});
         prof_end(ps__, redo ? 0.0 : (double)Ls.count() * n * 4 + (form == PMG_EDT_MORPH ? (double)Ls.count() * me.o2 : (double)Ls.count() * n * 4), st);
     }
     PMG_CHECK_LAUNCH();

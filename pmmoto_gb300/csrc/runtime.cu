@@ -86,8 +86,10 @@ static const TuneSpec g_tune_spec[kTuneKnobs] = {
     {"edt.path", 0, 0, 2},              // envelope passes: windowed (0), exact stream (1), float envelope (2)
     {"edt.fallback", 96, 0, 8193},      // probe samples (of 8192) from which a strided windowed pass goes to the envelope
     {"edt.fallback_rows", 2048, 0, 8193}, // the same for the contiguous (row) pass
+    {"edt.narrow", 64, 0, 8193},        // probe samples (of 8192) below which a strided pass takes the +-8 window
+    {"edt.narrow_rows", 32, 0, 8193},   // the same for the contiguous (row) pass
 };
-static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}, {0}, {0}, {96}, {2048}};
+static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}, {0}, {0}, {96}, {2048}, {64}, {32}};
 
 int tune_value(int knob) { return knob >= 0 && knob < kTuneKnobs ? g_tune[knob].load() : 0; }
 
