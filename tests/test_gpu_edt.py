@@ -95,6 +95,29 @@ def test_edt3d_line_pairs_vs_oracle(D, seed):
         np.testing.assert_array_equal(got, want)
 
 
+@pytest.mark.parametrize("seed", range(12))
+def test_edt3d_pass0_quads_vs_oracle(D, seed):
+    """Pass 0 on four lines per thread (the last extent a multiple of 4):
+    zeros, restarts between adjacent voxels of different values, periodic
+    correctors, long runs without a zero; power-of-two and other voxel
+    sizes."""
+    rng = np.random.default_rng(1200 + seed)
+    shape = [(64, 48, 40), (33, 20, 128), (130, 7, 12), (5, 64, 4)][seed % 4]
+    p0 = float([0.5, 0.1, 0.01, 0.9, 0.3, 0.0][seed % 6])
+    img = (rng.random(shape) >= p0).astype(np.uint8)
+    if seed % 3 == 1:
+        img = np.where(img > 0, rng.integers(1, 4, shape), 0).astype(np.uint8)
+    if seed % 6 == 5:
+        img[0] = 0  # lines along axis 0 starting and ending on zeros (smallest correctors)
+        img[-1] = 0
+    per = [(True, True, True), (False, False, False), (True, False, True)][seed % 3]
+    res = [(1.0, 1.0, 1.0), (0.5, 0.5, 0.5), (1 / 64, 1 / 64, 1 / 64), (0.3, 0.3, 0.3)][seed % 4]
+    for squared in (True, False):
+        got = D.edt3d(img, periodic=per, resolution=res, squared=squared)
+        want = O.edt3d(img, periodic=per, resolution=res, squared=squared)
+        np.testing.assert_array_equal(got, want)
+
+
 def test_edt_subdomain_golden(D, golden, golden_meta):
     from tests._helpers import geom_from_meta
     for ci, case in enumerate(golden_meta["sub_cases"]):
