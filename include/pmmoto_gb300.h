@@ -362,7 +362,10 @@ int pmg_set_iteration_cap(int32_t cap);
  * pass to the float envelope; 0 always, 8193 never; defaults 96 and 2048),
  * "edt.narrow" and "edt.narrow_rows" (probe samples the +-8 window does not
  * finish, below which the pass runs the +-8 window instead of the +-12 one;
- * 0 never; defaults 64 and 32).  A negative value restores the default, and so
+ * 0 never; defaults 64 and 32), "cc.seam_batched" (periodic merge: the
+ * seams of all periodic features deduplicated in one sort, 1, or one
+ * feature at a time, 0; default 1; one at a time is also taken when labels
+ * need more than 29 bits).  A negative value restores the default, and so
  * does 0 for the knobs whose smallest value is 1; values are process-wide
  * and apply to launches that follow.  pmmoto_gb300.tune sets them from its
  * cached measurements.

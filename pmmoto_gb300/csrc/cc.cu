@@ -372,10 +372,14 @@ struct LabImg {
     }
 };
 
+// keys[row0 + r] = fkey | label << lbits | twin label (fkey = 0, lbits = 32
+// for one feature alone), idx[row0 + r] = row0 + r.
 template <class Src>
-__global__ void k_seam_pairs(Src src, Box a0, Box a1, Box b0, Box b1, uint64_t *__restrict__ keys,
-                             uint32_t *__restrict__ idx)
+__global__ void k_seam_pairs(Src src, Box a0, Box a1, Box b0, Box b1, uint64_t fkey, int lbits, long long row0,
+                             uint64_t *__restrict__ keys, uint32_t *__restrict__ idx)
 {
+    keys += row0;
+    idx += row0;
     const long long n0 = a0.size(), n = n0 + a1.size();
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
          r += (long long)gridDim.x * blockDim.x) {
@@ -388,8 +392,8 @@ __global__ void k_seam_pairs(Src src, Box a0, Box a1, Box b0, Box b1, uint64_t *
         const long long bk = q % wb, bj = (q / wb) % hb, bi = q / (wb * hb);
         const uint64_t la = src.at(A.lo[0] + ai, A.lo[1] + aj, A.lo[2] + ak);
         const uint64_t lb = src.at(B.lo[0] + bi, B.lo[1] + bj, B.lo[2] + bk);
-        keys[r] = (la << 32) | lb;
-        idx[r] = (uint32_t)r;
+        keys[r] = fkey | (la << lbits) | lb;
+        idx[r] = (uint32_t)(row0 + r);
     }
 }
 
@@ -626,55 +630,24 @@ static std::vector<std::array<int, 3>> feature_order()
     return all;
 }
 
-// Periodic renumbering of the reference (connect_subdomain_boundaries on one
-// rank): boundary pairs of every periodic feature, deduplicated on the device
-// in first-occurrence order, replayed through the same hash-set container the
-// reference uses so its iteration order is reproduced, then the dict / stack
-// merge of merge_matched_voxels and local_to_global_labeling on the host
-// (boundary data only), and one relabel pass on the device.
-// The labels come from src; with lut_out the relabelling table (indexed by
-// the local label) is handed back instead of being applied to L.
+// One periodic feature's seam: its own and neighbour slabs and the opposite
+// feature's neighbour and own slabs they pair with, row by row.
+struct SeamFeature {
+    Box own, nb, oown, onb;
+    long long rows;
+};
+
+// Every feature's distinct seam keys (label << 32 | twin label) in order of
+// first row, one feature at a time: keys in row order, stable radix sort,
+// first row of every distinct key.  Two host round trips per feature.
 template <class Src>
-static int periodic_renumber(const Src &src, uint64_t *L, const int64_t *shape, const int32_t *bc,
-                             const int32_t *pad, int64_t count, int64_t *out_count, cudaStream_t st,
-                             uint64_t **lut_out = nullptr)
+static int seam_keys_each(const Src &src, const std::vector<SeamFeature> &fs,
+                          std::vector<std::vector<uint64_t>> &out, cudaStream_t st)
 {
-    const long long n = shape[0] * shape[1] * shape[2];
-    auto feats = feature_order();
-    // insertion-ordered map (key label -> neighbour list), as a Python dict
-    std::vector<uint64_t> keys_order;
-    std::vector<std::vector<uint64_t>> nbrs;
-    std::unordered_map<uint64_t, long long> key_pos;
-    for (auto &f : feats) {
-        int fid[3] = {f[0], f[1], f[2]};
-        bool has_nb = true;
-        int kind = PMG_BC_PERIODIC;
-        for (int d = 0; d < 3; d++) {
-            if (fid[d] == 0)
-                continue;
-            const int b = bc[2 * d + (fid[d] > 0 ? 1 : 0)];
-            if (b != PMG_BC_PERIODIC)
-                has_nb = false;
-            if (b == PMG_BC_END)
-                kind = PMG_BC_END;
-            else if (b == PMG_BC_WALL && kind != PMG_BC_END)
-                kind = PMG_BC_WALL;
-        }
-        if (!has_nb)
-            continue;
-        int opp[3] = {-fid[0], -fid[1], -fid[2]};
-        Box own, nb, oown, onb;
-        feature_slabs(fid, kind, shape, pad, own, nb);
-        feature_slabs(opp, kind, shape, pad, oown, onb);
-        const long long rows = own.size() + nb.size();
-        if (rows == 0)
-            continue;
-        if (own.size() != onb.size() || nb.size() != oown.size()) {
-            set_error("periodic merge: mismatched feature slabs");
-            return PMG_EINVAL;
-        }
-        // device: keys in row order, stable radix sort by key, first row of
-        // every distinct key
+    out.assign(fs.size(), {});
+    for (size_t fi = 0; fi < fs.size(); fi++) {
+        const SeamFeature &f = fs[fi];
+        const long long rows = f.rows;
         uint64_t *d_k = nullptr, *d_k2 = nullptr, *d_k3 = nullptr;
         uint32_t *d_i = nullptr, *d_i2 = nullptr;
         uint8_t *d_f = nullptr;
@@ -688,7 +661,8 @@ static int periodic_renumber(const Src &src, uint64_t *L, const int64_t *shape, 
         PMG_TRY(scratch_alloc((void **)&d_nsel, 2 * sizeof(int), st));
         {
             const int ps__ = prof_begin("k_seam_pairs", st);
-            k_seam_pairs<Src><<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(src, own, nb, onb, oown, d_k, d_i);
+            k_seam_pairs<Src><<<grid_for(rows, 256, 1LL << 30), 256, 0, st>>>(src, f.own, f.nb, f.onb, f.oown, 0ull,
+                                                                            32, 0, d_k, d_i);
             prof_end(ps__, (double)rows * 28, st);
         }
         PMG_CHECK_LAUNCH();
@@ -718,24 +692,181 @@ static int periodic_renumber(const Src &src, uint64_t *L, const int64_t *shape, 
             PMG_CUDA(cudaMemcpyAsync(dkeys.data(), d_k3, (size_t)nsel * 8, cudaMemcpyDeviceToHost, st));
         }
         PMG_CUDA(cudaStreamSynchronize(st));
-        PMG_TRY(scratch_free(d_t, st));
-        PMG_TRY(scratch_free(d_k, st));
-        PMG_TRY(scratch_free(d_k2, st));
-        PMG_TRY(scratch_free(d_k3, st));
-        PMG_TRY(scratch_free(d_i, st));
-        PMG_TRY(scratch_free(d_i2, st));
-        PMG_TRY(scratch_free(d_f, st));
-        PMG_TRY(scratch_free(d_nsel, st));
+        for (void *q : {(void *)d_t, (void *)d_k, (void *)d_k2, (void *)d_k3, (void *)d_i, (void *)d_i2, (void *)d_f,
+                        (void *)d_nsel})
+            PMG_TRY(scratch_free(q, st));
         std::vector<size_t> order((size_t)nsel);
         for (size_t q = 0; q < order.size(); q++)
             order[q] = q;
         std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return first[x] < first[y]; });
+        for (size_t q : order)
+            out[fi].push_back(dkeys[q]);
+    }
+    return PMG_OK;
+}
+
+// The same for all features at once, when labels fit `lbits` bits with
+// 2 lbits + 5 <= 64: keys (feature << 2 lbits | label << lbits | twin label)
+// of every feature in one array, one stable radix sort over those bits, the
+// first row of every distinct key; two host round trips in all.  Rows of a
+// feature are consecutive and in its row order, so the first row of a key is
+// its first occurrence in that feature, as above.
+template <class Src>
+static int seam_keys_batched(const Src &src, const std::vector<SeamFeature> &fs, int lbits,
+                             std::vector<std::vector<uint64_t>> &out, cudaStream_t st)
+{
+    out.assign(fs.size(), {});
+    long long T = 0;
+    for (auto &f : fs)
+        T += f.rows;
+    if (T == 0)
+        return PMG_OK;
+    if (T >= (1LL << 31)) {
+        set_error("periodic merge: %lld seam rows", T);
+        return PMG_ERANGE;
+    }
+    uint64_t *d_k = nullptr, *d_k2 = nullptr, *d_k3 = nullptr;
+    uint32_t *d_i = nullptr, *d_i2 = nullptr;
+    uint8_t *d_f = nullptr;
+    int *d_nsel = nullptr;
+    PMG_TRY(scratch_alloc((void **)&d_k, T * 8, st));
+    PMG_TRY(scratch_alloc((void **)&d_k2, T * 8, st));
+    PMG_TRY(scratch_alloc((void **)&d_k3, T * 8, st));
+    PMG_TRY(scratch_alloc((void **)&d_i, T * 4, st));
+    PMG_TRY(scratch_alloc((void **)&d_i2, T * 4, st));
+    PMG_TRY(scratch_alloc((void **)&d_f, T, st));
+    PMG_TRY(scratch_alloc((void **)&d_nsel, 2 * sizeof(int), st));
+    {
+        const int ps__ = prof_begin("k_seam_pairs", st);
+        long long row0 = 0;
+        for (size_t fi = 0; fi < fs.size(); fi++) {
+            const SeamFeature &f = fs[fi];
+            k_seam_pairs<Src><<<grid_for(f.rows, 256, 1LL << 30), 256, 0, st>>>(
+                src, f.own, f.nb, f.onb, f.oown, (uint64_t)fi << (2 * lbits), lbits, row0, d_k, d_i);
+            row0 += f.rows;
+        }
+        prof_end(ps__, (double)T * 28, st);
+    }
+    PMG_CHECK_LAUNCH();
+    const int nbits = 2 * lbits + 5;
+    size_t tb = 0, tb2 = 0, tb3 = 0;
+    PMG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, d_k, d_k2, d_i, d_i2, (int)T, 0, nbits, st));
+    PMG_CUDA(cub::DeviceSelect::Flagged(nullptr, tb2, d_i2, d_f, d_i, d_nsel, (int)T, st));
+    PMG_CUDA(cub::DeviceSelect::Flagged(nullptr, tb3, d_k2, d_f, d_k3, d_nsel + 1, (int)T, st));
+    size_t tbs = std::max(tb, std::max(tb2, tb3));
+    void *d_t = nullptr;
+    PMG_TRY(scratch_alloc(&d_t, tbs, st));
+    PMG_CUDA(cub::DeviceRadixSort::SortPairs(d_t, tbs, d_k, d_k2, d_i, d_i2, (int)T, 0, nbits, st));
+    {
+        const int ps__ = prof_begin("k_head_flags", st);
+        k_head_flags<<<grid_for(T, 256, 1LL << 30), 256, 0, st>>>(d_k2, T, d_f);
+        prof_end(ps__, (double)T * 9, st);
+    }
+    PMG_CHECK_LAUNCH();
+    PMG_CUDA(cub::DeviceSelect::Flagged(d_t, tbs, d_i2, d_f, d_i, d_nsel, (int)T, st));
+    PMG_CUDA(cub::DeviceSelect::Flagged(d_t, tbs, d_k2, d_f, d_k3, d_nsel + 1, (int)T, st));
+    int nsel = 0;
+    PMG_CUDA(cudaMemcpyAsync(&nsel, d_nsel, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PMG_CUDA(cudaStreamSynchronize(st));
+    std::vector<uint32_t> first((size_t)nsel);
+    std::vector<uint64_t> dkeys((size_t)nsel);
+    if (nsel > 0) {
+        PMG_CUDA(cudaMemcpyAsync(first.data(), d_i, (size_t)nsel * 4, cudaMemcpyDeviceToHost, st));
+        PMG_CUDA(cudaMemcpyAsync(dkeys.data(), d_k3, (size_t)nsel * 8, cudaMemcpyDeviceToHost, st));
+    }
+    PMG_CUDA(cudaStreamSynchronize(st));
+    for (void *q : {(void *)d_t, (void *)d_k, (void *)d_k2, (void *)d_k3, (void *)d_i, (void *)d_i2, (void *)d_f,
+                    (void *)d_nsel})
+        PMG_TRY(scratch_free(q, st));
+    // entries come sorted by feature: split, then first-row order per feature
+    const uint64_t mask = (1ull << lbits) - 1ull;
+    size_t q0 = 0;
+    while (q0 < (size_t)nsel) {
+        const size_t fi = (size_t)(dkeys[q0] >> (2 * lbits));
+        size_t q1 = q0;
+        while (q1 < (size_t)nsel && (size_t)(dkeys[q1] >> (2 * lbits)) == fi)
+            q1++;
+        if (fi >= fs.size()) {
+            set_error("periodic merge: bad seam key");
+            return PMG_EINVAL;
+        }
+        std::vector<size_t> order;
+        for (size_t q = q0; q < q1; q++)
+            order.push_back(q);
+        std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return first[x] < first[y]; });
+        for (size_t q : order)
+            out[fi].push_back((((dkeys[q] >> lbits) & mask) << 32) | (dkeys[q] & mask));
+        q0 = q1;
+    }
+    return PMG_OK;
+}
+
+// Periodic renumbering of the reference (connect_subdomain_boundaries on one
+// rank): boundary pairs of every periodic feature, deduplicated on the device
+// in first-occurrence order, replayed through the same hash-set container the
+// reference uses so its iteration order is reproduced, then the dict / stack
+// merge of merge_matched_voxels and local_to_global_labeling on the host
+// (boundary data only), and one relabel pass on the device.
+// The labels come from src; with lut_out the relabelling table (indexed by
+// the local label) is handed back instead of being applied to L.
+template <class Src>
+static int periodic_renumber(const Src &src, uint64_t *L, const int64_t *shape, const int32_t *bc,
+                             const int32_t *pad, int64_t count, int64_t *out_count, cudaStream_t st,
+                             uint64_t **lut_out = nullptr)
+{
+    const long long n = shape[0] * shape[1] * shape[2];
+    auto feats = feature_order();
+    std::vector<SeamFeature> fs;
+    for (auto &f : feats) {
+        int fid[3] = {f[0], f[1], f[2]};
+        bool has_nb = true;
+        int kind = PMG_BC_PERIODIC;
+        for (int d = 0; d < 3; d++) {
+            if (fid[d] == 0)
+                continue;
+            const int b = bc[2 * d + (fid[d] > 0 ? 1 : 0)];
+            if (b != PMG_BC_PERIODIC)
+                has_nb = false;
+            if (b == PMG_BC_END)
+                kind = PMG_BC_END;
+            else if (b == PMG_BC_WALL && kind != PMG_BC_END)
+                kind = PMG_BC_WALL;
+        }
+        if (!has_nb)
+            continue;
+        int opp[3] = {-fid[0], -fid[1], -fid[2]};
+        SeamFeature sf;
+        feature_slabs(fid, kind, shape, pad, sf.own, sf.nb);
+        feature_slabs(opp, kind, shape, pad, sf.oown, sf.onb);
+        sf.rows = sf.own.size() + sf.nb.size();
+        if (sf.rows == 0)
+            continue;
+        if (sf.own.size() != sf.onb.size() || sf.nb.size() != sf.oown.size()) {
+            set_error("periodic merge: mismatched feature slabs");
+            return PMG_EINVAL;
+        }
+        fs.push_back(sf);
+    }
+    // labels (0 .. count) in lbits bits
+    int lbits = 1;
+    while (lbits < 40 && ((uint64_t)count >> lbits) != 0)
+        lbits++;
+    std::vector<std::vector<uint64_t>> seam;
+    if (2 * lbits + 5 <= 64 && fs.size() <= 32 && tune_value(kTuneCcSeamBatched))
+        PMG_TRY(seam_keys_batched(src, fs, lbits, seam, st));
+    else
+        PMG_TRY(seam_keys_each(src, fs, seam, st));
+    // insertion-ordered map (key label -> neighbour list), as a Python dict
+    std::vector<uint64_t> keys_order;
+    std::vector<std::vector<uint64_t>> nbrs;
+    std::unordered_map<uint64_t, long long> key_pos;
+    for (auto &keys : seam) {
         // unique_pairs (_voxels.hpp:106-125): the same container fed the same
         // sequence of first insertions iterates in the same order (repeated
         // keys are no-ops)
         std::unordered_set<unsigned long> uset;
-        for (size_t q : order)
-            uset.insert((unsigned long)dkeys[q]);
+        for (uint64_t k : keys)
+            uset.insert((unsigned long)k);
         for (unsigned long e : uset) {
             const uint64_t a = e >> 32, b = e & 0xFFFFFFFFul;
             if (a == 0 || b == 0)

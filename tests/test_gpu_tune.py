@@ -71,7 +71,7 @@ def test_envelope_paths_agree_on_wide_pores(per):
 
 @pytest.mark.parametrize("kinds,p", [(("periodic",) * 3, 0.35), (("end", "wall", "periodic"), 0.6),
                                      (("end",) * 3, 0.8)])
-def test_cross_tile_variants_give_the_same_labels(kinds, p):
+def test_cross_tile_and_seam_variants_give_the_same_labels(kinds, p):
     from pmmoto_gb300 import tune
     from pmmoto_gb300.core import initialize
     from pmmoto_gb300.filters import connected_components as C
@@ -84,13 +84,15 @@ def test_cross_tile_variants_give_the_same_labels(kinds, p):
     img = O.update_buffer(g, (rng.random(sd.voxels) < p).astype(np.uint8))
     want, wn = O.connect_components(img, g)
     try:
-        for fused in (0, 1):
+        for fused, batched in ((0, 1), (1, 1), (0, 0)):
             tune._set_lib("cc.cross_fused", fused)
+            tune._set_lib("cc.seam_batched", batched)
             lbl, n = C.connect_components(img, sd)
             np.testing.assert_array_equal(lbl, want)
             assert n == wn
     finally:
         tune.reset_lib("cc")
+        tune._set_lib("cc.seam_batched", -1)
 
 
 def test_tune_cache_apply_and_override(tmp_path, monkeypatch):
