@@ -1105,9 +1105,45 @@ namespace pmg {
 // neighbouring blocks are connected exactly when each has a foreground voxel in
 // the part of the block that touches the other (a face, an edge or a corner):
 // every voxel of one touching part is 26-adjacent to every voxel of the other.
+// floor(n / d) of a 32-bit n by one multiplication (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", 1994: the
+// round-up multiplier m = floor(2^32 (2^l - d) / d) + 1, l = ceil(log2 d),
+// with the add-and-halve fix-up), exact for every n and d >= 1
+struct FastDiv {
+    unsigned m;
+    int s1, s2;
+};
+
+static inline FastDiv fastdiv_of(unsigned d)
+{
+    int l = 0;
+    while (l < 32 && (1ull << l) < d)
+        l++;
+    FastDiv f;
+    f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1ull);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 1 ? l - 1 : 0;
+    return f;
+}
+
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv &f)
+{
+    const unsigned t = __umulhi(f.m, n);
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
 struct BGrid {
     int s0, s1, s2;    // voxel shape
     int b0, b1, b2;    // block shape
+    FastDiv q2, q1;    // division by b2 and by b1
+    // block index -> (c0, c1, c2)
+    __device__ __forceinline__ void coords(int b, int &c0, int &c1, int &c2) const
+    {
+        const int r = (int)fdiv((unsigned)b, q2);
+        c2 = b - r * b2;
+        c0 = (int)fdiv((unsigned)r, q1);
+        c1 = r - c0 * b1;
+    }
 };
 
 __device__ __forceinline__ bool fg_of(uint8_t v, int fgval) { return fgval >= 0 ? v == fgval : v != 0; }
@@ -1563,8 +1599,8 @@ __global__ void k_bcc_cross_unite(int *P, const uint8_t *__restrict__ M, BGrid G
         int bi = 0, pb = 0;
         if (h < cnt) {
             bi = hard[h];
-            const int r = bi / G.b2;
-            const int c2 = bi - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+            int c2, c0, c1;
+            G.coords(bi, c0, c1, c2);
             const int a = c0 % kT0, b = c1 % kT1, c = c2 % kT2;
             const unsigned m = M[bi];
             unsigned conn, local;
@@ -1831,10 +1867,8 @@ __global__ void k_bcc_select(const uint8_t *__restrict__ M, int *P, const uint8_
     const int nb = G.b0 * G.b1 * G.b2;
     unsigned int cnt = 0; // kept voxels (mask bits exist only for voxels inside the volume)
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
-        const int r = b / G.b2;
-        const int c2 = b - r * G.b2;
-        const int c0 = r / G.b1;
-        const int c1 = r - c0 * G.b1;
+        int c0, c1, c2;
+        G.coords(b, c0, c1, c2);
         unsigned m = M[b];
         if (m) {
             // the root, and the parent flattened to it
@@ -1904,6 +1938,8 @@ static BGrid bgrid_of(const int64_t *shape)
     G.b0 = (G.s0 + 1) / 2;
     G.b1 = (G.s1 + 1) / 2;
     G.b2 = (G.s2 + 1) / 2;
+    G.q2 = fastdiv_of((unsigned)G.b2);
+    G.q1 = fastdiv_of((unsigned)G.b1);
     return G;
 }
 
@@ -2123,8 +2159,8 @@ __global__ void k_grow_masks(Src src, uint8_t *__restrict__ M, int *__restrict__
         bool changed = false;
         if (b < nb) {
             // the old mask and the source are loaded independently
-            const int r = b / G.b2;
-            const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+            int c2, c0, c1;
+            G.coords(b, c0, c1, c2);
             const unsigned old = M[b];
             const unsigned m = block_mask(src, G, c0, c1, c2);
             if (m != old) {
@@ -2176,8 +2212,8 @@ __global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, con
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long it = warp; it < cnt; it += nwarps) {
         const int b = list[it];
-        const int r = b / G.b2;
-        const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+        int c2, c0, c1;
+        G.coords(b, c0, c1, c2);
         const unsigned m = M[b];
         const int pb = ld(P + b);
         const int a0 = c0 + d0, a1 = c1 + d1, a2 = c2 + d2;
@@ -2238,8 +2274,8 @@ __global__ void k_grow_apply(Src src, uint8_t *__restrict__ M, int *__restrict__
         atomicAdd(units, (unsigned long long)cnt);
     for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
         const int b = list[a + it];
-        const int r = b / G.b2;
-        const int c2 = b - r * G.b2, c0 = r / G.b1, c1 = r - (r / G.b1) * G.b1;
+        int c2, c0, c1;
+        G.coords(b, c0, c1, c2);
         const unsigned old = M[b];
         const unsigned m = block_mask(src, G, c0, c1, c2);
         if (old & ~m)
@@ -2395,10 +2431,8 @@ __global__ void k_grow_pair_select(const uint8_t *__restrict__ MA, int *PA, cons
             const int b = bb[q];
             if (b >= nb)
                 continue;
-            const int r = b / G.b2;
-            const int c2 = b - r * G.b2;
-            const int c0 = r / G.b1;
-            const int c1 = r - c0 * G.b1;
+            int c0, c1, c2;
+            G.coords(b, c0, c1, c2);
             unsigned mm = ka[q] & 1u ? m[q] : 0u;
             const unsigned keepB = kb[q] & 1u ? mb[q] : 0u;
             cnt += __popc(mm);
@@ -2516,10 +2550,9 @@ __global__ void k_step_count(const uint8_t *__restrict__ S, BGrid G, int nsteps,
     __syncthreads();
     const int nb = G.b0 * G.b1 * G.b2;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
-        const int r = b / G.b2;
-        int nd;
-        const unsigned long long d =
-            distinct_steps(block_steps(S, G, r / G.b1, r - (r / G.b1) * G.b1, b - r * G.b2), nsteps, nd);
+        int c0, c1, c2, nd;
+        G.coords(b, c0, c1, c2);
+        const unsigned long long d = distinct_steps(block_steps(S, G, c0, c1, c2), nsteps, nd);
         for (int e = 0; e < nd; e++)
             atomicAdd(&hist[(d >> (8 * e)) & 0xffu], 1);
     }
@@ -2546,8 +2579,9 @@ __global__ void k_step_scatter(const uint8_t *__restrict__ S, BGrid G, int nstep
         unsigned long long d = 0;
         int loc[8];
         if (b < nb) {
-            const int r = b / G.b2;
-            d = distinct_steps(block_steps(S, G, r / G.b1, r - (r / G.b1) * G.b1, b - r * G.b2), nsteps, nd);
+            int c0, c1, c2;
+            G.coords(b, c0, c1, c2);
+            d = distinct_steps(block_steps(S, G, c0, c1, c2), nsteps, nd);
         }
 #pragma unroll
         for (int e = 0; e < 8; e++)
@@ -2779,10 +2813,10 @@ __global__ void __launch_bounds__(256, 5) k_drain_update_blocks(uint8_t *__restr
         for (int q = 0; q < NB; q++) {
             const int b = base + q * blockDim.x + threadIdx.x;
             bq[q] = b;
-            const int r = b / G.b2, c0 = r / G.b1;
+            int c0, c1b, c2b;
+            G.coords(b, c0, c1b, c2b);
             ind[q] = c0 >= bxlo && c0 <= bxhi;
             act[q] = b < bend && (ind[q] || !ranged);
-            const int c2b = b - r * G.b2, c1b = r - c0 * G.b1;
             const int i0 = 2 * c0, j0 = 2 * c1b, k0 = 2 * c2b;
             vol[q] = act[q] ? spread_x(in2(i0, 0, G.s0)) & spread_y(in2(j0, 0, G.s1)) & spread_z(in2(k0, 0, G.s2)) : 0u;
             base0[q] = (long long)i0 * sx + (long long)j0 * sy + k0;
@@ -2816,8 +2850,8 @@ __global__ void __launch_bounds__(256, 5) k_drain_update_blocks(uint8_t *__restr
             const int b = bq[q];
             bool changed = false;
             if (act[q]) {
-                const int r = b / G.b2;
-                const int c2b = b - r * G.b2, c0 = r / G.b1, c1b = r - (r / G.b1) * G.b1;
+                int c2b, c0, c1b;
+                G.coords(b, c0, c1b, c2b);
                 const int i0 = 2 * c0, j0 = 2 * c1b, k0 = 2 * c2b;
                 // voxels inside the own box and the reservoir slabs
                 const unsigned v = vol[q];
@@ -3022,7 +3056,8 @@ __global__ void k_fill_i32(int *a, long long n, int v)
 
 __device__ __forceinline__ int block_first_voxel(const BGrid &G, int b, unsigned m)
 {
-    const int c2 = b % G.b2, c1 = (b / G.b2) % G.b1, c0 = b / (G.b2 * G.b1);
+    int c0, c1, c2;
+    G.coords(b, c0, c1, c2);
     const int bit = __ffs(m) - 1;
     const int x = bit >> 2, y = (bit >> 1) & 1, z = bit & 1;
     return ((2 * c0 + x) * G.s1 + 2 * c1 + y) * G.s2 + 2 * c2 + z;
@@ -3093,10 +3128,8 @@ __global__ void k_blk_label_out(const int *__restrict__ P, const uint8_t *__rest
 {
     const int nb = G.b0 * G.b1 * G.b2;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
-        const int r = b / G.b2;
-        const int c2 = b - r * G.b2;
-        const int c0 = r / G.b1;
-        const int c1 = r - c0 * G.b1;
+        int c0, c1, c2;
+        G.coords(b, c0, c1, c2);
         const unsigned m = M[b];
         uint64_t lab = m ? (uint64_t)F[P[b]] : 0;
         if (lut && lab)
