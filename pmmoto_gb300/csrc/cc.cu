@@ -1856,6 +1856,38 @@ __global__ void k_bcc_mark(const uint8_t *__restrict__ M, const int *__restrict_
     }
 }
 
+// k_bcc_mark for two block union-finds of the same grid at once
+// (blockIdx.y picks the set), marking the same face box.
+__global__ void k_bcc_mark2(const uint8_t *__restrict__ Ma, const int *__restrict__ Pa, uint8_t *mark_a,
+                            const uint8_t *__restrict__ Mb, const int *__restrict__ Pb, uint8_t *mark_b, BGrid G,
+                            Box bx, uint8_t bit, int *err)
+{
+    const uint8_t *M = blockIdx.y ? Mb : Ma;
+    const int *P = blockIdx.y ? Pb : Pa;
+    uint8_t *mark = blockIdx.y ? mark_b : mark_a;
+    long long lo[3], nbk[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = bx.lo[d] >> 1;
+        nbk[d] = ((bx.hi[d] + 1) >> 1) - lo[d];
+    }
+    const long long n = nbk[0] * nbk[1] * nbk[2];
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int c2 = (int)(lo[2] + q % nbk[2]), c1 = (int)(lo[1] + (q / nbk[2]) % nbk[1]),
+                  c0 = (int)(lo[0] + q / (nbk[2] * nbk[1]));
+        const int b = (c0 * G.b1 + c1) * G.b2 + c2;
+        const unsigned inbox = spread_x(in2(2 * c0, bx.lo[0], bx.hi[0])) & spread_y(in2(2 * c1, bx.lo[1], bx.hi[1])) &
+                               spread_z(in2(2 * c2, bx.lo[2], bx.hi[2]));
+        if (!(M[b] & inbox))
+            continue;
+        int p = ld(P + b);
+        if (p >= 0)
+            p = find_root(P, p, err);
+        if (p >= 0 && !(mark[p] & bit))
+            atomicOr((unsigned int *)(mark + (p & ~3)), (unsigned int)bit << (8 * (p & 3)));
+    }
+}
+
 // One thread per block: the block's root and marks decide all its voxels at
 // once; kept foreground voxels receive `val`, everything else 0.  A warp
 // covers 32 consecutive blocks, i.e. 64 contiguous voxels of each of the
@@ -2191,48 +2223,96 @@ __global__ void k_grow_masks(Src src, uint8_t *__restrict__ M, int *__restrict__
 // block's starting parent is already in its component; of the others, one
 // lane per distinct parent unites (neighbours with one parent are in one
 // component already).
-__global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, const int *__restrict__ list,
-                             const int *__restrict__ count, const int *__restrict__ off, int *err,
-                             unsigned long long *units)
+// One listed block b of a growing set: its lane's neighbour (q, d) and, once
+// per distinct neighbour parent, the union.
+__device__ __forceinline__ void grow_unite_block(int *P, const uint8_t *__restrict__ M, const BGrid &G, int b,
+                                                 int lane, int d0, int d1, int d2, unsigned tself, unsigned tnb,
+                                                 int *err)
 {
-    int cnt;
-    if (off) {
-        list += off[0];
-        cnt = off[1] - off[0];
-    } else {
-        cnt = *count;
+    int c2, c0, c1;
+    G.coords(b, c0, c1, c2);
+    const unsigned m = M[b];
+    const int pb = ld(P + b);
+    const int a0 = c0 + d0, a1 = c1 + d1, a2 = c2 + d2;
+    const bool valid = (m & tself) && a0 >= 0 && a1 >= 0 && a2 >= 0 && a0 < G.b0 && a1 < G.b1 && a2 < G.b2;
+    const int o = (a0 * G.b1 + a1) * G.b2 + a2;
+    unsigned mo = 0;
+    int po = -1;
+    if (valid) {
+        mo = M[o];
+        po = ld(P + o);
     }
-    if (units && blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0)
-        atomicAdd(units, (unsigned long long)cnt);
+    const bool need = (mo & tnb) && po != pb;
+    const unsigned needs = __ballot_sync(0xffffffffu, need);
+    if (!needs)
+        return;
+    const unsigned same = __match_any_sync(0xffffffffu, need ? po : -2 - lane);
+    if (need && (__ffs(same & needs) - 1) == lane)
+        unite(P, b, o, err);
+}
+
+// A set's listed blocks: step k's precomputed list (off) or the list a mask
+// pass (or the drainage update) filled (count).
+struct UniteList {
+    int *P;
+    const uint8_t *M;
+    const int *list, *count, *off;
+    __device__ __forceinline__ int size(const int *&l) const
+    {
+        if (off) {
+            l = list + off[0];
+            return off[1] - off[0];
+        }
+        l = list;
+        return *count;
+    }
+};
+
+// One warp per listed block of set A, then of set B (two growing sets of the
+// same grid in one launch: their dependent loads overlap), one lane per
+// neighbour (lanes 0-25): every lane loads its neighbour's mask and parent
+// at once.  The parents were flattened after the previous step, so a
+// touching neighbour whose parent equals the block's starting parent is
+// already in its component; of the others, one lane per distinct parent
+// unites (neighbours with one parent are in one component already).
+__global__ void k_grow_unite2(UniteList A, UniteList B, BGrid G, int *err, unsigned long long *units)
+{
+    const int *la = nullptr, *lb = nullptr;
+    const int ca = A.P ? A.size(la) : 0, cb = B.P ? B.size(lb) : 0;
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && ca + cb > 0)
+        atomicAdd(units, (unsigned long long)(ca + cb));
     const int lane = threadIdx.x & 31;
     const int q = lane < 13 ? lane : lane + 1; // offset code (d0 + 1) * 9 + (d1 + 1) * 3 + d2 + 1, 13 skipped
     const int d0 = q / 9 - 1, d1 = (q / 3) % 3 - 1, d2 = q % 3 - 1;
     const unsigned tself = lane < 26 ? touch_bits(d0, d1, d2) : 0u, tnb = touch_bits(-d0, -d1, -d2);
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long it = warp; it < cnt; it += nwarps) {
-        const int b = list[it];
-        int c2, c0, c1;
-        G.coords(b, c0, c1, c2);
-        const unsigned m = M[b];
-        const int pb = ld(P + b);
-        const int a0 = c0 + d0, a1 = c1 + d1, a2 = c2 + d2;
-        const bool valid = (m & tself) && a0 >= 0 && a1 >= 0 && a2 >= 0 && a0 < G.b0 && a1 < G.b1 && a2 < G.b2;
-        const int o = (a0 * G.b1 + a1) * G.b2 + a2;
-        unsigned mo = 0;
-        int po = -1;
-        if (valid) {
-            mo = M[o];
-            po = ld(P + o);
-        }
-        const bool need = (mo & tnb) && po != pb;
-        const unsigned needs = __ballot_sync(0xffffffffu, need);
-        if (!needs)
-            continue;
-        const unsigned same = __match_any_sync(0xffffffffu, need ? po : -2 - lane);
-        if (need && (__ffs(same & needs) - 1) == lane)
-            unite(P, b, o, err);
+    for (long long it = warp; it < (long long)ca + cb; it += nwarps) {
+        if (it < ca)
+            grow_unite_block(A.P, A.M, G, la[it], lane, d0, d1, d2, tself, tnb, err);
+        else
+            grow_unite_block(B.P, B.M, G, lb[it - ca], lane, d0, d1, d2, tself, tnb, err);
     }
+}
+
+// A single set: set B empty.
+__global__ void k_grow_unite(int *P, const uint8_t *__restrict__ M, BGrid G, const int *__restrict__ list,
+                             const int *__restrict__ count, const int *__restrict__ off, int *err,
+                             unsigned long long *units)
+{
+    UniteList A{P, M, list, count, off};
+    const int *la = nullptr;
+    const int ca = A.size(la);
+    if (units && blockIdx.x == 0 && threadIdx.x == 0 && ca > 0)
+        atomicAdd(units, (unsigned long long)ca);
+    const int lane = threadIdx.x & 31;
+    const int q = lane < 13 ? lane : lane + 1;
+    const int d0 = q / 9 - 1, d1 = (q / 3) % 3 - 1, d2 = q % 3 - 1;
+    const unsigned tself = lane < 26 ? touch_bits(d0, d1, d2) : 0u, tnb = touch_bits(-d0, -d1, -d2);
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long it = warp; it < ca; it += nwarps)
+        grow_unite_block(P, M, G, la[it], lane, d0, d1, d2, tself, tnb, err);
 }
 
 size_t grow_sel_bytes(const int64_t *shape)
@@ -2658,6 +2738,101 @@ int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *
 {
     SrcImg src{img, fgval};
     return grow_step(g, src, shape, bc, pad, inlet_box, nullptr, err, st);
+}
+
+// The two growing selections of a drainage radius, up to their inlet marks,
+// in one union launch and one marks launch: the eroded space A (its step k
+// from the precomputed lists when S is given, else from the capped EDT E > T)
+// and the non-wetting phase B (fgval in img, or the list the last drainage
+// update left).  Taken once both are past their first full build and no axis
+// is periodic (no seam twins); otherwise the two steps run one after the
+// other.  Same parents and marks either way: each set's unions only involve
+// its own parents.
+int grow_marks_pair(GrowSel &a, const uint8_t *S, int k, const uint16_t *E, int T, GrowSel &b, const uint8_t *img,
+                    int fgval, const int64_t *shape, const int32_t *bc, const int32_t *pad, const int64_t *inlet_box,
+                    int *err, cudaStream_t st)
+{
+    const bool step_lists = S && a.ev;
+    if (!a.built || !b.built || any_periodic(bc) || (!S && !E)) {
+        if (S)
+            PMG_TRY(grow_marks_step(a, S, k, shape, bc, pad, inlet_box, err, st));
+        else
+            PMG_TRY(grow_marks_erode(a, E, T, shape, bc, pad, inlet_box, err, st));
+        return grow_marks_binary(b, img, fgval, shape, bc, pad, inlet_box, err, st);
+    }
+    PMG_TRY(check_boxes(shape, inlet_box, nullptr));
+    PMG_TRY(ensure_tables());
+    PMG_TRY(ensure_block_tables());
+    const BGrid G = bgrid_of(shape);
+    const int nb = G.b0 * G.b1 * G.b2;
+    const long long n = shape[0] * shape[1] * shape[2];
+    const int *a_off = step_lists ? a.off + k : nullptr;
+    // A's grown blocks
+    if (step_lists) {
+        const SrcStep src{S, k};
+        const int ps__ = prof_begin("k_grow_apply", st);
+        k_grow_apply<SrcStep><<<152 * 8, 256, 0, st>>>(src, a.M, a.P, G, a.ev, a_off, err,
+                                                       prof_units(kUnitsGrowApply));
+        prof_end_units(ps__, kUnitsGrowApply, 4 + 8 * sizeof(*src_elem(src)) + 2 + 4, st);
+        PMG_CHECK_LAUNCH();
+    } else if (S) {
+        const SrcStep src{S, k};
+        PMG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+        const int ps__ = prof_begin("k_grow_masks", st);
+        k_grow_masks<SrcStep><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(src, a.M, a.P, G, a.list, a.count, err);
+        prof_end(ps__, (double)n + (double)nb, st);
+        PMG_CHECK_LAUNCH();
+    } else {
+        const SrcErode src = erode_src(E, T, shape, bc);
+        PMG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+        const int ps__ = prof_begin("k_grow_masks", st);
+        k_grow_masks<SrcErode><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(src, a.M, a.P, G, a.list, a.count,
+                                                                            err);
+        prof_end(ps__, (double)n * 2 + (double)nb, st);
+        PMG_CHECK_LAUNCH();
+    }
+    // B's grown blocks: listed by the last update, or from its new masks
+    if (b.pending) {
+        b.pending = false;
+    } else {
+        const SrcImg src{img, fgval};
+        PMG_CUDA(cudaMemsetAsync(b.count, 0, sizeof(int), st));
+        const int ps__ = prof_begin("k_grow_masks", st);
+        k_grow_masks<SrcImg><<<grid_for(nb, 256, 152LL * 64), 256, 0, st>>>(src, b.M, b.P, G, b.list, b.count, err);
+        prof_end(ps__, (double)n + (double)nb, st);
+        PMG_CHECK_LAUNCH();
+    }
+    {
+        const int ps__ = prof_begin("k_grow_unite[pair]", st);
+        k_grow_unite2<<<152 * 32, 256, 0, st>>>(UniteList{a.P, a.M, step_lists ? a.ev : a.list, a.count, a_off},
+                                                UniteList{b.P, b.M, b.list, b.count, nullptr}, G, err,
+                                                prof_units(kUnitsGrowUnitePair));
+        // per listed block: its list entry, mask and parent, and the masks and
+        // parents of its 26 neighbours
+        prof_end_units(ps__, kUnitsGrowUnitePair, 4 + 5 + 26 * 5, st);
+        PMG_CHECK_LAUNCH();
+    }
+    // inlet marks of both
+    PMG_CUDA(cudaMemsetAsync(a.mark, 0, ((size_t)nb + 3) & ~(size_t)3, st));
+    PMG_CUDA(cudaMemsetAsync(b.mark, 0, ((size_t)nb + 3) & ~(size_t)3, st));
+    if (inlet_box && inlet_box[0] >= 0) {
+        Box bx;
+        for (int d = 0; d < 3; d++) {
+            bx.lo[d] = inlet_box[2 * d];
+            bx.hi[d] = inlet_box[2 * d + 1];
+        }
+        if (bx.size() > 0) {
+            long long nbk = 1;
+            for (int d = 0; d < 3; d++)
+                nbk *= ((bx.hi[d] + 1) >> 1) - (bx.lo[d] >> 1);
+            const int ps__ = prof_begin("k_bcc_mark", st);
+            k_bcc_mark2<<<dim3((unsigned)grid_for(nbk, 256, 1LL << 30), 2), 256, 0, st>>>(
+                a.M, a.P, a.mark, b.M, b.P, b.mark, G, bx, (uint8_t)1, err);
+            prof_end(ps__, (double)nbk * 18, st);
+            PMG_CHECK_LAUNCH();
+        }
+    }
+    return PMG_OK;
 }
 
 int grow_pair_select(GrowSel &a, GrowSel &b, const unsigned long long *b_count, uint8_t *out,

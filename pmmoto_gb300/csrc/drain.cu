@@ -200,11 +200,7 @@ static int porosimetry_run(const uint8_t *pm, uint8_t *out, const int64_t *shape
         // both selections grow along the curve: one pass writes the eroded
         // inlet-connected space constrained by the inlet-connected
         // non-wetting phase (when that phase exists, counted in w.cnt[1])
-        if (Sv)
-            PMG_TRY(grow_marks_step(*g_er, Sv, step, shape, bc, pad, Bx.inlet, w.err, st));
-        else
-            PMG_TRY(grow_marks_erode(*g_er, KC, Te, shape, bc, pad, Bx.inlet, w.err, st));
-        PMG_TRY(grow_marks_binary(*g_nw, mp, 1, shape, bc, pad, Bx.inlet, w.err, st));
+        PMG_TRY(grow_marks_pair(*g_er, Sv, step, KC, Te, *g_nw, mp, 1, shape, bc, pad, Bx.inlet, w.err, st));
         // the selection's x range (w.cnt[4]) limits the dilation to the planes
         // it can reach; the dilation's result range goes to orange
         int *xr = orange ? (int *)(w.cnt + 4) : nullptr;

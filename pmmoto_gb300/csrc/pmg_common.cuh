@@ -51,9 +51,10 @@ void prof_end(int slot, double bytes, cudaStream_t st);
 // Kernels whose work is sized on the device add the units they process to
 // prof_units(id) (one counter per kind of kernel); prof_end_units records the
 // bytes per unit for the profile.
-constexpr int kUnitSlots = 8;
+constexpr int kUnitSlots = 16;
 constexpr int kUnitsCapRows = 0, kUnitsCapMid = 1, kUnitsCapLast = 2, kUnitsDrainUpdate = 3;
 constexpr int kUnitsGrowUniteA = 4, kUnitsGrowUniteB = 5, kUnitsCrossUnite = 6, kUnitsGrowApply = 7;
+constexpr int kUnitsGrowUnitePair = 8;
 unsigned long long *prof_units(int id);
 void prof_end_units(int slot, int id, double bytes_per_unit, cudaStream_t st);
 

@@ -81,6 +81,13 @@ int grow_marks_binary(GrowSel &g, const uint8_t *img, int fgval, const int64_t *
 // (the set: voxels with step S <= k)
 int grow_marks_step(GrowSel &g, const uint8_t *S, int k, const int64_t *shape, const int32_t *bc,
                     const int32_t *pad, const int64_t *inlet_box, int *err, cudaStream_t st);
+// Both growing selections of a drainage radius up to their inlet marks (the
+// eroded space a: step k of S when S is given, else E > T; the non-wetting
+// phase b: fgval in img) in one union launch and one marks launch, once both
+// are built and no axis is periodic; the two steps above otherwise.
+int grow_marks_pair(GrowSel &a, const uint8_t *S, int k, const uint16_t *E, int T, GrowSel &b, const uint8_t *img,
+                    int fgval, const int64_t *shape, const int32_t *bc, const int32_t *pad, const int64_t *inlet_box,
+                    int *err, cudaStream_t st);
 // ... and the inlet selection of a constrained by b (when *b_count > 0) in one
 // pass; kept counts a's inlet-connected voxels.
 // xr (optional): the x range of the output's set (kRangeBig encoding);
