@@ -50,3 +50,18 @@ def test_library_knob_table():
     assert L.pmg_tune_get(b"cc.cross_fused", ctypes.byref(v)) == 0 and v.value == 0
     assert L.pmg_tune_set(b"edt.pair_seg", 1) == _lib.PMG_ERANGE
     assert L.pmg_tune_set(b"no.such", 4) == _lib.PMG_EINVAL
+    # path choices and probe thresholds: their defaults, 0 as a value, the
+    # range ends, a negative value back to the default
+    defaults = {b"edt.path": 0, b"edt.fallback": 96, b"edt.fallback_rows": 2048, b"edt.narrow": 64,
+                b"edt.narrow_rows": 32, b"cc.seam_batched": 1}
+    for name, default in defaults.items():
+        assert L.pmg_tune_get(name, ctypes.byref(v)) == 0 and v.value == default
+        assert L.pmg_tune_set(name, 0) == 0
+        assert L.pmg_tune_get(name, ctypes.byref(v)) == 0 and v.value == 0
+        assert L.pmg_tune_set(name, -1) == 0
+        assert L.pmg_tune_get(name, ctypes.byref(v)) == 0 and v.value == default
+    assert L.pmg_tune_set(b"edt.path", 3) == _lib.PMG_ERANGE
+    assert L.pmg_tune_set(b"edt.fallback", 8193) == 0
+    assert L.pmg_tune_set(b"edt.fallback", 8194) == _lib.PMG_ERANGE
+    assert L.pmg_tune_set(b"edt.fallback", -1) == 0
+    assert L.pmg_tune_set(b"cc.seam_batched", 2) == _lib.PMG_ERANGE
