@@ -1981,7 +1981,7 @@ static BGrid bgrid_of(const int64_t *shape)
 template <class Src>
 static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, const int32_t *pad, bool twins,
                      int *P, uint8_t *M, int *err, cudaStream_t st, bool flatten = true, int *Pl = nullptr,
-                     int *dirty = nullptr)
+                     int *dirty = nullptr, int *hard_buf = nullptr)
 {
     PMG_TRY(ensure_tables());
     PMG_TRY(ensure_block_tables());
@@ -2006,9 +2006,11 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
     } else {
         const long long border = (long long)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) *
                                  ((G.b2 + kT2 - 1) / kT2) * kBorder;
-        // list of the border blocks that need unions, and its length
-        int *hard = nullptr;
-        PMG_TRY(scratch_alloc((void **)&hard, sizeof(int) * (size_t)(border + 64), st));
+        // list of the border blocks that need unions, and its length (in the
+        // caller's buffer of border + 64 ints, if given)
+        int *hard = hard_buf;
+        if (!hard)
+            PMG_TRY(scratch_alloc((void **)&hard, sizeof(int) * (size_t)(border + 64), st));
         int *nhard = hard + border + 32;
         PMG_CUDA(cudaMemsetAsync(nhard, 0, sizeof(int), st));
         {
@@ -2028,7 +2030,8 @@ static int bcc_build(const Src &src, const int64_t *shape, const int32_t *bc, co
             prof_end_units(ps__, kUnitsCrossUnite, 4 + 1 + 13 + 8, st);
         }
         PMG_CHECK_LAUNCH();
-        PMG_TRY(scratch_free(hard, st));
+        if (!hard_buf)
+            PMG_TRY(scratch_free(hard, st));
     }
     if (twins && any_periodic(bc)) {
         const int ps__ = prof_begin("k_bcc_twins", st);
@@ -2898,7 +2901,9 @@ size_t shrink_sel_bytes(const int64_t *shape)
     const size_t nb = (size_t)G.b0 * G.b1 * G.b2;
     const size_t a = (nb + 255) & ~(size_t)255;
     const size_t nt = (size_t)((G.b0 + kT0 - 1) / kT0) * ((G.b1 + kT1 - 1) / kT1) * ((G.b2 + kT2 - 1) / kT2);
-    return a * 4 * 2 + a * 2 + ((nt * 4 + 255) & ~(size_t)255) + 256;
+    // P, Pl, M, mark, per-tile flags, the cross-tile list (kBorder per tile + 64)
+    return a * 4 * 2 + a * 2 + ((nt * 4 + 255) & ~(size_t)255) + (((nt * kBorder + 64) * 4 + 255) & ~(size_t)255) +
+           256;
 }
 
 void shrink_sel_init(ShrinkSel &g, void *mem, const int64_t *shape)
@@ -2917,6 +2922,8 @@ void shrink_sel_init(ShrinkSel &g, void *mem, const int64_t *shape)
     g.mark = (uint8_t *)p;
     p += a;
     g.dirty = (int *)p;
+    p += (nt * 4 + 255) & ~(size_t)255;
+    g.hard = (int *)p;
     g.ntiles = (int)nt;
     g.built = false;
 }
@@ -2930,10 +2937,10 @@ int shrink_marks_binary(ShrinkSel &g, const uint8_t *img, int fgval, const int64
         PMG_CUDA(cudaMemsetAsync(g.dirty, 0, sizeof(int) * (size_t)g.ntiles, st));
     if (g.built) {
         // the producer of the changes kept the block masks current
-        PMG_TRY(bcc_build(SrcMask{g.M}, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, g.dirty));
+        PMG_TRY(bcc_build(SrcMask{g.M}, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, g.dirty, g.hard));
     } else {
         SrcImg src{img, fgval};
-        PMG_TRY(bcc_build(src, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, nullptr));
+        PMG_TRY(bcc_build(src, shape, bc, pad, true, g.P, g.M, err, st, false, g.Pl, nullptr, g.hard));
     }
     g.built = true;
     return bcc_marks(shape, inlet_box, outlet_box, g.P, g.M, g.mark, err, st);

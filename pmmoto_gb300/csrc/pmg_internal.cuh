@@ -104,6 +104,7 @@ struct ShrinkSel {
     uint8_t *M = nullptr;
     uint8_t *mark = nullptr;
     int *dirty = nullptr; // per tile: changed since the last step
+    int *hard = nullptr;  // the cross-tile union list (kBorder per tile + 64 ints)
     int ntiles = 0;
     bool built = false;
 };
