@@ -7,7 +7,8 @@ Builds, into ``oracle/_ref/`` (git-ignored):
   multiply-add is fused, and with OpenMP over independent lines.
 * ``libpmref.so`` -- PMMoTo's own C++ line kernels compiled from the
   reference source tree through ``ref_shim.cpp``; built only where the
-  reference sources are present (``PMMOTO_REF_SRC`` or the default path).
+  reference sources are present (the ``PMMOTO_REF_SRC`` environment
+  variable, or the path the caller passes).
 
 Run ``python -m oracle.build`` or call :func:`build_oracle`.
 """
@@ -20,7 +21,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("PMMOTO_REF_SRC", "/root/reference/src/pmmoto")
+REF_SRC = os.environ.get("PMMOTO_REF_SRC")
 
 
 def _run(cmd):
@@ -43,11 +44,16 @@ def build_oracle(force: bool = False) -> str:
     return so
 
 
-def build_reference(force: bool = False) -> str | None:
-    """Compile the reference's own line kernels (only where its sources exist)."""
-    dist = os.path.join(REF_SRC, "filters", "distance")
-    core = os.path.join(REF_SRC, "core")
-    parts = os.path.join(REF_SRC, "particles")
+def build_reference(force: bool = False, ref_src: str | None = None) -> str | None:
+    """Compile the reference's own line kernels from its source tree
+    (``ref_src``, else ``$PMMOTO_REF_SRC``); None when no tree is given or
+    it has no line kernels."""
+    ref_src = ref_src or REF_SRC
+    if not ref_src:
+        return None
+    dist = os.path.join(ref_src, "filters", "distance")
+    core = os.path.join(ref_src, "core")
+    parts = os.path.join(ref_src, "particles")
     if not os.path.isdir(dist):
         return None
     os.makedirs(OUT, exist_ok=True)

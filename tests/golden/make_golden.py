@@ -32,7 +32,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import refshim  # noqa: E402
 
-REF_TESTS = os.environ.get("PMMOTO_REF_TESTS", "/root/reference/tests")
+# the reference's test directory (its fixture scripts are read in place)
+REF_TESTS = os.environ.get("PMMOTO_REF_TESTS")
 
 
 def sha(a: np.ndarray) -> str:
@@ -40,6 +41,8 @@ def sha(a: np.ndarray) -> str:
 
 
 def main():
+    if not REF_TESTS or not os.path.isdir(REF_TESTS):
+        raise SystemExit("set PMMOTO_REF_TESTS to the reference's tests directory")
     pm = refshim.load()
     if pm is None:
         raise SystemExit("reference not importable; install it under baseline/_ref first")

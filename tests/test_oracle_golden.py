@@ -122,7 +122,11 @@ def test_sphere_kat(golden):
 # ---------------------------------------------------------------------------
 
 def _reflib():
-    so = OB.build_reference()
+    # built by the build recipe where the reference sources are mounted, or
+    # from $PMMOTO_REF_SRC
+    so = os.path.join(OB.OUT, "libpmref.so")
+    if not os.path.exists(so):
+        so = OB.build_reference()
     if so is None or not os.path.exists(so):
         pytest.skip("reference sources not available to build libpmref")
     L = ctypes.CDLL(so)
