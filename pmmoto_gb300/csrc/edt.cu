@@ -1035,7 +1035,6 @@ __global__ void __launch_bounds__(256) k_env_pair(const float *__restrict__ fin,
     const int n = g0.n;
     const long long st = g0.stride;
     const int nseg = (n + seglen - 1) / seglen;
-    const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
     const uint32_t big = kClamp * 0x10001u;
     const float2 kOut = make_float2(-1.0f, -1.0f); // marks a position outside the line
     for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < npairs * nseg;
@@ -1184,7 +1183,6 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
     const int n = (int)Ls.s2;
     const int ntx = (n + kRowsTX - 1) / kRowsTX;
     const long long ntiles = ((nlines + 63) / 64) * ntx;
-    const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
     const uint32_t big = kClamp * 0x10001u;
     const int tid = threadIdx.x;
     // rows start on 16-byte boundaries when the row length is a multiple of 4
@@ -1247,7 +1245,6 @@ __global__ void __launch_bounds__(256) k_env_pair_rows(const float *__restrict__
             int need0 = 0, need1 = 0;
             const long long lia = li0 + 2 * pr;
             if (2 * pr < rows && xs < xe) {
-                const long long rbase = sbase[2 * pr];
                 uint32_t win[R];
 #pragma unroll
                 for (int s2 = 0; s2 < R; s2++)
