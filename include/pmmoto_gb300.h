@@ -362,7 +362,11 @@ int pmg_set_iteration_cap(int32_t cap);
  * pass to the float envelope; 0 always, 8193 never; defaults 96 and 2048),
  * "edt.narrow" and "edt.narrow_rows" (probe samples the +-8 window does not
  * finish, below which the pass runs the +-8 window instead of the +-12 one;
- * 0 never; defaults 64 and 32), "cc.seam_batched" (periodic merge: the
+ * 0 never; defaults 64 and 32), "edt.wide" (probe samples the +-24 window
+ * does not finish, below which a strided pass of at least 131,072 lines that
+ * the +-12 window would hand to the float envelope runs the +-24 window;
+ * 0 never, 8193 always and for any line count; default 1024),
+ * "cc.seam_batched" (periodic merge: the
  * seams of all periodic features deduplicated in one sort, 1, or one
  * feature at a time, 0; default 1; one at a time is also taken when labels
  * need more than 29 bits).  A negative value restores the default, and so

@@ -577,22 +577,29 @@ __device__ __forceinline__ void evaluate(Stack &S, const float *line, long long 
 // finish.  Choice 0 runs the +-8 line-pair kernels, 1 the +-12 ones, 2 the
 // float envelope on every line; the kernels of the other choices return at
 // once.  Without a probe the +-12 window runs.
+// count[2] counts those the +-24 window does not finish: below thr24 (the
+// strided passes only) the +-24 kernel takes a pass the +-12 one would
+// leave to the envelope (choice 3).
 struct Probe {
     const int *count;
-    int thr8, thr12;
+    int thr8, thr12, thr24;
     __device__ __forceinline__ int choice() const
     {
         if (!count)
             return 1;
-        return count[0] < thr8 ? 0 : (count[1] < thr12 ? 1 : 2);
+        if (count[0] < thr8)
+            return 0;
+        if (count[1] < thr12)
+            return 1;
+        return count[2] < thr24 ? 3 : 2;
     }
 };
 
 template <int W>
 __host__ __device__ constexpr int window_choice()
 {
-    static_assert(W == 8 || W == 12, "windows of +-8 and +-12");
-    return W == 8 ? 0 : 1;
+    static_assert(W == 8 || W == 12 || W == 24, "windows of +-8, +-12 and +-24");
+    return W == 8 ? 0 : W == 12 ? 1 : 3;
 }
 
 __global__ void k_envelope(const float *__restrict__ fin, float *__restrict__ fout, Lines Ls, float res,
@@ -926,7 +933,8 @@ __global__ void __launch_bounds__(256) k_env_slow(const float *__restrict__ fin,
                                                   const int *__restrict__ count, int cap, Probe probe)
 {
     // the window of the kernel that deferred the voxels
-    const int W = probe.choice() == 0 ? 8 : 12;
+    const int ch = probe.choice();
+    const int W = ch == 0 ? 8 : ch == 3 ? 24 : 12;
     const int cnt = min(*count, cap);
     const int n = line_addr(Ls, 0).n;
     const float kmax = 16777216.0f - (float)(3 * n) * (float)(3 * n);
@@ -969,7 +977,7 @@ __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin
     if (nl <= 0)
         return;
     const int n = line_addr(Ls, 0).n;
-    int c8 = 0, c12 = 0;
+    int c8 = 0, c12 = 0, c24 = 0;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < kProbe; s += gridDim.x * blockDim.x) {
         const long long li = (long long)(((unsigned long long)s * (unsigned long long)nl) / kProbe);
         const int x = (int)(((unsigned)s * 2654435761u) % (unsigned)n);
@@ -979,7 +987,7 @@ __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin
         float best = fmul(line[x * st], inv_a);
         bool bad = !(best < 65000.0f && best == truncf(best));
 #pragma unroll
-        for (int d = 1; d <= 12; d++) {
+        for (int d = 1; d <= 24; d++) {
             const float dd = (float)(d * d);
             if (x - d >= 0) {
                 const float k = fmul(line[(x - d) * st], inv_a);
@@ -993,16 +1001,21 @@ __global__ void __launch_bounds__(256) k_env_probe(const float *__restrict__ fin
             }
             if (d == 8)
                 c8 += (bad || best > 81.0f) ? 1 : 0;
+            if (d == 12)
+                c12 += (bad || best > 169.0f) ? 1 : 0;
         }
-        c12 += (bad || best > 169.0f) ? 1 : 0;
+        c24 += (bad || best > 625.0f) ? 1 : 0;
     }
     c8 = __reduce_add_sync(0xffffffffu, c8);
     c12 = __reduce_add_sync(0xffffffffu, c12);
+    c24 = __reduce_add_sync(0xffffffffu, c24);
     if ((threadIdx.x & 31) == 0) {
         if (c8)
             atomicAdd(count, c8);
         if (c12)
             atomicAdd(count + 1, c12);
+        if (c24)
+            atomicAdd(count + 2, c24);
     }
 }
 
@@ -1511,7 +1524,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
         long long fcap = nl, slow_cap = 0;
         if (!flag_buf) {
             slow_cap = std::min<long long>(nl * n / 16 + 1024, 1LL << 27);
-            const size_t head = ((sizeof(int) * (size_t)(2 * nl + 4)) + 15) & ~(size_t)15;
+            const size_t head = ((sizeof(int) * (size_t)(2 * nl + 5)) + 15) & ~(size_t)15;
             void *mem = nullptr;
             PMG_TRY(scratch_alloc(&mem, head + sizeof(unsigned long long) * (size_t)slow_cap, st));
             flag = (int *)mem;
@@ -1520,14 +1533,19 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
         } else {
             fcap = flag_cap / 2;
             probe = flag_buf + fcap;
-            const uintptr_t lo = ((uintptr_t)(probe + 3) + 15) & ~(uintptr_t)15, hi = (uintptr_t)(flag_buf + flag_cap);
+            const uintptr_t lo = ((uintptr_t)(probe + 4) + 15) & ~(uintptr_t)15, hi = (uintptr_t)(flag_buf + flag_cap);
             slow = (unsigned long long *)lo;
             slow_cap = hi > lo ? (long long)((hi - lo) / sizeof(unsigned long long)) : 0;
         }
-        slow_cnt = probe + 2;
+        slow_cnt = probe + 3;
         const bool rows_pass = Ls.ax == 2;
+        // the +-24 window only for strided passes of many lines (on small
+        // volumes its 106-register grid runs too few warps and the envelope
+        // is faster), unless its threshold is 8193 (always)
+        const int wide = tune_value(kTuneEdtWide);
         const Probe pr{probe, tune_value(rows_pass ? kTuneEdtNarrowRows : kTuneEdtNarrow),
-                       tune_value(rows_pass ? kTuneEdtFallbackRows : kTuneEdtFallback)};
+                       tune_value(rows_pass ? kTuneEdtFallbackRows : kTuneEdtFallback),
+                       rows_pass || (nl < (1LL << 17) && wide < 8193) ? 0 : wide};
         // a caller-supplied flag buffer smaller than the line count is used
         // for one block of rows (lines along the first other axis) at a time
         const int rows = flag_buf ? (int)std::min<long long>(Ls.nb1, std::max<long long>(1, fcap / Ls.nb2))
@@ -1543,8 +1561,8 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
             C.nb1 = std::min(rows, Ls.nb1 - r0);
             const long long nc = C.count();
             s = cudaMemsetAsync(flag, 0, sizeof(int) * (size_t)nc, st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
-            if (s == PMG_OK) // the probe's two counts and the deferred count
-                s = cudaMemsetAsync(probe, 0, 3 * sizeof(int), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
+            if (s == PMG_OK) // the probe's three counts and the deferred count
+                s = cudaMemsetAsync(probe, 0, 4 * sizeof(int), st) == cudaSuccess ? PMG_OK : PMG_ECUDA;
             if (s == PMG_OK) {
                 const int ps__ = prof_begin("k_env_probe", st);
                 k_env_probe<<<kProbe / 256, 256, 0, st>>>(fin, C, 1.0f / (res * res), probe);
@@ -1565,6 +1583,10 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
                                                                 flag, seg, pr, slow, slow_cnt, (int)slow_cap);
                     k_env_pair<12, kAhead><<<grid, 256, 0, st>>>(fin, fout, C, a, 1.0f / a, cfg.periodic ? 1 : 0,
                                                                  form, flag, seg, pr, slow, slow_cnt, (int)slow_cap);
+                    if (pr.thr24 > 0)
+                        k_env_pair<24, kAhead><<<grid, 256, 0, st>>>(fin, fout, C, a, 1.0f / a,
+                                                                     cfg.periodic ? 1 : 0, form, flag, seg, pr, slow,
+                                                                     slow_cnt, (int)slow_cap);
                     prof_end(ps__, (double)nc * n * 8, st);
                 } else if (contiguous && !(C.nb2 & 1) && !(C.b2lo & 1)) {
                     // row pairs through shared-memory tiles
@@ -1644,7 +1666,7 @@ int launch_envelope(const float *fin, float *fout, const Lines &Ls, float res,
     {
         const int ps__ = prof_begin(redo ? "k_envelope_redo" : "k_envelope", st);
         k_envelope<<<grid_for(Ls.count(), block, redo ? 152LL * 8 : 1LL << 30), block, smem, st>>>(
-            fin, fout, Ls, res, cfg, num_hull, form, me, redo, Probe{nullptr, 0, 0});
+            fin, fout, Ls, res, cfg, num_hull, form, me, redo, Probe{nullptr, 0, 0, 0});
         prof_end(ps__, redo ? 0.0 : (double)Ls.count() * n * 4 + (form == PMG_EDT_MORPH ? (double)Ls.count() * me.o2 : (double)Ls.count() * n * 4), st);
     }
     PMG_CHECK_LAUNCH();

@@ -61,7 +61,7 @@ void prof_end_units(int slot, int id, double bytes_per_unit, cudaStream_t st);
 // Launch parameters an autotuner may change at run time (pmg_tune_set):
 // results never depend on them, only speed.  Read once per launch.
 enum TuneKnob { kTuneEdtPairSeg = 0, kTuneEdtPairCtas, kTuneEdtRowsCtas, kTuneCcCrossFused, kTuneEdtPath, kTuneEdtFallback, kTuneEdtFallbackRows, kTuneEdtNarrow, kTuneEdtNarrowRows,
-               kTuneCcSeamBatched, kTuneKnobs };
+               kTuneCcSeamBatched, kTuneEdtWide, kTuneKnobs };
 int tune_value(int knob);
 
 // Validate a padded single-rank geometry: positive shape, boundary codes in

@@ -89,8 +89,9 @@ static const TuneSpec g_tune_spec[kTuneKnobs] = {
     {"edt.narrow", 64, 0, 8193},        // probe samples (of 8192) below which a strided pass takes the +-8 window
     {"edt.narrow_rows", 32, 0, 8193},   // the same for the contiguous (row) pass
     {"cc.seam_batched", 1, 0, 1},       // periodic merge: all features' seams in one sort (1) or one by one (0)
+    {"edt.wide", 1024, 0, 8193},        // probe samples (of 8192) below which a strided pass takes the +-24 window
 };
-static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}, {0}, {0}, {96}, {2048}, {64}, {32}, {1}};
+static std::atomic<int> g_tune[kTuneKnobs] = {{256}, {32}, {16}, {0}, {0}, {96}, {2048}, {64}, {32}, {1}, {1024}};
 
 int tune_value(int knob) { return knob >= 0 && knob < kTuneKnobs ? g_tune[knob].load() : 0; }
 

@@ -47,23 +47,24 @@ def _wide_pore_media():
 
 @pytest.mark.parametrize("per", [(True, True, True), (True, False, True), (False, False, False)])
 def test_envelope_paths_agree_on_wide_pores(per):
-    """The windowed passes with the +-12 and the +-8 window (deferred voxels
-    scanned past the window), the same passes handed to the float envelope
-    by the probe, the exact integer stream and the float envelope give the
-    oracle's bits."""
+    """The windowed passes with the +-12, +-8 and (strided) +-24 windows
+    (deferred voxels scanned past the window), the same passes handed to the
+    float envelope by the probe, the exact integer stream and the float
+    envelope give the oracle's bits."""
     from pmmoto_gb300 import tune
     from pmmoto_gb300.filters import distance as D
 
-    names = ("edt.path", "edt.fallback", "edt.fallback_rows", "edt.narrow", "edt.narrow_rows")
+    names = ("edt.path", "edt.fallback", "edt.fallback_rows", "edt.narrow", "edt.narrow_rows", "edt.wide")
     try:
         for img in _wide_pore_media():
             want = O.edt3d(img, periodic=per, squared=True)
             assert want.max() > 14 ** 2  # the scans pass the window
-            for path, thr, narrow in ((0, 8193, 0), (0, 8193, 8193), (0, 0, 0), (1, 8193, 0), (2, 8193, 0)):
-                for name, v in zip(names, (path, thr, thr, narrow, narrow)):
+            for path, thr, narrow, wide in ((0, 8193, 0, 0), (0, 8193, 8193, 0), (0, 0, 0, 0), (0, 0, 0, 8193),
+                                            (1, 8193, 0, 0), (2, 8193, 0, 0)):
+                for name, v in zip(names, (path, thr, thr, narrow, narrow, wide)):
                     tune._set_lib(name, v)
                 np.testing.assert_array_equal(D.edt3d(img, periodic=per, squared=True), want,
-                                              err_msg=f"path {path} fallback {thr} narrow {narrow}")
+                                              err_msg=f"path {path} fallback {thr} narrow {narrow} wide {wide}")
     finally:
         for name in names:
             tune._set_lib(name, -1)

@@ -53,7 +53,7 @@ def test_library_knob_table():
     # path choices and probe thresholds: their defaults, 0 as a value, the
     # range ends, a negative value back to the default
     defaults = {b"edt.path": 0, b"edt.fallback": 96, b"edt.fallback_rows": 2048, b"edt.narrow": 64,
-                b"edt.narrow_rows": 32, b"cc.seam_batched": 1}
+                b"edt.narrow_rows": 32, b"cc.seam_batched": 1, b"edt.wide": 1024}
     for name, default in defaults.items():
         assert L.pmg_tune_get(name, ctypes.byref(v)) == 0 and v.value == default
         assert L.pmg_tune_set(name, 0) == 0
