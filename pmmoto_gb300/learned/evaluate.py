@@ -4,7 +4,7 @@
 
 For each held-out medium, four curves over the same 64 radii:
 
-* dense   -- all 64 radii evaluated exactly (the judge of curve error);
+* dense   -- all 64 radii evaluated exactly (the curve errors are measured against it);
 * learned -- ``LearnedSchedule`` (at most 12 exact radii, dense fallback);
 * uniform -- 12 evenly spaced exact radii, linear fill (no network);
 * predicted -- the network's curve alone, no exact radius.

@@ -7,7 +7,7 @@ has not seen:
   has without a network) on held-out GRF media;
 * the learned schedule evaluates at most 12 radii exactly (no fallback on
   these media) and returns a full, monotone 64-point curve in [0, 1];
-* the dense reference it is judged against is the exact sweep, checked
+* the dense curve it is compared with is the exact sweep, checked
   bit for bit elsewhere (test_gpu_large.py, test_gpu_workflows.py).
 """
 
